@@ -1,0 +1,375 @@
+"""Benchmark of the headless path-tracing hot path (one JSON line on rank 0).
+
+Workload (one "step"): the mid-size scene — ~260k instanced triangles in 200
+instances of 6 seeded meshes, 32 emissive triangles, thin lens — rendered at
+1024x1024 with 128 samples per pixel and at most 8 bounces, FP32 running-mean
+accumulation.  Synthetic, seeded scene data (pt_gb300.scenes.mid_scene).
+
+  value   Mpath-segs/s of the device render with the scene and image resident
+          in HBM: path segments (primary + extension rays, each with its
+          shading and NEE shadow ray) / device time (CUDA events on the render
+          stream), summed over the timed steps.  L2 is flushed (512 MiB write)
+          between steps, outside the event pairs.
+  e2e     the same metric through the C ABI with host buffers: each step
+          uploads the packed scene from pinned host memory, builds the BVH,
+          renders and reads the image back to host memory.
+  roofline  algorithmic bytes per segment (B_seg, fixed per scene from the
+          oracle's BVH2 visit counts) x segments / device time, against the
+          measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (the C++ restatement of the reference's shader
+          math, OpenMP over pixels) on a bounded sample of the same workload.
+
+--impl reference runs the reference's CPU implementation of the path on the
+host cores: the reference's Vulkan tracer cannot run on this machine, so this
+arm times the oracle port with all host threads.
+
+Multi-GPU (torchrun): replicas with disjoint sample ranges (rank r renders
+samples [r*S, (r+1)*S)), weak scaling, no data-path collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WIDTH, HEIGHT, SPP, BOUNCES = 1024, 1024, 128, 8
+WORKLOAD = "mid scene: 1024x1024, 128 spp, max 8 bounces, ~260k tris / 200 instances / 6 meshes, 32 emitters, thin lens"
+
+# Algorithmic bytes per path segment of the mid scene:
+#   B_seg = 128 (path state r/w: the reference's 16-u32 queue item each way)
+#         + 332 (hit fetch: InstanceData 128 + PbrMaterial 96 + 3 indices 12 + 3 vertices 96)
+#         + p_nee * (40 + 24 + 128 + 96 + 96) (light bin, emitter bin, instance, 3 vertices, material)
+#         + (N_node * 64 + N_tri * 36) * (1 + p_nee)
+# with N_node, N_tri the mean interior-node visits and triangle tests per ray
+# of the oracle's binned-SAH BVH2 over the first sample of the image, and
+# p_nee the shadow rays per segment (measured by tests/test_bseg.py).
+BSEG = {"mid": {"n_node": None, "n_tri": None, "p_nee": None}}
+
+
+def bseg_bytes(m: dict) -> float | None:
+    if m["n_node"] is None:
+        return None
+    p = m["p_nee"]
+    return 128 + 332 + p * (40 + 24 + 128 + 96 + 96) + (m["n_node"] * 64 + m["n_tri"] * 36) * (1 + p)
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks every 200 ms while running."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", "--query-gpu=" + ",".join(self.FIELDS), "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == len(self.FIELDS):
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[0]) for r in self.rows if num(r[0]) is not None]
+        mx = [num(r[1]) for r in self.rows if num(r[1]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for name, v in zip(names, r[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def make_scene(workdir: Path):
+    import pt_gb300 as P
+    from pt_gb300 import scenes
+    path = scenes.mid_scene(workdir / "mid", seed=1)
+    hs = P.HostScene.load(path)
+    return hs
+
+
+def cpu_baseline(view, params_fn, seconds_target: float = 15.0) -> dict:
+    """Oracle port on all host threads over a bounded sample (rows of the first spp)."""
+    import oracle
+    threads = os.cpu_count() or 1
+    osc = oracle.OracleScene(view)
+    p = params_fn(1)
+    # bands of 32 rows taken alternately below and above the image centre
+    # until about seconds_target of CPU time has been spent
+    segs, dt, rows_done = 0, 0.0, 0
+    lo = hi = HEIGHT // 2
+    while dt < seconds_target and rows_done < HEIGHT:
+        if (rows_done // 32) % 2 == 0 and hi < HEIGHT:
+            band = (hi, min(HEIGHT, hi + 32))
+            hi = band[1]
+        else:
+            band = (max(0, lo - 32), lo)
+            lo = band[0]
+        t0 = time.perf_counter()
+        _, st = osc.render(p, rows=band, threads=threads)
+        dt += time.perf_counter() - t0
+        segs += st.segments
+        rows_done += band[1] - band[0]
+    return {"value": segs / dt / 1e6, "unit": "Mpath-segs/s", "cores": threads, "kind": "port",
+            "sample": f"mid scene, sample 0 of rows {lo}-{hi - 1} of 1024x1024 ({segs} segments, {dt:.1f} s)",
+            "segments": int(segs), "seconds": dt}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as td:
+        hs = make_scene(Path(td))
+        view = hs.pack()
+        base = cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES), seconds_target=float(args.cpu_seconds))
+        values = []
+        for _ in range(args.warmup):
+            cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES), seconds_target=2.0)
+        for _ in range(args.steps):
+            values.append(cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES),
+                                       seconds_target=float(args.cpu_seconds))["value"])
+        v = statistics.median(values)
+        line = {"metric": METRIC, "value": v, "unit": "Mpath-segs/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+                "config": {"workload": WORKLOAD, "l2": "n/a (CPU)"},
+                "cpu_baseline": {"value": v, "unit": "Mpath-segs/s", "cores": base["cores"], "kind": "port",
+                                 "sample": base["sample"] + "; the reference's Vulkan tracer is unavailable on this box "
+                                                           "(no graphics stack), so its CPU restatement is timed"},
+                "e2e": {"value": v, "unit": "Mpath-segs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+
+
+METRIC = "time to MSE≤1e-3 vs FP64 ref: denoised vs plain (1 GB300); Mpath-segs/s"
+
+
+def pinned_view(view):
+    """Copy every array of a packed scene view into pinned host memory (torch)."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from pt_gb300 import abi, view_arrays
+    arrs = view_arrays(view)
+    keep = []
+
+    def pin(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        keep.append(t)
+        return t.data_ptr()
+
+    v = abi.SceneView()
+    v.vertices = C.cast(pin(arrs["vertices"]), C.POINTER(C.c_float))
+    v.vertex_count = view.vertex_count
+    v.indices = C.cast(pin(arrs["indices"]), C.POINTER(C.c_uint32))
+    v.index_count = view.index_count
+    v.meshes = C.cast(pin(arrs["meshes"]), C.POINTER(abi.MeshRange))
+    v.mesh_count = view.mesh_count
+    v.instances = C.cast(pin(arrs["instances"]), C.POINTER(abi.InstanceData))
+    v.instance_mesh = C.cast(pin(arrs["instance_mesh"]), C.POINTER(C.c_uint32))
+    v.instance_world_to_object = C.cast(pin(arrs["w2o"]), C.POINTER(C.c_float))
+    v.instance_opaque = C.cast(pin(arrs["opaque"]), C.POINTER(C.c_uint8))
+    v.instance_count = view.instance_count
+    v.materials = C.cast(pin(arrs["materials"]), C.POINTER(abi.Material))
+    v.material_count = view.material_count
+    v.light_words = C.cast(pin(arrs["light"]), C.POINTER(C.c_uint32))
+    v.light_word_count = view.light_word_count
+    v.light_count = view.light_count
+    for k in range(3):
+        v.environment_colour[k] = view.environment_colour[k]
+    nbytes = sum(a.nbytes for a in arrs.values() if hasattr(a, "nbytes"))
+    return v, keep, nbytes
+
+
+def run_ours(args) -> None:
+    import numpy as np
+    import torch
+    import pt_gb300 as P
+    from pt_gb300 import abi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    device_index = local
+
+    td = tempfile.TemporaryDirectory()
+    hs = make_scene(Path(td.name))
+    view = hs.pack()
+    pview, keep, scene_bytes = pinned_view(view)
+    ctx = P.Context(device_index)
+    ctx.upload(view)
+    info = ctx.build_accel()
+    first = rank * SPP
+
+    def params(n=SPP, start=first):
+        return hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=start, kernel=args.kernel)
+
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device_index}")
+
+    def l2_flush():
+        flush.zero_()
+        torch.cuda.synchronize()
+
+    # warm-up (also gives the deterministic segment count of one step)
+    st = None
+    for _ in range(max(args.warmup, 1)):
+        st = ctx.render(params())
+    segs_per_step = st.segments
+    launches_per_step = st.kernel_launches
+
+    # ---- device-resident timing
+    dev_ms = []
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with ClockSampler(device_index) as clocks:
+        for _ in range(args.steps):
+            l2_flush()
+            s = ctx.render(params())
+            if s.segments != segs_per_step:
+                raise RuntimeError("segment count changed between identical renders")
+            dev_ms.append(s.milliseconds)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    t_dev = sum(dev_ms) / 1000.0
+    if dist:
+        t = torch.tensor([t_dev], device=f"cuda:{device_index}")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        t_dev = float(t.item())
+    total_segs = segs_per_step * args.steps * world
+    value = total_segs / t_dev / 1e6
+
+    # ---- end to end through the C ABI with host buffers
+    img = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.float32).pin_memory()
+    e2e_ctx = P.Context(device_index)
+    e2e_ctx.upload(pview)
+    e2e_ctx.build_accel()
+    e2e_ctx.render(params(4))
+    e2e_ctx.read_image(out=img.numpy())
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_ctx.upload(pview)
+        e2e_ctx.build_accel()
+        e2e_ctx.render(params(), stats=False)
+        e2e_ctx.read_image(out=img.numpy())
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - e0
+    if dist:
+        t = torch.tensor([t_e2e], device=f"cuda:{device_index}")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e_value = total_segs / t_e2e / 1e6
+    e2e_ctx.close()
+
+    if rank == 0:
+        peaks = measured_peaks()
+        b = bseg_bytes(BSEG["mid"])
+        achieved = (b * segs_per_step / (t_dev / args.steps) / 1e9) if b else None
+        traffic = None
+        tfile = ROOT / "profiles" / "traffic.json"
+        if tfile.exists():
+            traffic = json.loads(tfile.read_text()).get("mid_megakernel_bytes_per_launch")
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": traffic,
+                "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)" if peaks["source"] == "measured" else "fallback",
+                "bytes_per_segment": b}
+        base = cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES), seconds_target=float(args.cpu_seconds)) \
+            if not args.no_cpu else None
+        line = {"metric": METRIC, "value": value, "unit": "Mpath-segs/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB write, outside the event pairs)",
+                           "parallelism": f"replicas x{world} (disjoint sample ranges)", "kernel": "megakernel",
+                           "segments_per_step": int(segs_per_step), "accel_build_ms": info.build_ms},
+                "e2e": {"value": e2e_value, "unit": "Mpath-segs/s", "h2d_bytes_per_step": int(scene_bytes),
+                        "d2h_bytes_per_step": int(HEIGHT * WIDTH * 16), "ms_per_step": 1000.0 * t_e2e / args.steps,
+                        "includes": "scene upload + BVH build + render + image read-back"},
+                "gpu_launches": int(launches_per_step * args.steps),
+                "roofline": roof, "cpu_baseline": base, "clocks": clocks.summary(),
+                "wall_s_timed_region": wall}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    td.cleanup()
+    if dist:
+        tdist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--kernel", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

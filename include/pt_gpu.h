@@ -1,0 +1,234 @@
+/*
+ * pt_gpu.h — C ABI of the GB300 path-tracing library (libptgpu.so).
+ *
+ * This header is the drop-in boundary for pt's headless path-tracing path.
+ * Each entry point names the interface of the reference (anveba/pt) that it
+ * replaces, as file:line within that project.  No C++ or torch types cross
+ * this boundary: plain pointers, sizes and status codes only.
+ *
+ * Ownership: the caller owns every host array passed in (borrowed for the
+ * duration of the call only); a pt_ctx owns all device memory it allocates;
+ * results are copied into caller buffers.  A pt_ctx is thread-compatible
+ * (one thread at a time), not thread-safe.  No exception crosses the ABI:
+ * every call returns a pt_status and pt_last_error() explains the last one.
+ */
+#ifndef PT_GPU_H_INCLUDED
+#define PT_GPU_H_INCLUDED
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PT_ABI_VERSION 1
+
+/* Status codes (0 = ok, < 0 = error class).  The reference throws
+ * std::runtime_error instead (e.g. src/pathtrace/ptdispatch.cpp:44-47,127-128). */
+typedef enum pt_status {
+    PT_OK = 0,
+    PT_ERR_INVALID = -1,     /* bad argument or malformed scene data            */
+    PT_ERR_CUDA = -2,        /* CUDA runtime error                              */
+    PT_ERR_OOM = -3,         /* device or host allocation failed                */
+    PT_ERR_STATE = -4,       /* call out of order (e.g. render before upload)   */
+    PT_ERR_TIMEOUT = -5,     /* a device loop hit its iteration cap            */
+    PT_ERR_DEVICE = -6,      /* a kernel reported an error word (bounds etc.)   */
+    PT_ERR_IO = -7,          /* file could not be read or written               */
+    PT_ERR_UNSUPPORTED = -8  /* feature outside what this build implements      */
+} pt_status;
+
+/* ---- Constants shared with the reference's device contract (share/constants.h:3-28) ---- */
+#define PT_BASE_COLOUR_MAP_BIT (1u << 0)
+#define PT_EMISSION_MAP_BIT (1u << 1)
+#define PT_ROUGHNESS_MAP_BIT (1u << 2)
+#define PT_METALNESS_MAP_BIT (1u << 3)
+#define PT_ROUGHNESS_METALNESS_MAP_BIT (1u << 4)
+#define PT_SPECULAR_MAP_BIT (1u << 5)
+#define PT_SPECULAR_TINT_MAP_BIT (1u << 6)
+#define PT_SHEEN_MAP_BIT (1u << 7)
+#define PT_SHEEN_TINT_MAP_BIT (1u << 8)
+#define PT_CLEARCOAT_MAP_BIT (1u << 9)
+#define PT_CLEARCOAT_ROUGHNESS_MAP_BIT (1u << 10)
+#define PT_ANISOTROPY_MAP_BIT (1u << 11)
+#define PT_NORMAL_MAP_BIT (1u << 12)
+#define PT_MATERIAL_IS_TRANSPARENT_BIT (1u << 13)
+#define PT_ANY_MAP_BITS 0x1FFFu
+
+#define PT_LIGHT_TYPE_POINT 1u
+#define PT_LIGHT_TYPE_DIRECTIONAL 2u
+#define PT_LIGHT_TYPE_EMITTER 3u
+#define PT_NO_EMITTER_INDEX 0xFFFFFFFFu
+#define PT_LIGHT_BIN_SIZE 10u   /* u32 words per light alias-table bin   */
+#define PT_EMITTER_BIN_SIZE 6u  /* u32 words per emitter-triangle bin    */
+
+/* ---- Scene data contract (the reference's SceneBuffer regions) ---- */
+
+/* Vertex: 32 B = position xyz, normal xyz, uv (src/scene/mesh.h:10-18;
+ * read on the device as two float4, shaders/pathtrace/geometry.hlsli:27-36). */
+#define PT_VERTEX_FLOATS 8
+
+/* Per-mesh ranges into the flat vertex/index arrays (the reference's
+ * SceneBuffer::start_indices, src/scene/scenebuffer.cpp:116-132). */
+typedef struct pt_mesh_range {
+    uint32_t vertex_offset; /* first vertex of the mesh in the vertex array  */
+    uint32_t index_offset;  /* first index (3 per triangle) in index array   */
+    uint32_t tri_count;
+    uint32_t vertex_count;
+} pt_mesh_range;
+
+/* InstanceData, 128 B (src/scene/scenebuffer.h:13-24): transform is the
+ * object-to-world matrix stored row-major (world = transform * p); normal
+ * holds the rows of the normal matrix (inverse-transpose), each padded to
+ * 16 B, as the shaders read it (shaders/pathtrace/geometry.hlsli:4-11). */
+typedef struct pt_instance_data {
+    uint32_t vertex_index;
+    uint32_t index_index;
+    uint32_t emitter_index;  /* PT_NO_EMITTER_INDEX if not emissive */
+    uint32_t material_index;
+    float transform[4][4];
+    float normal[3][4];
+} pt_instance_data;
+
+/* PbrMaterial, 96 B (src/scene/material.h:24-29). rough_metal_normal_map_bits[3]
+ * carries the map bits as raw u32 bits. */
+typedef struct pt_material {
+    float base_colour[4];
+    float emission[4]; /* rgb, a = strength */
+    float rough_metal_normal_map_bits[4];
+    float specular[4];
+    float sheen[4];
+    float cc_ccrgh_aniso[4];
+} pt_material;
+
+/* A borrowed view of a packed scene.  Mirrors the descriptor bindings 3-6 and
+ * 9 of the reference (src/pathtrace/pathtrace.cpp:36-69) plus the per-instance
+ * data the reference hands to the driver's acceleration-structure build
+ * (src/pathtrace/accstruct.cpp:186-218). */
+typedef struct pt_scene_view {
+    const float* vertices;   /* vertex_count * PT_VERTEX_FLOATS */
+    uint32_t vertex_count;
+    const uint32_t* indices; /* mesh-local vertex indices, 3 per triangle */
+    uint32_t index_count;
+    const pt_mesh_range* meshes;
+    uint32_t mesh_count;
+    const pt_instance_data* instances;
+    const uint32_t* instance_mesh; /* mesh (BLAS) of each instance */
+    /* Optional: world-to-object affine transform per instance, 12 floats
+     * row-major (3x4).  NULL lets the library derive it from transform. */
+    const float* instance_world_to_object;
+    const uint8_t* instance_opaque; /* optional; NULL = all opaque (accstruct.cpp:212-214) */
+    uint32_t instance_count;
+    const pt_material* materials;
+    uint32_t material_count;
+    const uint32_t* light_words; /* light-sampler stream (lightsample.cpp:89-221) */
+    uint32_t light_word_count;
+    uint32_t light_count;        /* bins of the top-level light alias table */
+    float environment_colour[3]; /* linear (already sRGB-decoded) */
+} pt_scene_view;
+
+/* Accumulation modes. */
+#define PT_ACCUM_FP32 0u      /* running mean in FP32, as the reference       */
+#define PT_ACCUM_FP32_FP64 1u /* additionally sum radiance in FP64 (oracle)   */
+
+/* Kernel strategy (chosen by the autotuner when PT_KERNEL_AUTO). */
+#define PT_KERNEL_AUTO 0u
+#define PT_KERNEL_MEGA 1u
+#define PT_KERNEL_WAVEFRONT 2u
+
+/* Render parameters: the reference's UniformBufferObject
+ * (src/pathtrace/pathtrace.h:21-41, shaders/pathtrace/pathtrace.hlsli:8-29). */
+typedef struct pt_render_params {
+    float inv_view[16]; /* row-major, as uploaded (pathtrace.cpp:387-388) */
+    float inv_proj[16];
+    float near_plane;
+    float far_plane;
+    float focus_dist;
+    float lens_radius;
+    float exposure;
+    uint32_t width;
+    uint32_t height;
+    uint32_t sample_index; /* first sample of this call; 0 resets the image */
+    uint32_t samples;      /* samples per pixel rendered by this call      */
+    uint32_t max_bounces;
+    uint32_t accum_mode;   /* PT_ACCUM_*  */
+    uint32_t kernel;       /* PT_KERNEL_* */
+    uint32_t rr_start;     /* first segment with Russian roulette; 1 = reference */
+    uint32_t reserved[3];
+} pt_render_params;
+
+/* Counters of the last pt_render call. */
+typedef struct pt_render_stats {
+    uint64_t segments;        /* traced primary + extension rays           */
+    uint64_t shadow_rays;     /* traced NEE shadow rays                    */
+    uint64_t paths;           /* pixel samples                             */
+    float milliseconds;       /* device time of the render (CUDA events)   */
+    uint32_t kernel_launches; /* kernels launched by the call              */
+    uint32_t kernel_used;     /* PT_KERNEL_MEGA or PT_KERNEL_WAVEFRONT     */
+    uint32_t error_word;      /* device error word (0 = none)              */
+} pt_render_stats;
+
+/* Accelerating-structure summary. */
+typedef struct pt_accel_info {
+    uint32_t blas_count;
+    uint32_t tlas_nodes;
+    uint64_t blas_nodes;
+    uint64_t triangles;
+    uint64_t device_bytes;
+    float build_ms;
+} pt_accel_info;
+
+typedef struct pt_ctx pt_ctx;
+
+/* Library ABI version (PT_ABI_VERSION of the build). */
+int pt_abi_version(void);
+
+/* Create a context on CUDA device `device`.  Replaces the Vulkan context and
+ * device set-up of PathTraceDispatcher's constructor (ptdispatch.cpp:18-35). */
+pt_ctx* pt_create(int device);
+
+/* Destroy a context and free its device memory (~PathTraceDispatcher,
+ * ptdispatch.cpp:37-40). */
+void pt_destroy(pt_ctx* ctx);
+
+/* Message for the last failing call on this context (or of pt_create when ctx
+ * is NULL).  Valid until the next call on the context. */
+const char* pt_last_error(const pt_ctx* ctx);
+
+/* Upload a packed scene (SceneBuffer::build, scenebuffer.cpp:65-168).  The
+ * view is copied; the caller may free its arrays after the call returns. */
+int pt_upload_scene(pt_ctx* ctx, const pt_scene_view* scene);
+
+/* Build the two-level acceleration structure on the device: one BLAS per mesh
+ * and one TLAS over all instances (AccelerationStructure ctor,
+ * accstruct.cpp:288-319, create_blas :69-164, create_tlas :186-286). */
+int pt_build_accel(pt_ctx* ctx, pt_accel_info* info_out /* may be NULL */);
+
+/* Render params->samples samples per pixel starting at params->sample_index.
+ * Replaces PathTraceDispatcher::render (ptdispatch.cpp:97-134) with
+ * PathTracer::set_camera/set_samples/set_max_bounces/update_uniforms
+ * (pathtrace.cpp:381-516).  Asynchronous unless stats_out is non-NULL. */
+int pt_render(pt_ctx* ctx, const pt_render_params* params, pt_render_stats* stats_out);
+
+/* Copy the accumulated image to host memory as RGBA rows of `pitch_bytes`
+ * bytes (float when fp64 == 0, double when fp64 == 1).  Replaces the copy
+ * into the host-visible image and vkMapMemory of ptdispatch.cpp:77-94. */
+int pt_read_image(pt_ctx* ctx, void* rgba, size_t pitch_bytes, int fp64);
+
+/* Wait for all work of the context. */
+int pt_synchronize(pt_ctx* ctx);
+
+/* ACES tone map of the accumulation image in place, as the reference does
+ * before writing PNG (tonemap.cs.hlsl:17-77, ptdispatch.cpp:175-179). */
+int pt_tonemap(pt_ctx* ctx);
+
+/* Mean squared error between the FP32 image of `ctx` and a reference RGBA
+ * image in device-visible host memory, with util/meansq semantics
+ * (meansq.cpp:34-43): SSE over RGB / (w*h*3 - 1), reduced in FP64. */
+int pt_mse_host(pt_ctx* ctx, const float* reference_rgba, double* mse_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PT_GPU_H_INCLUDED */

@@ -1,0 +1,596 @@
+// api.cu — the C ABI of libptgpu.so (include/pt_gpu.h): context, scene upload,
+// acceleration-structure build, rendering and read-back.
+//
+// Replaces the reference's PathTraceDispatcher / PathTracer host code
+// (src/pathtrace/ptdispatch.cpp:18-204, pathtrace.cpp:81-516) with one CUDA
+// stream per context and explicit device buffers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/pt_gpu.h"
+#include "device/render.cuh"
+#include "kernels.h"
+
+namespace pt {
+cudaError_t render_init_tables(const uint32_t* table128, cudaStream_t stream);
+}
+
+using namespace pt;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count)
+    {
+        release();
+        if (count == 0)
+            count = 1;
+        cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        n = count;
+        return cudaSuccess;
+    }
+    void release()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+// Sobol' direction numbers for 4 dimensions: van der Corput, then the
+// primitive polynomials / initial numbers (s, a, m) = (1, 0, {1}),
+// (2, 1, {1, 3}), (3, 1, {1, 3, 1}) of Joe & Kuo (2008) — the table of
+// shaders/pathtrace/sample.hlsli:31-67.
+void sobol_table(uint32_t v[4][32])
+{
+    for (int b = 0; b < 32; b++)
+        v[0][b] = 1u << (31 - b);
+    const int s_[3] = {1, 2, 3};
+    const uint32_t a_[3] = {0, 1, 1};
+    const uint32_t m_[3][3] = {{1, 0, 0}, {1, 3, 0}, {1, 3, 1}};
+    for (int d = 1; d < 4; d++) {
+        int s = s_[d - 1];
+        for (int k = 0; k < s; k++)
+            v[d][k] = m_[d - 1][k] << (31 - k);
+        for (int k = s; k < 32; k++) {
+            uint32_t x = v[d][k - s] ^ (v[d][k - s] >> s);
+            for (int j = 1; j < s; j++)
+                if ((a_[d - 1] >> (s - 1 - j)) & 1u)
+                    x ^= v[d][k - j];
+            v[d][k] = x;
+        }
+    }
+}
+
+// 4x4 inverse by cofactors in FP64 (row-major), for world-to-object rows
+// when the caller does not supply them.
+void inverse4(const double m[16], double out[16])
+{
+    const double* a = m;
+    double inv[16];
+    inv[0] = a[5] * a[10] * a[15] - a[5] * a[11] * a[14] - a[9] * a[6] * a[15] + a[9] * a[7] * a[14] + a[13] * a[6] * a[11] - a[13] * a[7] * a[10];
+    inv[4] = -a[4] * a[10] * a[15] + a[4] * a[11] * a[14] + a[8] * a[6] * a[15] - a[8] * a[7] * a[14] - a[12] * a[6] * a[11] + a[12] * a[7] * a[10];
+    inv[8] = a[4] * a[9] * a[15] - a[4] * a[11] * a[13] - a[8] * a[5] * a[15] + a[8] * a[7] * a[13] + a[12] * a[5] * a[11] - a[12] * a[7] * a[9];
+    inv[12] = -a[4] * a[9] * a[14] + a[4] * a[10] * a[13] + a[8] * a[5] * a[14] - a[8] * a[6] * a[13] - a[12] * a[5] * a[10] + a[12] * a[6] * a[9];
+    inv[1] = -a[1] * a[10] * a[15] + a[1] * a[11] * a[14] + a[9] * a[2] * a[15] - a[9] * a[3] * a[14] - a[13] * a[2] * a[11] + a[13] * a[3] * a[10];
+    inv[5] = a[0] * a[10] * a[15] - a[0] * a[11] * a[14] - a[8] * a[2] * a[15] + a[8] * a[3] * a[14] + a[12] * a[2] * a[11] - a[12] * a[3] * a[10];
+    inv[9] = -a[0] * a[9] * a[15] + a[0] * a[11] * a[13] + a[8] * a[1] * a[15] - a[8] * a[3] * a[13] - a[12] * a[1] * a[11] + a[12] * a[3] * a[9];
+    inv[13] = a[0] * a[9] * a[14] - a[0] * a[10] * a[13] - a[8] * a[1] * a[14] + a[8] * a[2] * a[13] + a[12] * a[1] * a[10] - a[12] * a[2] * a[9];
+    inv[2] = a[1] * a[6] * a[15] - a[1] * a[7] * a[14] - a[5] * a[2] * a[15] + a[5] * a[3] * a[14] + a[13] * a[2] * a[7] - a[13] * a[3] * a[6];
+    inv[6] = -a[0] * a[6] * a[15] + a[0] * a[7] * a[14] + a[4] * a[2] * a[15] - a[4] * a[3] * a[14] - a[12] * a[2] * a[7] + a[12] * a[3] * a[6];
+    inv[10] = a[0] * a[5] * a[15] - a[0] * a[7] * a[13] - a[4] * a[1] * a[15] + a[4] * a[3] * a[13] + a[12] * a[1] * a[7] - a[12] * a[3] * a[5];
+    inv[14] = -a[0] * a[5] * a[14] + a[0] * a[6] * a[13] + a[4] * a[1] * a[14] - a[4] * a[2] * a[13] - a[12] * a[1] * a[6] + a[12] * a[2] * a[5];
+    inv[3] = -a[1] * a[6] * a[11] + a[1] * a[7] * a[10] + a[5] * a[2] * a[11] - a[5] * a[3] * a[10] - a[9] * a[2] * a[7] + a[9] * a[3] * a[6];
+    inv[7] = a[0] * a[6] * a[11] - a[0] * a[7] * a[10] - a[4] * a[2] * a[11] + a[4] * a[3] * a[10] + a[8] * a[2] * a[7] - a[8] * a[3] * a[6];
+    inv[11] = -a[0] * a[5] * a[11] + a[0] * a[7] * a[9] + a[4] * a[1] * a[11] - a[4] * a[3] * a[9] - a[8] * a[1] * a[7] + a[8] * a[3] * a[5];
+    inv[15] = a[0] * a[5] * a[10] - a[0] * a[6] * a[9] - a[4] * a[1] * a[10] + a[4] * a[2] * a[9] + a[8] * a[1] * a[6] - a[8] * a[2] * a[5];
+    double det = a[0] * inv[0] + a[1] * inv[4] + a[2] * inv[8] + a[3] * inv[12];
+    double id = 1.0 / det;
+    for (int i = 0; i < 16; i++)
+        out[i] = inv[i] * id;
+}
+
+} // namespace
+
+struct pt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool tables = false;
+    // scene
+    bool scene_ok = false;
+    DevBuf<float4> vertices;
+    DevBuf<uint32_t> indices;
+    DevBuf<DevInstanceData> inst_data;
+    DevBuf<DevMaterial> materials;
+    DevBuf<uint32_t> light;
+    DevBuf<uint32_t> mesh_vertex_offset, mesh_index_offset, mesh_tri_base, inst_mesh;
+    DevBuf<DevInstance> dinst;
+    uint32_t vertex_count = 0, index_count = 0, mesh_count = 0, tri_count = 0, instance_count = 0, material_count = 0;
+    uint32_t light_words = 0, light_count = 0;
+    float env[3] = {0, 0, 0};
+    std::vector<DevInstance> h_dinst;
+    // acceleration structure
+    bool accel_ok = false;
+    DevBuf<BvhNode> nodes;
+    DevBuf<TriRec> tris;
+    DevBuf<int> mesh_root;
+    int tlas_root = REF_EMPTY;
+    pt_accel_info accel{};
+    // image
+    DevBuf<float4> image;
+    DevBuf<double> sum64;
+    uint32_t width = 0, height = 0;
+    uint32_t samples_done = 0;
+    bool have_fp64 = false;
+    DevBuf<unsigned long long> counters;
+    DevBuf<uint32_t> error_word;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    int fail(int code, const std::string& msg)
+    {
+        err = msg;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char* what)
+    {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA;
+    }
+};
+
+static thread_local std::string g_create_error;
+
+template <typename T>
+static cudaError_t upload(pt_ctx* c, DevBuf<T>& b, const T* src, size_t n)
+{
+    cudaError_t e = b.alloc(n);
+    if (e != cudaSuccess || n == 0)
+        return e;
+    return cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, c->stream);
+}
+
+
+extern "C" {
+
+int pt_abi_version(void) { return PT_ABI_VERSION; }
+
+pt_ctx* pt_create(int device)
+{
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        g_create_error = std::string("no CUDA device: ") + cudaGetErrorString(e);
+        return nullptr;
+    }
+    if (device < 0 || device >= count) {
+        g_create_error = "device index out of range";
+        return nullptr;
+    }
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+        return nullptr;
+    }
+    pt_ctx* c = new (std::nothrow) pt_ctx();
+    if (!c) {
+        g_create_error = "out of host memory";
+        return nullptr;
+    }
+    c->device = device;
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess ||
+        (e = c->counters.alloc(4)) != cudaSuccess || (e = c->error_word.alloc(1)) != cudaSuccess) {
+        g_create_error = std::string("context set-up: ") + cudaGetErrorString(e);
+        delete c;
+        return nullptr;
+    }
+    uint32_t table[4][32];
+    sobol_table(table);
+    if ((e = render_init_tables(&table[0][0], c->stream)) != cudaSuccess) {
+        g_create_error = std::string("sampler tables: ") + cudaGetErrorString(e);
+        delete c;
+        return nullptr;
+    }
+    cudaMemsetAsync(c->error_word.p, 0, sizeof(uint32_t), c->stream);
+    cudaStreamSynchronize(c->stream);
+    return c;
+}
+
+void pt_destroy(pt_ctx* c)
+{
+    if (!c)
+        return;
+    cudaSetDevice(c->device);
+    if (c->stream)
+        cudaStreamSynchronize(c->stream);
+    c->vertices.release();
+    c->indices.release();
+    c->inst_data.release();
+    c->materials.release();
+    c->light.release();
+    c->mesh_vertex_offset.release();
+    c->mesh_index_offset.release();
+    c->mesh_tri_base.release();
+    c->inst_mesh.release();
+    c->dinst.release();
+    c->nodes.release();
+    c->tris.release();
+    c->mesh_root.release();
+    c->image.release();
+    c->sum64.release();
+    c->counters.release();
+    c->error_word.release();
+    if (c->ev0)
+        cudaEventDestroy(c->ev0);
+    if (c->ev1)
+        cudaEventDestroy(c->ev1);
+    if (c->stream)
+        cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* pt_last_error(const pt_ctx* c)
+{
+    if (!c)
+        return g_create_error.c_str();
+    return c->err.c_str();
+}
+
+int pt_synchronize(pt_ctx* c)
+{
+    if (!c)
+        return PT_ERR_INVALID;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+        return c->cuda_fail(e, "synchronize");
+    return PT_OK;
+}
+
+int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
+{
+    if (!c || !v)
+        return PT_ERR_INVALID;
+    cudaSetDevice(c->device);
+    c->scene_ok = false;
+    c->accel_ok = false;
+    if ((v->vertex_count && !v->vertices) || (v->index_count && !v->indices) || (v->mesh_count && !v->meshes) ||
+        (v->instance_count && (!v->instances || !v->instance_mesh)) || (v->material_count && !v->materials) ||
+        (v->light_word_count && !v->light_words))
+        return c->fail(PT_ERR_INVALID, "scene view has a null array with a non-zero count");
+    if (v->index_count % 3 != 0)
+        return c->fail(PT_ERR_INVALID, "index count is not a multiple of 3");
+    if (v->mesh_count >= 65536)
+        return c->fail(PT_ERR_UNSUPPORTED, "more than 65535 meshes");
+    if (v->light_count > 0 && v->light_word_count < v->light_count * PT_LIGHT_BIN_SIZE)
+        return c->fail(PT_ERR_INVALID, "light stream shorter than its top-level table");
+    // meshes
+    std::vector<uint32_t> vo(v->mesh_count), io(v->mesh_count), tb(v->mesh_count + 1);
+    uint64_t tris = 0;
+    for (uint32_t m = 0; m < v->mesh_count; m++) {
+        const pt_mesh_range& r = v->meshes[m];
+        if ((uint64_t)r.vertex_offset + r.vertex_count > v->vertex_count || (uint64_t)r.index_offset + 3ull * r.tri_count > v->index_count)
+            return c->fail(PT_ERR_INVALID, "mesh " + std::to_string(m) + " range outside the vertex/index arrays");
+        for (uint64_t k = 0; k < 3ull * r.tri_count; k++)
+            if (v->indices[r.index_offset + k] >= r.vertex_count)
+                return c->fail(PT_ERR_INVALID, "mesh " + std::to_string(m) + " has an index outside its vertices");
+        vo[m] = r.vertex_offset;
+        io[m] = r.index_offset;
+        tb[m] = (uint32_t)tris;
+        tris += r.tri_count;
+    }
+    if (tris >= (1u << 28))
+        return c->fail(PT_ERR_UNSUPPORTED, "more than 2^28 triangles");
+    tb[v->mesh_count] = (uint32_t)tris;
+    if (v->instance_count >= (1u << 28))
+        return c->fail(PT_ERR_UNSUPPORTED, "more than 2^28 instances");
+    // materials: textures are outside this build
+    for (uint32_t i = 0; i < v->material_count; i++) {
+        uint32_t bits;
+        std::memcpy(&bits, &v->materials[i].rough_metal_normal_map_bits[3], 4);
+        if (bits & (PT_ANY_MAP_BITS & ~PT_MATERIAL_IS_TRANSPARENT_BIT))
+            return c->fail(PT_ERR_UNSUPPORTED, "material " + std::to_string(i) + " uses texture maps");
+    }
+    // instances
+    c->h_dinst.assign(v->instance_count, DevInstance{});
+    for (uint32_t i = 0; i < v->instance_count; i++) {
+        const pt_instance_data& d = v->instances[i];
+        uint32_t m = v->instance_mesh[i];
+        if (m >= v->mesh_count)
+            return c->fail(PT_ERR_INVALID, "instance " + std::to_string(i) + " names a missing mesh");
+        if (d.material_index >= v->material_count)
+            return c->fail(PT_ERR_INVALID, "instance " + std::to_string(i) + " names a missing material");
+        if (d.vertex_index != v->meshes[m].vertex_offset || d.index_index != v->meshes[m].index_offset)
+            return c->fail(PT_ERR_INVALID, "instance " + std::to_string(i) + " offsets disagree with its mesh");
+        DevInstance& di = c->h_dinst[i];
+        float w[12];
+        if (v->instance_world_to_object) {
+            std::memcpy(w, v->instance_world_to_object + 12 * (size_t)i, sizeof(w));
+        } else {
+            double M[16], inv[16];
+            for (int r = 0; r < 4; r++)
+                for (int k = 0; k < 4; k++)
+                    M[r * 4 + k] = d.transform[r][k];
+            inverse4(M, inv);
+            for (int k = 0; k < 12; k++)
+                w[k] = (float)inv[k];
+        }
+        for (int r = 0; r < 3; r++)
+            di.w2o[r] = make_float4(w[4 * r + 0], w[4 * r + 1], w[4 * r + 2], w[4 * r + 3]);
+        di.blas_root = REF_EMPTY;
+        di.flags = (v->instance_opaque == nullptr || v->instance_opaque[i]) ? 1u : 0u;
+        di.mesh = m;
+    }
+    cudaError_t e;
+    static_assert(sizeof(DevInstanceData) == sizeof(pt_instance_data), "InstanceData layout");
+    static_assert(sizeof(DevMaterial) == sizeof(pt_material), "PbrMaterial layout");
+    if ((e = upload(c, c->vertices, (const float4*)v->vertices, 2 * (size_t)v->vertex_count)) != cudaSuccess ||
+        (e = upload(c, c->indices, v->indices, v->index_count)) != cudaSuccess ||
+        (e = upload(c, c->inst_data, (const DevInstanceData*)v->instances, v->instance_count)) != cudaSuccess ||
+        (e = upload(c, c->materials, (const DevMaterial*)v->materials, v->material_count)) != cudaSuccess ||
+        (e = upload(c, c->light, v->light_words, v->light_word_count)) != cudaSuccess ||
+        (e = upload(c, c->mesh_vertex_offset, vo.data(), vo.size())) != cudaSuccess ||
+        (e = upload(c, c->mesh_index_offset, io.data(), io.size())) != cudaSuccess ||
+        (e = upload(c, c->mesh_tri_base, tb.data(), tb.size())) != cudaSuccess ||
+        (e = upload(c, c->inst_mesh, v->instance_mesh, v->instance_count)) != cudaSuccess ||
+        (e = upload(c, c->dinst, c->h_dinst.data(), c->h_dinst.size())) != cudaSuccess)
+        return c->cuda_fail(e, "scene upload");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
+        return c->cuda_fail(e, "scene upload");
+    c->vertex_count = v->vertex_count;
+    c->index_count = v->index_count;
+    c->mesh_count = v->mesh_count;
+    c->tri_count = (uint32_t)tris;
+    c->instance_count = v->instance_count;
+    c->material_count = v->material_count;
+    c->light_words = v->light_word_count;
+    c->light_count = v->light_count;
+    std::memcpy(c->env, v->environment_colour, sizeof(c->env));
+    c->scene_ok = true;
+    return PT_OK;
+}
+
+int pt_build_accel(pt_ctx* c, pt_accel_info* info)
+{
+    if (!c)
+        return PT_ERR_INVALID;
+    if (!c->scene_ok)
+        return c->fail(PT_ERR_STATE, "no scene uploaded");
+    cudaSetDevice(c->device);
+    cudaError_t e;
+    size_t n_nodes = bvh_node_count(c->tri_count, c->instance_count);
+    if ((e = c->nodes.alloc(n_nodes)) != cudaSuccess || (e = c->tris.alloc(c->tri_count)) != cudaSuccess ||
+        (e = c->mesh_root.alloc(c->mesh_count)) != cudaSuccess)
+        return c->cuda_fail(e, "acceleration structure allocation");
+    size_t scratch_bytes = bvh_scratch_bytes(c->mesh_count, c->tri_count, c->instance_count);
+    void* scratch = nullptr;
+    if ((e = cudaMalloc(&scratch, scratch_bytes)) != cudaSuccess)
+        return c->cuda_fail(e, "BVH scratch allocation");
+    BvhBuildInput in{};
+    in.vertices = c->vertices.p;
+    in.indices = c->indices.p;
+    in.mesh_vertex_offset = c->mesh_vertex_offset.p;
+    in.mesh_index_offset = c->mesh_index_offset.p;
+    in.mesh_tri_base = c->mesh_tri_base.p;
+    in.mesh_count = c->mesh_count;
+    in.tri_count = c->tri_count;
+    in.inst_data = c->inst_data.p;
+    in.inst_mesh = c->inst_mesh.p;
+    in.instance_count = c->instance_count;
+    BvhBuildOutput out{};
+    out.nodes = c->nodes.p;
+    out.tris = c->tris.p;
+    out.dinst = c->dinst.p;
+    out.mesh_root = c->mesh_root.p;
+    cudaEventRecord(c->ev0, c->stream);
+    e = bvh_build(in, out, scratch, scratch_bytes, c->stream);
+    cudaEventRecord(c->ev1, c->stream);
+    cudaError_t e2 = cudaStreamSynchronize(c->stream);
+    cudaFree(scratch);
+    if (e != cudaSuccess)
+        return c->cuda_fail(e, "BVH build");
+    if (e2 != cudaSuccess)
+        return c->cuda_fail(e2, "BVH build");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->tlas_root = out.tlas_root;
+    c->accel_ok = true;
+    c->accel.blas_count = c->mesh_count;
+    c->accel.tlas_nodes = c->instance_count > 1 ? c->instance_count - 1 : 0;
+    c->accel.blas_nodes = c->tri_count > 1 ? c->tri_count - 1 : 0;
+    c->accel.triangles = c->tri_count;
+    c->accel.device_bytes = n_nodes * sizeof(BvhNode) + (size_t)c->tri_count * sizeof(TriRec) + (size_t)c->instance_count * sizeof(DevInstance);
+    c->accel.build_ms = ms;
+    if (info)
+        *info = c->accel;
+    return PT_OK;
+}
+
+static int ensure_image(pt_ctx* c, uint32_t w, uint32_t h, bool fp64, bool reset)
+{
+    cudaError_t e;
+    size_t n = (size_t)w * h;
+    if (c->width != w || c->height != h || !c->image.p) {
+        if ((e = c->image.alloc(n)) != cudaSuccess)
+            return c->cuda_fail(e, "image allocation");
+        c->width = w;
+        c->height = h;
+        c->sum64.release();
+        reset = true;
+    }
+    if (fp64 && !c->sum64.p) {
+        if ((e = c->sum64.alloc(4 * n)) != cudaSuccess)
+            return c->cuda_fail(e, "FP64 image allocation");
+        cudaMemsetAsync(c->sum64.p, 0, 4 * n * sizeof(double), c->stream);
+    }
+    if (reset) {
+        cudaMemsetAsync(c->image.p, 0, n * sizeof(float4), c->stream);
+        if (c->sum64.p)
+            cudaMemsetAsync(c->sum64.p, 0, 4 * n * sizeof(double), c->stream);
+        c->samples_done = 0;
+    }
+    return PT_OK;
+}
+
+int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
+{
+    if (!c || !p)
+        return PT_ERR_INVALID;
+    if (!c->accel_ok)
+        return c->fail(PT_ERR_STATE, "acceleration structure not built");
+    if (p->width == 0 || p->height == 0 || p->samples == 0)
+        return c->fail(PT_ERR_INVALID, "zero width, height or sample count");
+    if ((uint64_t)p->width * p->height > (1ull << 31))
+        return c->fail(PT_ERR_UNSUPPORTED, "image larger than 2^31 pixels");
+    if ((uint64_t)p->sample_index + p->samples > 0xFFFFFFFFull)
+        return c->fail(PT_ERR_INVALID, "sample index overflows 32 bits");
+    if (p->accum_mode > PT_ACCUM_FP32_FP64 || p->kernel > PT_KERNEL_WAVEFRONT)
+        return c->fail(PT_ERR_INVALID, "unknown accumulation mode or kernel");
+    cudaSetDevice(c->device);
+    bool fp64 = p->accum_mode == PT_ACCUM_FP32_FP64;
+    int rc = ensure_image(c, p->width, p->height, fp64, p->sample_index == 0);
+    if (rc != PT_OK)
+        return rc;
+    RenderArgs a{};
+    a.s.vertices = c->vertices.p;
+    a.s.indices = c->indices.p;
+    a.s.inst_data = c->inst_data.p;
+    a.s.materials = c->materials.p;
+    a.s.light = c->light.p;
+    a.s.light_words = c->light_words;
+    a.s.light_count = c->light_count;
+    a.s.instance_count = c->instance_count;
+    a.s.nodes = c->nodes.p;
+    a.s.tris = c->tris.p;
+    a.s.dinst = c->dinst.p;
+    a.s.tlas_root = c->tlas_root;
+    a.s.env = mk3(c->env[0], c->env[1], c->env[2]);
+    a.s.error_word = c->error_word.p;
+    std::memcpy(a.inv_view, p->inv_view, sizeof(a.inv_view));
+    std::memcpy(a.inv_proj, p->inv_proj, sizeof(a.inv_proj));
+    a.near_plane = p->near_plane;
+    a.far_plane = p->far_plane;
+    a.focus_dist = p->focus_dist;
+    a.lens_radius = p->lens_radius;
+    a.exposure = p->exposure;
+    a.width = p->width;
+    a.height = p->height;
+    a.max_bounces = p->max_bounces;
+    a.rr_start = p->rr_start == 0 ? 1 : p->rr_start;
+    a.image = c->image.p;
+    a.sum64 = fp64 ? c->sum64.p : nullptr;
+    a.counters = c->counters.p;
+    cudaMemsetAsync(c->counters.p, 0, 4 * sizeof(unsigned long long), c->stream);
+    // Split long renders so no single launch covers more than 2^26 path samples.
+    uint64_t pixels = (uint64_t)p->width * p->height;
+    uint32_t per_launch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->samples, (1ull << 26) / pixels));
+    uint32_t launches = 0;
+    cudaEventRecord(c->ev0, c->stream);
+    for (uint32_t done = 0; done < p->samples; done += per_launch) {
+        a.sample_index = p->sample_index + done;
+        a.samples = std::min(per_launch, p->samples - done);
+        cudaError_t e = launch_megakernel(a, c->stream);
+        if (e != cudaSuccess)
+            return c->cuda_fail(e, "render launch");
+        launches++;
+    }
+    cudaEventRecord(c->ev1, c->stream);
+    c->samples_done = p->sample_index + p->samples;
+    c->have_fp64 = fp64;
+    if (stats) {
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess)
+            return c->cuda_fail(e, "render");
+        unsigned long long cnt[4];
+        uint32_t ew = 0;
+        cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&ew, c->error_word.p, sizeof(ew), cudaMemcpyDeviceToHost);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        stats->segments = cnt[0];
+        stats->shadow_rays = cnt[1];
+        stats->paths = cnt[2];
+        stats->milliseconds = ms;
+        stats->kernel_launches = launches;
+        stats->kernel_used = PT_KERNEL_MEGA;
+        stats->error_word = ew;
+        if (ew != 0)
+            return c->fail(PT_ERR_DEVICE, "device error word " + std::to_string(ew));
+    }
+    return PT_OK;
+}
+
+int pt_read_image(pt_ctx* c, void* rgba, size_t pitch, int fp64)
+{
+    if (!c || !rgba)
+        return PT_ERR_INVALID;
+    if (!c->image.p)
+        return c->fail(PT_ERR_STATE, "nothing rendered");
+    cudaSetDevice(c->device);
+    cudaError_t e;
+    if (!fp64) {
+        if (pitch < (size_t)c->width * 16)
+            return c->fail(PT_ERR_INVALID, "pitch smaller than a row");
+        e = cudaMemcpy2DAsync(rgba, pitch, c->image.p, (size_t)c->width * 16, (size_t)c->width * 16, c->height, cudaMemcpyDeviceToHost,
+                              c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess)
+            return c->cuda_fail(e, "image read-back");
+        return PT_OK;
+    }
+    if (!c->sum64.p)
+        return c->fail(PT_ERR_STATE, "no FP64 accumulation (render with PT_ACCUM_FP32_FP64)");
+    if (pitch < (size_t)c->width * 32)
+        return c->fail(PT_ERR_INVALID, "pitch smaller than a row");
+    size_t n = (size_t)c->width * c->height;
+    std::vector<double> sums(4 * n);
+    e = cudaMemcpyAsync(sums.data(), c->sum64.p, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+        return c->cuda_fail(e, "FP64 read-back");
+    for (uint32_t y = 0; y < c->height; y++) {
+        double* row = (double*)((char*)rgba + pitch * y);
+        for (uint32_t x = 0; x < c->width; x++) {
+            const double* s = &sums[4 * ((size_t)y * c->width + x)];
+            double cnt = s[3] > 0.0 ? s[3] : 1.0;
+            row[4 * x + 0] = s[0] / cnt;
+            row[4 * x + 1] = s[1] / cnt;
+            row[4 * x + 2] = s[2] / cnt;
+            row[4 * x + 3] = 1.0;
+        }
+    }
+    return PT_OK;
+}
+
+int pt_tonemap(pt_ctx* c)
+{
+    if (!c)
+        return PT_ERR_INVALID;
+    return c->fail(PT_ERR_UNSUPPORTED, "tone map not built yet");
+}
+
+int pt_mse_host(pt_ctx* c, const float* ref, double* mse)
+{
+    if (!c || !ref || !mse)
+        return PT_ERR_INVALID;
+    return c->fail(PT_ERR_UNSUPPORTED, "device MSE not built yet");
+}
+
+} // extern "C"

@@ -1,0 +1,528 @@
+// bvh_build.cu — two-level BVH construction on the device.
+//
+// Replaces the driver's acceleration-structure build of the reference
+// (vkCmdBuildAccelerationStructuresKHR, src/pathtrace/accstruct.cpp:57-61,
+// 69-164 for the per-mesh BLAS, 186-286 for the TLAS).
+//
+// Method: linear BVH (Karras 2012, "Maximizing parallelism in the
+// construction of BVHs, octrees, and k-d trees").  All meshes are built in a
+// single pass: each primitive's 64-bit key is (segment << 48 | 48-bit Morton
+// code of its centroid within the segment's centroid bounds), so after one
+// radix sort every mesh is a contiguous key range and the binary radix tree
+// over all keys contains, for every mesh, a node whose range is exactly that
+// mesh (the mesh's BLAS root).  Nodes that straddle two meshes are never
+// referenced.  Boxes are reduced bottom-up with one atomic counter per node,
+// then every node is written with both child boxes padded outward (relative
+// 1e-5 of the largest coordinate) so the traversal's box tests stay
+// conservative.  The TLAS is the same construction over instance world boxes
+// with one segment.
+#include <cub/cub.cuh>
+
+#include "device/scene.cuh"
+#include "kernels.h"
+
+namespace pt {
+
+namespace {
+
+constexpr int MORTON_BITS = 16;           // per axis
+constexpr int KEY_SEG_SHIFT = 3 * MORTON_BITS;
+
+__device__ __forceinline__ int f2ord(float f)
+{
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
+
+__device__ __forceinline__ uint64_t expand_bits16(uint32_t v)
+{
+    uint64_t x = v & 0xFFFFu;
+    x = (x | (x << 32)) & 0x0000FFFF0000FFFFull; // not needed for 16 bits but harmless
+    x = (x | (x << 16)) & 0x00FF0000FF0000FFull;
+    x = (x | (x << 8)) & 0xF00F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x30C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x9249249249249249ull;
+    return x;
+}
+
+__device__ __forceinline__ uint32_t upper_segment(const uint32_t* base, uint32_t nseg, uint32_t g)
+{
+    // largest m with base[m] <= g (base has nseg + 1 entries, base[0] = 0)
+    uint32_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (base[mid] <= g)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+struct Scratch {
+    float4* lo;      // primitive boxes
+    float4* hi;
+    uint32_t* seg;   // segment of each primitive
+    uint64_t* keys_in;
+    uint64_t* keys_out;
+    uint32_t* vals_in;
+    uint32_t* vals_out;
+    int* parent;       // internal nodes (n - 1)
+    int* leaf_parent;  // leaves (n)
+    int* child0;
+    int* child1;
+    uint32_t* flags;
+    float4* nlo;     // internal node boxes (unpadded)
+    float4* nhi;
+    int* seg_cb;     // 6 ints per segment: centroid bounds (ordered ints)
+    int* seg_box;    // 6 ints per segment: primitive bounds
+    uint32_t* seg_base; // segment begin (nseg + 1)
+    int* seg_root;
+    void* cub_temp;
+    size_t cub_bytes;
+};
+
+template <typename T>
+T* carve(char*& p, size_t count)
+{
+    uintptr_t a = ((uintptr_t)p + 255) & ~(uintptr_t)255;
+    T* r = (T*)a;
+    p = (char*)(a + count * sizeof(T));
+    return r;
+}
+
+size_t cub_sort_bytes(uint32_t n)
+{
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (uint64_t*)nullptr, (uint64_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (int)n, 0, 64);
+    return bytes;
+}
+
+Scratch carve_scratch(void* base, uint32_t n, uint32_t nseg)
+{
+    char* p = (char*)base;
+    Scratch s;
+    uint32_t nn = n > 0 ? n : 1;
+    s.lo = carve<float4>(p, nn);
+    s.hi = carve<float4>(p, nn);
+    s.seg = carve<uint32_t>(p, nn);
+    s.keys_in = carve<uint64_t>(p, nn);
+    s.keys_out = carve<uint64_t>(p, nn);
+    s.vals_in = carve<uint32_t>(p, nn);
+    s.vals_out = carve<uint32_t>(p, nn);
+    s.parent = carve<int>(p, nn);
+    s.leaf_parent = carve<int>(p, nn);
+    s.child0 = carve<int>(p, nn);
+    s.child1 = carve<int>(p, nn);
+    s.flags = carve<uint32_t>(p, nn);
+    s.nlo = carve<float4>(p, nn);
+    s.nhi = carve<float4>(p, nn);
+    s.seg_cb = carve<int>(p, 6 * (size_t)(nseg + 1));
+    s.seg_box = carve<int>(p, 6 * (size_t)(nseg + 1));
+    s.seg_base = carve<uint32_t>(p, nseg + 2);
+    s.seg_root = carve<int>(p, nseg + 1);
+    s.cub_bytes = cub_sort_bytes(nn);
+    s.cub_temp = carve<char>(p, s.cub_bytes);
+    return s;
+}
+
+size_t scratch_bytes_for(uint32_t n, uint32_t nseg)
+{
+    Scratch s = carve_scratch((void*)0, n, nseg);
+    return (size_t)((char*)s.cub_temp - (char*)0) + s.cub_bytes + 256;
+}
+
+__global__ void k_init_bounds(int* cb, int* box, int* roots, uint32_t nseg)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nseg)
+        return;
+    roots[i] = REF_EMPTY;
+    for (int k = 0; k < 3; k++) {
+        cb[6 * i + k] = f2ord(__int_as_float(0x7f800000));
+        cb[6 * i + 3 + k] = f2ord(-__int_as_float(0x7f800000));
+        box[6 * i + k] = f2ord(__int_as_float(0x7f800000));
+        box[6 * i + 3 + k] = f2ord(-__int_as_float(0x7f800000));
+    }
+}
+
+__device__ __forceinline__ void atomic_bounds(int* b, float4 lo, float4 hi)
+{
+    atomicMin(b + 0, f2ord(lo.x));
+    atomicMin(b + 1, f2ord(lo.y));
+    atomicMin(b + 2, f2ord(lo.z));
+    atomicMax(b + 3, f2ord(hi.x));
+    atomicMax(b + 4, f2ord(hi.y));
+    atomicMax(b + 5, f2ord(hi.z));
+}
+
+__global__ void k_tri_boxes(BvhBuildInput in, Scratch s)
+{
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= in.tri_count)
+        return;
+    uint32_t m = upper_segment(in.mesh_tri_base, in.mesh_count, g);
+    uint32_t local = g - in.mesh_tri_base[m];
+    uint32_t ib = in.mesh_index_offset[m] + 3 * local;
+    uint32_t vb = in.mesh_vertex_offset[m];
+    float4 a = in.vertices[2 * (size_t)(vb + in.indices[ib + 0])];
+    float4 b = in.vertices[2 * (size_t)(vb + in.indices[ib + 1])];
+    float4 c = in.vertices[2 * (size_t)(vb + in.indices[ib + 2])];
+    float4 lo = make_float4(fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y), fminf(fminf(a.z, b.z), c.z), 0.0f);
+    float4 hi = make_float4(fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y), fmaxf(fmaxf(a.z, b.z), c.z), 0.0f);
+    s.lo[g] = lo;
+    s.hi[g] = hi;
+    s.seg[g] = m;
+    float4 cen = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.0f);
+    atomic_bounds(s.seg_cb + 6 * m, cen, cen);
+    atomic_bounds(s.seg_box + 6 * m, lo, hi);
+}
+
+// World box of each instance: the 8 corners of its mesh box under the
+// object-to-world transform, padded.
+__global__ void k_inst_boxes(BvhBuildInput in, const int* mesh_box, Scratch s)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= in.instance_count)
+        return;
+    uint32_t m = in.inst_mesh[i];
+    const int* mb = mesh_box + 6 * m;
+    float blo[3] = {ord2f(mb[0]), ord2f(mb[1]), ord2f(mb[2])};
+    float bhi[3] = {ord2f(mb[3]), ord2f(mb[4]), ord2f(mb[5])};
+    const DevInstanceData& d = in.inst_data[i];
+    float4 rows[3] = {d.t0, d.t1, d.t2};
+    float4 lo = make_float4(__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000), 0.0f);
+    float4 hi = make_float4(-lo.x, -lo.y, -lo.z, 0.0f);
+    if (!(blo[0] <= bhi[0])) {
+        // empty mesh: a point at the instance origin (its BLAS root is empty)
+        lo = make_float4(rows[0].w, rows[1].w, rows[2].w, 0.0f);
+        hi = lo;
+    } else {
+        for (int corner = 0; corner < 8; corner++) {
+            double p[3] = {(corner & 1) ? bhi[0] : blo[0], (corner & 2) ? bhi[1] : blo[1], (corner & 4) ? bhi[2] : blo[2]};
+            float w[3];
+            for (int r = 0; r < 3; r++)
+                w[r] = (float)((double)rows[r].x * p[0] + (double)rows[r].y * p[1] + (double)rows[r].z * p[2] + (double)rows[r].w);
+            lo.x = fminf(lo.x, w[0]);
+            lo.y = fminf(lo.y, w[1]);
+            lo.z = fminf(lo.z, w[2]);
+            hi.x = fmaxf(hi.x, w[0]);
+            hi.y = fmaxf(hi.y, w[1]);
+            hi.z = fmaxf(hi.z, w[2]);
+        }
+    }
+    s.lo[i] = lo;
+    s.hi[i] = hi;
+    s.seg[i] = 0;
+    float4 cen = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.0f);
+    atomic_bounds(s.seg_cb, cen, cen);
+}
+
+__global__ void k_morton(Scratch s, uint32_t n)
+{
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n)
+        return;
+    uint32_t m = s.seg[g];
+    const int* cb = s.seg_cb + 6 * m;
+    float4 lo = s.lo[g], hi = s.hi[g];
+    float c[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
+    uint32_t q[3];
+    for (int k = 0; k < 3; k++) {
+        float a = ord2f(cb[k]), b = ord2f(cb[3 + k]);
+        float x = (b > a) ? (c[k] - a) / (b - a) : 0.0f;
+        x = fminf(fmaxf(x, 0.0f), 1.0f);
+        q[k] = (uint32_t)(x * 65535.0f);
+    }
+    uint64_t code = (expand_bits16(q[0]) << 2) | (expand_bits16(q[1]) << 1) | expand_bits16(q[2]);
+    s.keys_in[g] = ((uint64_t)m << KEY_SEG_SHIFT) | code;
+    s.vals_in[g] = g;
+}
+
+__device__ __forceinline__ int delta(const uint64_t* keys, int n, int i, int j)
+{
+    if (j < 0 || j >= n)
+        return -1;
+    uint64_t a = keys[i], b = keys[j];
+    if (a != b)
+        return __clzll((long long)(a ^ b));
+    return 64 + __clz(i ^ j);
+}
+
+// Karras 2012, Algorithm 1 (node ranges and splits of the binary radix tree).
+__global__ void k_karras(Scratch s, int n, int node_base, int mode_tlas)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1)
+        return;
+    const uint64_t* keys = s.keys_out;
+    int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin)
+        lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin)
+            l += t;
+    int j = i + l * d;
+    int dnode = delta(keys, n, i, j);
+    int sp = 0;
+    for (int div = 2;; div <<= 1) {
+        int t = (l + div - 1) / div;
+        if (delta(keys, n, i, i + (sp + t) * d) > dnode)
+            sp += t;
+        if (t <= 1)
+            break;
+    }
+    int gamma = i + sp * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    int c0 = (lo == gamma) ? ~gamma : gamma;
+    int c1 = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    s.child0[i] = c0;
+    s.child1[i] = c1;
+    if (c0 >= 0)
+        s.parent[c0] = i;
+    else
+        s.leaf_parent[~c0] = i;
+    if (c1 >= 0)
+        s.parent[c1] = i;
+    else
+        s.leaf_parent[~c1] = i;
+    uint32_t seg_lo = (uint32_t)(keys[lo] >> KEY_SEG_SHIFT), seg_hi = (uint32_t)(keys[hi] >> KEY_SEG_SHIFT);
+    // flags: bit 31 marks a node that straddles two segments
+    s.flags[i] = (seg_lo != seg_hi) ? 0x80000000u : 0u;
+    if (seg_lo == seg_hi && (uint32_t)lo == s.seg_base[seg_lo] && (uint32_t)hi + 1 == s.seg_base[seg_lo + 1])
+        s.seg_root[seg_lo] = node_base + i;
+    (void)mode_tlas;
+}
+
+// Segments with zero or one primitive have no internal root.
+__global__ void k_small_roots(Scratch s, uint32_t nseg, int mode_tlas)
+{
+    uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nseg)
+        return;
+    uint32_t b = s.seg_base[m], e = s.seg_base[m + 1];
+    if (e == b)
+        s.seg_root[m] = REF_EMPTY;
+    else if (e - b == 1)
+        s.seg_root[m] = mode_tlas ? make_leaf(s.vals_out[b], 1) : make_leaf(b, 1);
+}
+
+__global__ void k_bottom_up(Scratch s, int n)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= n || n < 2)
+        return;
+    int node = s.leaf_parent[pos];
+    while (node >= 0) {
+        if (s.flags[node] & 0x80000000u)
+            return; // straddling node: above every mesh root
+        __threadfence();
+        uint32_t old = atomicAdd(&s.flags[node], 1u);
+        if ((old & 0xFFu) == 0)
+            return; // first arrival; the sibling finishes this node
+        float4 lo = make_float4(__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000), 0.0f);
+        float4 hi = make_float4(-lo.x, -lo.y, -lo.z, 0.0f);
+        int cs[2] = {s.child0[node], s.child1[node]};
+        for (int k = 0; k < 2; k++) {
+            float4 a, b;
+            if (cs[k] < 0) {
+                uint32_t p = s.vals_out[~cs[k]];
+                a = s.lo[p];
+                b = s.hi[p];
+            } else {
+                a = __ldcg(s.nlo + cs[k]);
+                b = __ldcg(s.nhi + cs[k]);
+            }
+            lo.x = fminf(lo.x, a.x);
+            lo.y = fminf(lo.y, a.y);
+            lo.z = fminf(lo.z, a.z);
+            hi.x = fmaxf(hi.x, b.x);
+            hi.y = fmaxf(hi.y, b.y);
+            hi.z = fmaxf(hi.z, b.z);
+        }
+        __stcg(s.nlo + node, lo);
+        __stcg(s.nhi + node, hi);
+        __threadfence();
+        node = s.parent[node];
+    }
+}
+
+__device__ __forceinline__ void padded(float4 lo, float4 hi, float4& plo, float4& phi)
+{
+    float mag = fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(hi.x)), fmaxf(fabsf(lo.y), fabsf(hi.y))), fmaxf(fabsf(lo.z), fabsf(hi.z)));
+    float eps = mag * 1e-5f + 1e-30f;
+    plo = make_float4(lo.x - eps, lo.y - eps, lo.z - eps, 0.0f);
+    phi = make_float4(hi.x + eps, hi.y + eps, hi.z + eps, 0.0f);
+}
+
+__global__ void k_emit_nodes(Scratch s, int n, BvhNode* nodes, int node_base, int mode_tlas)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1)
+        return;
+    if (s.flags[i] & 0x80000000u)
+        return;
+    int cs[2] = {s.child0[i], s.child1[i]};
+    float4 blo[2], bhi[2];
+    int ref[2];
+    for (int k = 0; k < 2; k++) {
+        float4 a, b;
+        if (cs[k] < 0) {
+            int pos = ~cs[k];
+            uint32_t p = s.vals_out[pos];
+            a = s.lo[p];
+            b = s.hi[p];
+            ref[k] = mode_tlas ? make_leaf(p, 1) : make_leaf((uint32_t)pos, 1);
+        } else {
+            a = s.nlo[cs[k]];
+            b = s.nhi[cs[k]];
+            ref[k] = node_base + cs[k];
+        }
+        padded(a, b, blo[k], bhi[k]);
+    }
+    BvhNode nd;
+    nd.c0xy = make_float4(blo[0].x, bhi[0].x, blo[0].y, bhi[0].y);
+    nd.c1xy = make_float4(blo[1].x, bhi[1].x, blo[1].y, bhi[1].y);
+    nd.c01z = make_float4(blo[0].z, bhi[0].z, blo[1].z, bhi[1].z);
+    nd.link = make_int4(ref[0], ref[1], 0, 0);
+    nodes[node_base + i] = nd;
+}
+
+__global__ void k_write_tris(BvhBuildInput in, Scratch s, TriRec* tris)
+{
+    uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= in.tri_count)
+        return;
+    uint32_t g = s.vals_out[pos];
+    uint32_t m = s.seg[g];
+    uint32_t local = g - in.mesh_tri_base[m];
+    uint32_t ib = in.mesh_index_offset[m] + 3 * local;
+    uint32_t vb = in.mesh_vertex_offset[m];
+    float4 a = in.vertices[2 * (size_t)(vb + in.indices[ib + 0])];
+    float4 b = in.vertices[2 * (size_t)(vb + in.indices[ib + 1])];
+    float4 c = in.vertices[2 * (size_t)(vb + in.indices[ib + 2])];
+    TriRec r;
+    r.v0 = make_float4(a.x, a.y, a.z, __uint_as_float(local));
+    r.v1 = make_float4(b.x, b.y, b.z, 0.0f);
+    r.v2 = make_float4(c.x, c.y, c.z, 0.0f);
+    tris[pos] = r;
+}
+
+__global__ void k_set_roots(BvhBuildInput in, const int* mesh_root, DevInstance* dinst)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= in.instance_count)
+        return;
+    uint32_t m = in.inst_mesh[i];
+    dinst[i].blas_root = m < in.mesh_count ? mesh_root[m] : REF_EMPTY;
+    dinst[i].mesh = m;
+}
+
+inline unsigned blocks(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+
+int bits_for(uint32_t v)
+{
+    int b = 0;
+    while ((1ull << b) < (uint64_t)v)
+        b++;
+    return b;
+}
+
+// Sort + radix tree + boxes + node emission for one key set.
+cudaError_t build_tree(Scratch& s, uint32_t n, uint32_t nseg, BvhNode* nodes, int node_base, int mode_tlas, cudaStream_t st)
+{
+    if (n == 0) {
+        k_small_roots<<<blocks(nseg, 128), 128, 0, st>>>(s, nseg, mode_tlas);
+        return cudaGetLastError();
+    }
+    k_morton<<<blocks(n, 256), 256, 0, st>>>(s, n);
+    int end_bit = KEY_SEG_SHIFT + bits_for(nseg);
+    if (end_bit > 64)
+        return cudaErrorInvalidValue;
+    size_t bytes = s.cub_bytes;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(s.cub_temp, bytes, s.keys_in, s.keys_out, s.vals_in, s.vals_out, (int)n, 0, end_bit, st);
+    if (e != cudaSuccess)
+        return e;
+    cudaMemsetAsync(s.parent, 0xFF, sizeof(int) * n, st);
+    if (n > 1)
+        k_karras<<<blocks(n - 1, 256), 256, 0, st>>>(s, (int)n, node_base, mode_tlas);
+    k_small_roots<<<blocks(nseg, 128), 128, 0, st>>>(s, nseg, mode_tlas);
+    if (n > 1) {
+        k_bottom_up<<<blocks(n, 256), 256, 0, st>>>(s, (int)n);
+        k_emit_nodes<<<blocks(n - 1, 256), 256, 0, st>>>(s, (int)n, nodes, node_base, mode_tlas);
+    }
+    return cudaGetLastError();
+}
+
+} // namespace
+
+size_t bvh_node_count(uint32_t tri_count, uint32_t instance_count)
+{
+    return (size_t)(tri_count > 1 ? tri_count - 1 : 0) + (instance_count > 1 ? instance_count - 1 : 0) + 1;
+}
+
+size_t bvh_scratch_bytes(uint32_t mesh_count, uint32_t tri_count, uint32_t instance_count)
+{
+    uint32_t n = tri_count > instance_count ? tri_count : instance_count;
+    uint32_t nseg = mesh_count > 1 ? mesh_count : 1;
+    return scratch_bytes_for(n, nseg) + 6 * sizeof(int) * (size_t)(nseg + 1) + 512;
+}
+
+cudaError_t bvh_build(const BvhBuildInput& in, BvhBuildOutput& out, void* scratch, size_t scratch_bytes, cudaStream_t st)
+{
+    if (scratch_bytes < bvh_scratch_bytes(in.mesh_count, in.tri_count, in.instance_count))
+        return cudaErrorInvalidValue;
+    uint32_t n_max = in.tri_count > in.instance_count ? in.tri_count : in.instance_count;
+    uint32_t nseg_max = in.mesh_count > 1 ? in.mesh_count : 1;
+    Scratch s = carve_scratch(scratch, n_max, nseg_max);
+    // per-mesh primitive boxes survive the TLAS pass: keep them after the scratch
+    size_t used = (size_t)((char*)s.cub_temp - (char*)scratch) + s.cub_bytes;
+    int* mesh_box = (int*)(((uintptr_t)scratch + used + 255) & ~(uintptr_t)255);
+    cudaError_t e;
+
+    // ---- BLAS: every mesh in one key set
+    if (in.mesh_count > 0) {
+        k_init_bounds<<<blocks(in.mesh_count, 128), 128, 0, st>>>(s.seg_cb, mesh_box, s.seg_root, in.mesh_count);
+        cudaMemcpyAsync(s.seg_base, in.mesh_tri_base, sizeof(uint32_t) * (in.mesh_count + 1), cudaMemcpyDeviceToDevice, st);
+        if (in.tri_count > 0) {
+            Scratch sb = s;
+            sb.seg_box = mesh_box;
+            k_tri_boxes<<<blocks(in.tri_count, 256), 256, 0, st>>>(in, sb);
+        }
+        e = build_tree(s, in.tri_count, in.mesh_count, out.nodes, 0, 0, st);
+        if (e != cudaSuccess)
+            return e;
+        if (in.tri_count > 0)
+            k_write_tris<<<blocks(in.tri_count, 256), 256, 0, st>>>(in, s, out.tris);
+        cudaMemcpyAsync(out.mesh_root, s.seg_root, sizeof(int) * in.mesh_count, cudaMemcpyDeviceToDevice, st);
+    }
+    if (in.instance_count == 0) {
+        out.tlas_root = REF_EMPTY;
+        return cudaGetLastError();
+    }
+    k_set_roots<<<blocks(in.instance_count, 128), 128, 0, st>>>(in, out.mesh_root, out.dinst);
+
+    // ---- TLAS over instance world boxes (one segment)
+    int tlas_base = (int)(in.tri_count > 1 ? in.tri_count - 1 : 0);
+    uint32_t tb[2] = {0, in.instance_count};
+    k_init_bounds<<<1, 32, 0, st>>>(s.seg_cb, s.seg_box, s.seg_root, 1);
+    cudaMemcpyAsync(s.seg_base, tb, sizeof(tb), cudaMemcpyHostToDevice, st);
+    k_inst_boxes<<<blocks(in.instance_count, 128), 128, 0, st>>>(in, mesh_box, s);
+    e = build_tree(s, in.instance_count, 1, out.nodes, tlas_base, 1, st);
+    if (e != cudaSuccess)
+        return e;
+    int root = REF_EMPTY;
+    e = cudaMemcpyAsync(&root, s.seg_root, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess)
+        return e;
+    e = cudaStreamSynchronize(st);
+    out.tlas_root = root;
+    return e;
+}
+
+} // namespace pt

@@ -1,0 +1,425 @@
+// scene.cuh — device-side scene layout and two-level BVH traversal.
+//
+// HBM layout (one allocation per array, all 16-byte aligned):
+//   vertices   float4 x 2 per vertex: the reference's 32-B Vertex (mesh.h:10-18)
+//   indices    u32, mesh-local, 3 per triangle
+//   instances  pt_instance_data, 128 B (scenebuffer.h:13-24)
+//   materials  pt_material, 96 B (material.h:24-29)
+//   light      u32 light-sampler stream (lightsample.cpp:89-221)
+//   nodes      BvhNode, 64 B: both child boxes of a BVH2 node (one array for
+//              every BLAS and the TLAS)
+//   tris       TriRec, 48 B: the three object-space vertices of a triangle in
+//              BVH leaf order plus its mesh-local primitive index
+//   dinst      DevInstance, 64 B: world-to-object rows + BLAS root reference
+// Traversal reads nodes/tris/dinst with 16-byte vector loads through the
+// read-only path.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ptmath.cuh"
+
+namespace pt {
+
+// Child / root reference: >= 0 interior node index; < 0 a leaf holding the
+// primitives (first, count) encoded as ~((first << 2) | (count - 1)), with
+// first < 2^28.  Two sentinels below the leaf range drive the traversal loop.
+constexpr int REF_DONE = (int)0x80000000;
+constexpr int REF_EXIT_BLAS = (int)0x80000001;
+constexpr int REF_EMPTY = (int)0x80000002;
+__host__ __device__ __forceinline__ bool ref_is_leaf(int r) { return r < 0 && r > (int)0x8000000F; }
+__host__ __device__ __forceinline__ int make_leaf(uint32_t first, uint32_t count) { return ~(int)((first << 2) | (count - 1)); }
+__host__ __device__ __forceinline__ uint32_t leaf_first(int r) { return ((uint32_t)~r) >> 2; }
+__host__ __device__ __forceinline__ uint32_t leaf_count(int r) { return (((uint32_t)~r) & 3u) + 1u; }
+
+struct __align__(16) BvhNode {
+    float4 c0xy; // c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y
+    float4 c1xy; // c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y
+    float4 c01z; // c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z
+    int4 link;   // child0, child1, -, -
+};
+
+struct __align__(16) TriRec {
+    float4 v0; // xyz, w = primitive index (bits)
+    float4 v1;
+    float4 v2;
+};
+
+struct __align__(16) DevInstance {
+    float4 w2o[3];   // rows of the world-to-object 3x4 transform
+    int blas_root;   // reference into nodes/tris (REF_EMPTY for an empty mesh)
+    uint32_t flags;  // bit 0: opaque
+    uint32_t mesh;
+    uint32_t pad;
+};
+
+struct DevMaterial {
+    float4 base_colour, emission, rmn, specular, sheen, cc;
+};
+
+struct DevInstanceData {
+    uint32_t vertex_index, index_index, emitter_index, material_index;
+    float4 t0, t1, t2, t3; // transform rows
+    float4 n0, n1, n2;     // normal matrix rows
+};
+
+struct DevScene {
+    const float4* vertices;
+    const uint32_t* indices;
+    const DevInstanceData* inst_data;
+    const DevMaterial* materials;
+    const uint32_t* light;
+    uint32_t light_words;
+    uint32_t light_count;
+    uint32_t instance_count;
+    const BvhNode* nodes;
+    const TriRec* tris;
+    const DevInstance* dinst;
+    int tlas_root;
+    f3 env;
+    uint32_t* error_word; // bit 0: traversal stack overflow
+};
+
+constexpr uint32_t ERR_STACK_OVERFLOW = 1u;
+constexpr uint32_t ERR_BAD_INDEX = 2u;
+constexpr uint32_t ERR_WATCHDOG = 4u;
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+__device__ __forceinline__ int4 ldg4i(const int4* p) { return __ldg(p); }
+
+// Light-stream word with robust-buffer-access semantics (out of range reads 0).
+__device__ __forceinline__ uint32_t lw(const DevScene& s, uint32_t i) { return i < s.light_words ? __ldg(s.light + i) : 0u; }
+
+struct Ray {
+    f3 o, d;
+};
+
+struct ObjRay {
+    f3 o, d;
+    f3 inv_d, o_inv; // 1/d and o/d for the slab test
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+__device__ __forceinline__ void setup_slab(ObjRay& r)
+{
+    r.inv_d = mk3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+    r.o_inv = mk3(r.o.x * r.inv_d.x, r.o.y * r.inv_d.y, r.o.z * r.inv_d.z);
+}
+
+__device__ __forceinline__ void setup_watertight(ObjRay& r)
+{
+    float ax = fabsf(r.d.x), ay = fabsf(r.d.y), az = fabsf(r.d.z);
+    int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz + 1;
+    if (kx == 3)
+        kx = 0;
+    int ky = kx + 1;
+    if (ky == 3)
+        ky = 0;
+    float dz = comp(r.d, kz);
+    if (dz < 0.0f) {
+        int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.sx = comp(r.d, kx) / dz;
+    r.sy = comp(r.d, ky) / dz;
+    r.sz = 1.0f / dz;
+}
+
+// Robust slab test (Ize 2013): far distances are scaled by 1 + 2*gamma(3).
+// Box planes are padded at build time, so NaNs from 0*inf (a ray on a slab
+// plane of a zero direction component) are ignored by fminf/fmaxf safely.
+constexpr float SLAB_SCALE = 1.0f + 2.0f * (3.0f * 0x1p-24f) / (1.0f - 3.0f * 0x1p-24f);
+
+__device__ __forceinline__ float slab_enter(float lo, float hi, float inv, float oinv, float& tfar)
+{
+    float t0 = fmaf(lo, inv, -oinv);
+    float t1 = fmaf(hi, inv, -oinv);
+    tfar = fmaxf(t0, t1) * SLAB_SCALE;
+    return fminf(t0, t1);
+}
+
+// Intersect both children of a node; returns a bitmask (1 = c0, 2 = c1) and
+// the entry distances.
+__device__ __forceinline__ int node_children(const BvhNode* node, const ObjRay& r, float tmin, float tmax, float& e0, float& e1,
+                                             int& c0, int& c1)
+{
+    float4 a = ldg4(&node->c0xy);
+    float4 b = ldg4(&node->c1xy);
+    float4 z = ldg4(&node->c01z);
+    int4 l = ldg4i(&node->link);
+    float f0x, f0y, f0z, f1x, f1y, f1z;
+    float n0x = slab_enter(a.x, a.y, r.inv_d.x, r.o_inv.x, f0x);
+    float n0y = slab_enter(a.z, a.w, r.inv_d.y, r.o_inv.y, f0y);
+    float n0z = slab_enter(z.x, z.y, r.inv_d.z, r.o_inv.z, f0z);
+    float n1x = slab_enter(b.x, b.y, r.inv_d.x, r.o_inv.x, f1x);
+    float n1y = slab_enter(b.z, b.w, r.inv_d.y, r.o_inv.y, f1y);
+    float n1z = slab_enter(z.z, z.w, r.inv_d.z, r.o_inv.z, f1z);
+    e0 = fmaxf(fmaxf(fmaxf(n0x, n0y), n0z), tmin);
+    float x0 = fminf(fminf(fminf(f0x, f0y), f0z), tmax);
+    e1 = fmaxf(fmaxf(fmaxf(n1x, n1y), n1z), tmin);
+    float x1 = fminf(fminf(fminf(f1x, f1y), f1z), tmax);
+    c0 = l.x;
+    c1 = l.y;
+    return (e0 <= x0 ? 1 : 0) | (e1 <= x1 ? 2 : 0);
+}
+
+// Watertight ray/triangle test (Woop, Benthin & Wald 2013) without culling.
+__device__ __forceinline__ bool watertight(const ObjRay& r, f3 p0, f3 p1, f3 p2, float& t, float& b1, float& b2)
+{
+    f3 A = p0 - r.o, B = p1 - r.o, C = p2 - r.o;
+    float Akx = comp(A, r.kx), Aky = comp(A, r.ky), Akz = comp(A, r.kz);
+    float Bkx = comp(B, r.kx), Bky = comp(B, r.ky), Bkz = comp(B, r.kz);
+    float Ckx = comp(C, r.kx), Cky = comp(C, r.ky), Ckz = comp(C, r.kz);
+    float Ax = Akx - r.sx * Akz, Ay = Aky - r.sy * Akz;
+    float Bx = Bkx - r.sx * Bkz, By = Bky - r.sy * Bkz;
+    float Cx = Ckx - r.sx * Ckz, Cy = Cky - r.sy * Ckz;
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f))
+        return false;
+    float det = (U + V) + W;
+    if (det == 0.0f)
+        return false;
+    float Az = r.sz * Akz, Bz = r.sz * Bkz, Cz = r.sz * Ckz;
+    float T = (U * Az + V * Bz) + W * Cz;
+    float inv = 1.0f / det;
+    t = T * inv;
+    b1 = V * inv;
+    b2 = W * inv;
+    return true;
+}
+
+__device__ __forceinline__ void to_object(const DevInstance* di, f3 o, f3 d, ObjRay& r)
+{
+    float4 w0 = ldg4(&di->w2o[0]), w1 = ldg4(&di->w2o[1]), w2 = ldg4(&di->w2o[2]);
+    r.o = mk3(((w0.x * o.x + w0.y * o.y) + w0.z * o.z) + w0.w, ((w1.x * o.x + w1.y * o.y) + w1.z * o.z) + w1.w,
+              ((w2.x * o.x + w2.y * o.y) + w2.z * o.z) + w2.w);
+    r.d = mk3((w0.x * d.x + w0.y * d.y) + w0.z * d.z, (w1.x * d.x + w1.y * d.y) + w1.z * d.z, (w2.x * d.x + w2.y * d.y) + w2.z * d.z);
+    setup_slab(r);
+    setup_watertight(r);
+}
+
+struct Hit {
+    float t, b1, b2;
+    uint32_t inst, prim;
+};
+
+__device__ __forceinline__ bool better(float t, uint32_t inst, uint32_t prim, const Hit& h)
+{
+    if (t < h.t)
+        return true;
+    if (t > h.t)
+        return false;
+    return inst < h.inst || (inst == h.inst && prim < h.prim);
+}
+
+constexpr int STACK_SIZE = 96;
+
+struct TraceCounters {
+    uint32_t nodes, tris;
+};
+
+// Closest hit with the (t, instance, primitive) order of the oracle.  Returns
+// true on a hit.  The stack lives in local memory (L1-resident).
+static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h)
+{
+    h.t = tmax;
+    h.inst = 0xFFFFFFFFu;
+    h.prim = 0xFFFFFFFFu;
+    h.b1 = h.b2 = 0.0f;
+    bool found = false;
+    ObjRay world;
+    world.o = o;
+    world.d = d;
+    setup_slab(world);
+    ObjRay r = world;
+    int stack[STACK_SIZE];
+    int sp = 0;
+    stack[sp++] = REF_DONE;
+    int ref = s.tlas_root;
+    bool in_blas = false;
+    uint32_t cur_inst = 0;
+    if (ref == REF_EMPTY)
+        return false;
+    while (true) {
+        if (ref >= 0) {
+            float e0, e1;
+            int c0, c1;
+            int m = node_children(s.nodes + ref, r, tmin, h.t, e0, e1, c0, c1);
+            if (m == 3) {
+                int near = c0, far = c1;
+                if (e1 < e0) {
+                    near = c1;
+                    far = c0;
+                }
+                if (sp < STACK_SIZE)
+                    stack[sp++] = far;
+                else
+                    atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+                ref = near;
+            } else if (m == 1) {
+                ref = c0;
+            } else if (m == 2) {
+                ref = c1;
+            } else {
+                ref = stack[--sp];
+            }
+            continue;
+        }
+        if (ref == REF_DONE)
+            break;
+        if (ref == REF_EXIT_BLAS) {
+            r = world;
+            in_blas = false;
+            ref = stack[--sp];
+            continue;
+        }
+        uint32_t first = leaf_first(ref), count = leaf_count(ref);
+        if (!in_blas) {
+            // TLAS leaf: instances [first, first + count); one per leaf here.
+            cur_inst = first;
+            const DevInstance* di = s.dinst + cur_inst;
+            int root = __ldg(&di->blas_root);
+            if (root == REF_EMPTY || count != 1) {
+                ref = stack[--sp];
+                continue;
+            }
+            to_object(di, o, d, r);
+            if (sp >= STACK_SIZE) {
+                atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+                ref = stack[--sp];
+                continue;
+            }
+            stack[sp++] = REF_EXIT_BLAS;
+            in_blas = true;
+            ref = root;
+            continue;
+        }
+        for (uint32_t k = 0; k < count; k++) {
+            const TriRec* tr = s.tris + first + k;
+            float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
+            float t, b1, b2;
+            uint32_t prim = __float_as_uint(a.w);
+            if (watertight(r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), t, b1, b2) && t >= tmin && t <= h.t &&
+                better(t, cur_inst, prim, h)) {
+                h.t = t;
+                h.b1 = b1;
+                h.b2 = b2;
+                h.inst = cur_inst;
+                h.prim = prim;
+                found = true;
+            }
+        }
+        ref = stack[--sp];
+    }
+    return found;
+}
+
+// Shadow ray of shadowray.ah.hlsl / shadowray.ms.hlsl: the first opaque hit in
+// [tmin, tmax] occludes; transparent instances attenuate by (1 - alpha).
+// Returns the visibility throughput (0 = occluded).
+static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d, float tmin, float tmax)
+{
+    ObjRay world;
+    world.o = o;
+    world.d = d;
+    setup_slab(world);
+    ObjRay r = world;
+    int stack[STACK_SIZE];
+    int sp = 0;
+    stack[sp++] = REF_DONE;
+    int ref = s.tlas_root;
+    bool in_blas = false;
+    bool opaque = true;
+    float alpha_pass = 1.0f;
+    float throughput = 1.0f;
+    if (ref == REF_EMPTY)
+        return 1.0f;
+    while (true) {
+        if (ref >= 0) {
+            float e0, e1;
+            int c0, c1;
+            int m = node_children(s.nodes + ref, r, tmin, tmax, e0, e1, c0, c1);
+            if (m == 3) {
+                int near = c0, far = c1;
+                if (e1 < e0) {
+                    near = c1;
+                    far = c0;
+                }
+                if (sp < STACK_SIZE)
+                    stack[sp++] = far;
+                else
+                    atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+                ref = near;
+            } else if (m == 1) {
+                ref = c0;
+            } else if (m == 2) {
+                ref = c1;
+            } else {
+                ref = stack[--sp];
+            }
+            continue;
+        }
+        if (ref == REF_DONE)
+            break;
+        if (ref == REF_EXIT_BLAS) {
+            r = world;
+            in_blas = false;
+            ref = stack[--sp];
+            continue;
+        }
+        uint32_t first = leaf_first(ref), count = leaf_count(ref);
+        if (!in_blas) {
+            const DevInstance* di = s.dinst + first;
+            int root = __ldg(&di->blas_root);
+            if (root == REF_EMPTY || count != 1) {
+                ref = stack[--sp];
+                continue;
+            }
+            uint32_t flags = __ldg(&di->flags);
+            opaque = (flags & 1u) != 0;
+            if (!opaque) {
+                uint32_t mi = __ldg(&s.inst_data[first].material_index);
+                alpha_pass = 1.0f - __ldg(&s.materials[mi].base_colour.w);
+            }
+            to_object(di, o, d, r);
+            if (sp >= STACK_SIZE) {
+                atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+                ref = stack[--sp];
+                continue;
+            }
+            stack[sp++] = REF_EXIT_BLAS;
+            in_blas = true;
+            ref = root;
+            continue;
+        }
+        for (uint32_t k = 0; k < count; k++) {
+            const TriRec* tr = s.tris + first + k;
+            float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
+            float t, b1, b2;
+            if (watertight(r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), t, b1, b2) && t >= tmin && t <= tmax) {
+                if (opaque)
+                    return 0.0f;
+                throughput *= alpha_pass;
+                if (throughput < 1e-5f)
+                    return 0.0f;
+            }
+        }
+        ref = stack[--sp];
+    }
+    return throughput < 1e-5f ? 0.0f : throughput;
+}
+
+} // namespace pt

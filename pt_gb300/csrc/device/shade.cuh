@@ -1,0 +1,381 @@
+// shade.cuh — per-segment shading of pt's path tracer on the device.
+//
+// Restates pathtrace.ch.hlsl:159-360 (closest hit, NEE, BSDF sampling),
+// pathtrace.ms.hlsl:6-11 (miss), lightsample.hlsli:13-143 (light sampling),
+// geometry.hlsli:38-69 and pathtrace.hlsli:118-139 (Russian roulette,
+// radiance correction) in the operation order of the HLSL source.
+//
+// The reference traces the NEE shadow ray in the middle of the closest-hit
+// shader.  Here shading stops at that point and returns the shadow ray as a
+// request; BSDF sampling (which does not depend on visibility) runs before
+// the ray is traced, and finish_nee() later adds the light term with the
+// throughput the reference used.  The radiance sum is therefore formed in the
+// reference's order whether the shadow ray is traced inline (megakernel) or
+// in a later stage (wavefront).
+#pragma once
+#include "scene.cuh"
+
+namespace pt {
+
+constexpr uint32_t LIGHT_BIN_SIZE = 10;
+constexpr uint32_t EMITTER_BIN_SIZE = 6;
+constexpr uint32_t LIGHT_TYPE_POINT = 1;
+constexpr uint32_t LIGHT_TYPE_DIRECTIONAL = 2;
+constexpr uint32_t LIGHT_TYPE_EMITTER = 3;
+constexpr uint32_t NO_EMITTER_INDEX = 0xFFFFFFFFu;
+
+// Path state of one pixel sample: the reference's RayPayload
+// (pathtrace.hlsli:36-45) plus the next ray.
+struct PathState {
+    f3 throughput;
+    f3 radiance;
+    float brdf_pdf; // < 0 on the first ray
+    bool final_segment;
+    Sampler smp;
+    f3 next_o, next_d;
+};
+
+// Terms of light_contribution() that remain once the shadow ray is known.
+struct NeeRequest {
+    f3 origin, dir;
+    float tmax;
+    f3 emission, brdf;
+    float w, cos_i, pdf; // w < 0 marks a delta light
+    f3 tp_before;        // path throughput the light term is weighted by
+    bool add;            // the reference adds light_contribution() (maybe 0)
+    bool trace;          // a shadow ray decides the contribution
+};
+
+__device__ __forceinline__ void add_radiance(PathState& p, f3 r) { p.radiance = p.radiance + p.throughput * r; }
+
+__device__ __forceinline__ f3 vpos(const DevScene& s, uint32_t i)
+{
+    float4 a = ldg4(s.vertices + 2 * (size_t)i);
+    return mk3(a.x, a.y, a.z);
+}
+
+struct VertexF {
+    f3 p, n;
+    f2 uv;
+};
+__device__ __forceinline__ VertexF vfetch(const DevScene& s, uint32_t i)
+{
+    float4 a = ldg4(s.vertices + 2 * (size_t)i);
+    float4 b = ldg4(s.vertices + 2 * (size_t)i + 1);
+    VertexF v;
+    v.p = mk3(a.x, a.y, a.z);
+    v.n = mk3(a.w, b.x, b.y);
+    v.uv = f2{b.z, b.w};
+    return v;
+}
+
+__device__ __forceinline__ f3 mul3_rows(float4 r0, float4 r1, float4 r2, f3 v)
+{
+    return mk3((r0.x * v.x + r0.y * v.y) + r0.z * v.z, (r1.x * v.x + r1.y * v.y) + r1.z * v.z, (r2.x * v.x + r2.y * v.y) + r2.z * v.z);
+}
+__device__ __forceinline__ f3 mul_point_rows(float4 r0, float4 r1, float4 r2, f3 p)
+{
+    return mk3(((r0.x * p.x + r0.y * p.y) + r0.z * p.z) + r0.w * 1.0f, ((r1.x * p.x + r1.y * p.y) + r1.z * p.z) + r1.w * 1.0f,
+               ((r2.x * p.x + r2.y * p.y) + r2.z * p.z) + r2.w * 1.0f);
+}
+
+__device__ __forceinline__ uint32_t sample_alias_table(const DevScene& s, uint32_t bin_count, uint32_t bin_size, uint32_t table_offset,
+                                                       float& u, float& p)
+{
+    float ub = u * __uint2float_rn(bin_count);
+    uint32_t i = min(bin_count - 1, __float2uint_rz(ub));
+    uint32_t bin_offset = table_offset + i * bin_size;
+    u = fminf(ub - __uint2float_rn(i), JUST_BELOW_ONE);
+    float q = __uint_as_float(lw(s, bin_offset + 1));
+    if (u < q) {
+        u = fminf(u / q, JUST_BELOW_ONE);
+    } else {
+        i = lw(s, bin_offset + 2);
+        bin_offset = table_offset + i * bin_size;
+        u = fminf((u - q) / (1.0f - q), JUST_BELOW_ONE);
+    }
+    p = __uint_as_float(lw(s, bin_offset + 0));
+    return bin_offset + 3;
+}
+
+__device__ __forceinline__ float light_pdf(const DevScene& s, uint32_t emitter_index, uint32_t primitive_index)
+{
+    if (emitter_index == NO_EMITTER_INDEX)
+        return 0.0f;
+    uint32_t bin_offset = emitter_index * LIGHT_BIN_SIZE;
+    float p = __uint_as_float(lw(s, bin_offset + 0));
+    uint32_t light_type = lw(s, bin_offset + 3);
+    if (light_type == LIGHT_TYPE_EMITTER) {
+        uint32_t table_offset = lw(s, bin_offset + 4);
+        bin_offset = table_offset + primitive_index * EMITTER_BIN_SIZE;
+        p = p * __uint_as_float(lw(s, bin_offset + 0));
+    }
+    return p;
+}
+
+__device__ __forceinline__ f3 material_emission(const DevMaterial* m)
+{
+    float4 e = ldg4(&m->emission);
+    return mk3(e.x, e.y, e.z) * e.w;
+}
+
+__device__ __forceinline__ f3 sample_light(const DevScene& s, Sampler& smp, f3 pt, f3& light_dir, float& light_dist, float& pdf,
+                                           bool& is_delta)
+{
+    float ux = sample_1d(smp);
+    f2 u12 = sample_2d(smp);
+    uint32_t bin_offset = sample_alias_table(s, s.light_count, LIGHT_BIN_SIZE, 0, ux, pdf);
+    uint32_t light_type = lw(s, bin_offset + 0);
+    if (light_type == LIGHT_TYPE_EMITTER) {
+        uint32_t table_offset = lw(s, bin_offset + 1);
+        uint32_t tri_count = lw(s, bin_offset + 2);
+        uint32_t instance_offset = lw(s, bin_offset + 3);
+        uint32_t instance_count = lw(s, bin_offset + 4);
+        float p;
+        bin_offset = sample_alias_table(s, tri_count, EMITTER_BIN_SIZE, table_offset, ux, p);
+        pdf = pdf * p;
+        uint32_t instance_id = instance_offset + min(instance_count - 1, __float2uint_rz(ux * __uint2float_rn(instance_count)));
+        if (instance_id >= s.instance_count) {
+            atomicOr(s.error_word, ERR_BAD_INDEX);
+            light_dist = 0.0f;
+            is_delta = true;
+            return mk3(0.0f, 0.0f, 0.0f);
+        }
+        const DevInstanceData* id = s.inst_data + instance_id;
+        float4 t0 = ldg4(&id->t0), t1 = ldg4(&id->t1), t2 = ldg4(&id->t2);
+        uint32_t vbase = __ldg(&id->vertex_index);
+        f3 pa = mul_point_rows(t0, t1, t2, vpos(s, vbase + lw(s, bin_offset + 0)));
+        f3 pb = mul_point_rows(t0, t1, t2, vpos(s, vbase + lw(s, bin_offset + 1)));
+        f3 pc = mul_point_rows(t0, t1, t2, vpos(s, vbase + lw(s, bin_offset + 2)));
+        f3 bary = random_barycentric(u12);
+        f3 point = (bary.x * pa + bary.y * pb) + bary.z * pc;
+        light_dir = point - pt;
+        light_dist = 1.0f;
+        f3 tn = cross(pb - pa, pc - pa);
+        float area = sqrtf(dot(tn, tn)) * 0.5f;
+        float cosine = fabsf(dot(normalize(light_dir), normalize(tn)));
+        float dist2 = dot(light_dir, light_dir);
+        pdf = pdf * (dist2 / (area * cosine));
+        is_delta = false;
+        if (!isfinite(pdf))
+            return mk3(0.0f, 0.0f, 0.0f);
+        return material_emission(s.materials + __ldg(&id->material_index));
+    } else if (light_type == LIGHT_TYPE_POINT) {
+        f3 lp = mk3(__uint_as_float(lw(s, bin_offset + 1)), __uint_as_float(lw(s, bin_offset + 2)), __uint_as_float(lw(s, bin_offset + 3)));
+        light_dir = lp - pt;
+        light_dist = 1.0f;
+        is_delta = true;
+        f3 col = mk3(__uint_as_float(lw(s, bin_offset + 4)), __uint_as_float(lw(s, bin_offset + 5)), __uint_as_float(lw(s, bin_offset + 6)));
+        return (1.0f / dot(light_dir, light_dir)) * col;
+    } else if (light_type == LIGHT_TYPE_DIRECTIONAL) {
+        light_dir = mk3(__uint_as_float(lw(s, bin_offset + 1)), __uint_as_float(lw(s, bin_offset + 2)), __uint_as_float(lw(s, bin_offset + 3)));
+        light_dist = __int_as_float(0x7f800000);
+        is_delta = true;
+        return mk3(__uint_as_float(lw(s, bin_offset + 4)), __uint_as_float(lw(s, bin_offset + 5)), __uint_as_float(lw(s, bin_offset + 6)));
+    }
+    light_dist = 0.0f;
+    is_delta = true;
+    return mk3(0.0f, 0.0f, 0.0f);
+}
+
+// Miss shader (pathtrace.ms.hlsl:6-11).
+__device__ __forceinline__ void shade_miss(const DevScene& s, PathState& pl)
+{
+    add_radiance(pl, s.env);
+    pl.final_segment = true;
+}
+
+// Closest-hit shader (pathtrace.ch.hlsl:227-360) without the shadow ray.
+__device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 ray_o, f3 ray_d, const Hit& h, NeeRequest& nee)
+{
+    nee.add = false;
+    nee.trace = false;
+    const DevInstanceData* id = s.inst_data + h.inst;
+    const DevInstance* di = s.dinst + h.inst;
+    uint32_t vbase = __ldg(&id->vertex_index);
+    uint32_t ibase = __ldg(&id->index_index);
+    uint32_t emitter_index = __ldg(&id->emitter_index);
+    const DevMaterial* mat = s.materials + __ldg(&id->material_index);
+    uint32_t i0 = __ldg(s.indices + ibase + h.prim * 3 + 0);
+    uint32_t i1 = __ldg(s.indices + ibase + h.prim * 3 + 1);
+    uint32_t i2 = __ldg(s.indices + ibase + h.prim * 3 + 2);
+    VertexF va = vfetch(s, vbase + i0), vb = vfetch(s, vbase + i1), vc = vfetch(s, vbase + i2);
+
+    float ba = (1.0f - h.b1) - h.b2;
+    f3 obj_normal = normalize((ba * va.n + h.b1 * vb.n) + h.b2 * vc.n);
+
+    f3 emission = material_emission(mat);
+    if (maxc(emission) > 0.0f) {
+        float4 w0 = ldg4(&di->w2o[0]), w1 = ldg4(&di->w2o[1]), w2 = ldg4(&di->w2o[2]);
+        f3 obj_dir = mul3_rows(w0, w1, w2, ray_d);
+        if (dot(obj_dir, obj_normal) < 0.0f) {
+            if (pl.brdf_pdf < 0.0f) {
+                add_radiance(pl, emission);
+            } else {
+                float4 t0 = ldg4(&id->t0), t1 = ldg4(&id->t1), t2 = ldg4(&id->t2);
+                f3 wab = mul3_rows(t0, t1, t2, vb.p - va.p);
+                f3 wac = mul3_rows(t0, t1, t2, vc.p - va.p);
+                f3 en = cross(wab, wac);
+                float area = sqrtf(dot(en, en)) * 0.5f;
+                float dist2 = h.t * h.t;
+                float cosine = fabsf(dot(ray_d, normalize(en)));
+                float pdf_l = light_pdf(s, emitter_index, h.prim);
+                pdf_l = pdf_l * (dist2 / (area * cosine));
+                if (pdf_l > 0.0f && dist2 > 0.0f) {
+                    float w = pl.brdf_pdf / (pl.brdf_pdf + pdf_l);
+                    add_radiance(pl, w * emission);
+                }
+            }
+        }
+    }
+    if (pl.final_segment)
+        return;
+
+    float4 bc = ldg4(&mat->base_colour);
+    if (bc.w < sample_1d(pl.smp)) {
+        pl.next_o = ray_o + ray_d * (h.t + ORIGIN_OFFSET);
+        pl.next_d = ray_d;
+        return;
+    }
+    float4 rmn = ldg4(&mat->rmn);
+    float4 spec = ldg4(&mat->specular);
+    float4 sheen = ldg4(&mat->sheen);
+    float anisotropy = __ldg(&mat->cc.z);
+    BrdfInput bi;
+    bi.base_colour = mk3(bc.x, bc.y, bc.z);
+    float roughness = rmn.x;
+    bi.metalness = rmn.y;
+    bi.specular = mk3(spec.x, spec.y, spec.z);
+    bi.sheen = mk3(sheen.x, sheen.y, sheen.z);
+    roughness = fmaxf(0.00001f, roughness * roughness);
+    float aspect = sqrtf(1.0f - 0.9f * fabsf(anisotropy));
+    bi.alpha = f2{roughness / aspect, roughness * aspect};
+    if (anisotropy < 0.0f)
+        bi.alpha = f2{bi.alpha.y, bi.alpha.x};
+
+    // get_vertex_vectors (geometry.hlsli:49-69)
+    f2 duv_ab = {vb.uv.x - va.uv.x, vb.uv.y - va.uv.y};
+    f2 duv_ac = {vc.uv.x - va.uv.x, vc.uv.y - va.uv.y};
+    f3 ab = vb.p - va.p, ac = vc.p - va.p;
+    f3 true_obj_normal = cross(ab, ac);
+    float denom = duv_ab.x * duv_ac.y - duv_ac.x * duv_ab.y;
+    f3 tangent;
+    if (fabsf(denom) < 1e-5f) {
+        tangent = cross(obj_normal, fabsf(obj_normal.y) > 1e-5f ? mk3(1.0f, 0.0f, 0.0f) : mk3(0.0f, 1.0f, 0.0f));
+    } else {
+        tangent = (duv_ac.y * ab - duv_ab.y * ac) / denom;
+        tangent = tangent - dot(tangent, obj_normal) * obj_normal;
+    }
+    f3 bitangent = cross(obj_normal, tangent);
+
+    float4 n0 = ldg4(&id->n0), n1 = ldg4(&id->n1), n2 = ldg4(&id->n2);
+    f3 wx = normalize(mul3_rows(n0, n1, n2, tangent));
+    f3 wy = normalize(mul3_rows(n0, n1, n2, bitangent));
+    f3 wn = normalize(mul3_rows(n0, n1, n2, obj_normal));
+    if (dot(wn, ray_d) > 0.0f) {
+        wx = -wx;
+        wy = -wy;
+        wn = -wn;
+    }
+    f3 twn = normalize(mul3_rows(n0, n1, n2, true_obj_normal));
+    if (dot(ray_d, twn) > 0.0f)
+        twn = -twn;
+    // Normal maps are rejected at upload, so the mapped-normal rotation of
+    // pathtrace.ch.hlsl:322-326 never applies.
+    f3 nd = -ray_d;
+    f3 o = normalize(mk3(dot(wx, nd), dot(wy, nd), dot(wn, nd)));
+    if (o.z <= 0.0f) {
+        pl.final_segment = true;
+        return;
+    }
+    f3 ip = (ray_o + ray_d * h.t) + twn * ORIGIN_OFFSET;
+
+    // light_contribution (pathtrace.ch.hlsl:159-225) up to the shadow ray.
+    nee.add = true;
+    nee.tp_before = pl.throughput;
+    if (s.light_count != 0) {
+        float pdf, light_dist;
+        f3 light_dir;
+        bool is_delta;
+        f3 le = sample_light(s, pl.smp, ip, light_dir, light_dist, pdf, is_delta);
+        if (maxc(le) > 0.0f) {
+            f3 li = mk3(dot(wx, light_dir), dot(wy, light_dir), dot(wn, light_dir));
+            if (li.z > 0.0f) {
+                li = normalize(li);
+                f3 m = normalize(li + o);
+                float pdf_brdf;
+                f3 brdf = evaluate_brdf(bi, li, o, m, pdf_brdf);
+                nee.trace = true;
+                nee.origin = ip;
+                nee.dir = light_dir;
+                nee.tmax = light_dist - 1e-5f;
+                nee.emission = le;
+                nee.brdf = brdf;
+                nee.w = is_delta ? -1.0f : pdf / (pdf + pdf_brdf);
+                nee.cos_i = cos_theta(li);
+                nee.pdf = pdf;
+            }
+        }
+    }
+
+    f3 m;
+    float w, pdf;
+    f3 i = sample_direction(o, bi.alpha, bi.metalness, pl.smp, m, w, pdf);
+    if (i.z * o.z <= 0.0f) {
+        pl.final_segment = true;
+        return;
+    }
+    float pdf_brdf;
+    f3 brdf = evaluate_brdf(bi, i, o, m, pdf_brdf);
+    f3 tp = ((w * brdf) * cos_theta(i)) / pdf;
+    pl.brdf_pdf = pdf_brdf;
+    pl.throughput = pl.throughput * tp;
+    f3 wi = mk3((wx.x * i.x + wy.x * i.y) + wn.x * i.z, (wx.y * i.x + wy.y * i.y) + wn.y * i.z, (wx.z * i.x + wy.z * i.y) + wn.z * i.z);
+    pl.next_o = ip;
+    pl.next_d = normalize(wi);
+}
+
+// Adds light_contribution() to the path radiance given the shadow ray's
+// visibility (1 = unoccluded opaque path, 0 = occluded).
+__device__ __forceinline__ void finish_nee(f3& radiance, const NeeRequest& nee, float vis)
+{
+    if (!nee.add)
+        return;
+    f3 L = mk3(0.0f, 0.0f, 0.0f);
+    if (nee.trace && vis != 0.0f) {
+        f3 e = nee.emission * vis;
+        if (nee.w < 0.0f)
+            L = ((e * nee.brdf) * nee.cos_i) / nee.pdf;
+        else
+            L = (((nee.w * e) * nee.brdf) * nee.cos_i) / nee.pdf;
+    }
+    radiance = radiance + nee.tp_before * L;
+}
+
+__device__ __forceinline__ bool russian_roulette(PathState& pl)
+{
+    f3 T = pl.throughput;
+    float mt = fmaxf(fmaxf(T.x, T.y), T.z);
+    float u = sample_1d(pl.smp);
+    if (mt < 1.0f) {
+        float q = fmaxf(0.0f, 1.0f - mt);
+        if (u < q)
+            return true;
+        float sc = 1.0f / (1.0f - q);
+        pl.throughput = pl.throughput * sc;
+    }
+    return false;
+}
+
+__device__ __forceinline__ f3 correct_radiance(f3 r)
+{
+    if (r.x < 0.0f || !isfinite(r.x))
+        r.x = 0.0f;
+    if (r.y < 0.0f || !isfinite(r.y))
+        r.y = 0.0f;
+    if (r.z < 0.0f || !isfinite(r.z))
+        r.z = 0.0f;
+    return r;
+}
+
+} // namespace pt

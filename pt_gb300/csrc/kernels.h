@@ -1,0 +1,49 @@
+// kernels.h — host-side declarations of the device kernels' launchers.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pt {
+
+struct RenderArgs;
+struct BvhNode;
+struct TriRec;
+struct DevInstance;
+struct DevInstanceData;
+
+cudaError_t launch_megakernel(const RenderArgs& a, cudaStream_t stream);
+
+// Two-level LBVH build on the device (Karras 2012 radix tree per segment).
+struct BvhBuildInput {
+    // BLAS: all meshes at once, one key segment per mesh.
+    const float4* vertices;     // 2 float4 per vertex
+    const uint32_t* indices;    // mesh-local
+    const uint32_t* mesh_vertex_offset;
+    const uint32_t* mesh_index_offset;
+    const uint32_t* mesh_tri_base; // prefix sum of tri counts (mesh_count + 1 entries)
+    uint32_t mesh_count;
+    uint32_t tri_count;
+    // TLAS
+    const DevInstanceData* inst_data;
+    const uint32_t* inst_mesh;
+    uint32_t instance_count;
+};
+
+struct BvhBuildOutput {
+    BvhNode* nodes;      // (tri_count - 1) BLAS nodes followed by TLAS nodes
+    TriRec* tris;        // tri_count records in leaf order
+    DevInstance* dinst;  // blas_root and the world box are filled in
+    int* mesh_root;      // mesh_count
+    int tlas_root;       // host value after the build
+};
+
+// Scratch sizing for bvh_build (bytes).
+size_t bvh_scratch_bytes(uint32_t mesh_count, uint32_t tri_count, uint32_t instance_count);
+size_t bvh_node_count(uint32_t tri_count, uint32_t instance_count);
+
+// Builds everything on `stream`; `scratch` must hold bvh_scratch_bytes().
+// dinst must already hold the world-to-object rows and flags.
+cudaError_t bvh_build(const BvhBuildInput& in, BvhBuildOutput& out, void* scratch, size_t scratch_bytes, cudaStream_t stream);
+
+} // namespace pt

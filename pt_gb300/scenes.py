@@ -1,0 +1,409 @@
+"""Seeded procedural scenes for the headless path, written in the reference's
+drop-in formats: one `.scn` file (camera + objects + instances, README.md:25-52
+of the reference) and one glTF 2.0 file (+ .bin) per object.
+
+Random numbers come from the reference's host generator: xoshiro128++
+(`Xshiro128`) seeded by four Splitmix32 outputs (src/rng.cpp), next_float =
+next() / UINT32_MAX in float32.
+
+Camera convention: the reference starts primary rays at -position and looks
+along -lookdir (src/scene/camera.h:16 + src/pathtrace/pathtrace.cpp:387-388 +
+src/scene/scenebuild.cpp:251-257), so a generator that wants the eye at E
+looking at T writes `position -E` and `lookdir E - T`.
+
+Scenes (configuration names follow the workload they model):
+  small_scene  one 20x20 ground quad, 8 instances of a subdivision-3
+               icosphere (1,280 tris) at xz ~ U[-4,4]^2 with scale U[0.5,1.5],
+               albedo U[0.2,0.8]^3, a 2x2 emissive quad at y=6 (radiance 10),
+               envcol 0.375 0.45 0.9, eye (-1,2,-3), fov 60, pinhole.
+  mid_scene    ~260k instanced triangles from 200 instances of 6 meshes (two
+               displaced 64x64 grids of 8,192 tris, two subdivision-4
+               icospheres of 5,120 tris, two rounded boxes of 1,200 tris), four
+               metallic-roughness materials per mesh (roughness U[0.05,1],
+               metallic Bernoulli(0.3), base colour U[0.1,0.9]^3), 32 emissive
+               triangles with strength log-uniform [1,100], thin lens
+               (lensradius 0.03, focusdist 8).
+"""
+from __future__ import annotations
+
+import json
+import math
+import struct
+from pathlib import Path
+
+import numpy as np
+
+U32 = 0xFFFFFFFF
+
+
+class SceneRng:
+    """Xshiro128 (xoshiro128++) seeded with Splitmix32, as src/rng.cpp."""
+
+    def __init__(self, seed: int):
+        st = seed & U32
+        s = []
+        for _ in range(4):
+            st = (st + 0x9E3779B9) & U32
+            z = st
+            z = ((z ^ (z >> 16)) * 0x85EBCA6B) & U32
+            z = ((z ^ (z >> 13)) * 0xC2B2AE35) & U32
+            s.append(z ^ (z >> 16))
+        self.s = s
+
+    def next(self) -> int:
+        s = self.s
+        rotl = lambda x, k: ((x << k) | (x >> (32 - k))) & U32
+        result = (rotl((s[0] + s[3]) & U32, 7) + s[0]) & U32
+        t = (s[1] << 9) & U32
+        s[2] ^= s[0]
+        s[3] ^= s[1]
+        s[1] ^= s[2]
+        s[0] ^= s[3]
+        s[2] ^= t
+        s[3] = rotl(s[3], 11)
+        return result
+
+    def next_float(self) -> float:
+        return float(np.float32(np.float32(self.next()) / np.float32(4294967295.0)))
+
+    def uniform(self, lo: float, hi: float) -> float:
+        return lo + (hi - lo) * self.next_float()
+
+
+def to_srgb(x: float) -> float:
+    return 12.92 * x if x <= 0.0031308 else 1.055 * x ** (1.0 / 2.4) - 0.055
+
+
+# ---------------------------------------------------------------- meshes
+# Each mesh: (positions (n,3), normals (n,3), uvs (n,2), indices (m,3)) float32/uint32.
+
+def quad(size: float, y: float, facing_down: bool):
+    h = size / 2
+    p = np.array([[-h, y, -h], [h, y, -h], [h, y, h], [-h, y, h]], np.float32)
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    if facing_down:
+        n = np.tile(np.array([[0, -1, 0]], np.float32), (4, 1))
+        idx = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    else:
+        n = np.tile(np.array([[0, 1, 0]], np.float32), (4, 1))
+        idx = np.array([[0, 2, 1], [0, 3, 2]], np.uint32)
+    return p, n, uv, idx
+
+
+def icosphere(subdiv: int):
+    t = (1.0 + 5 ** 0.5) / 2
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [tuple(c / math.sqrt(sum(x * x for x in v)) for c in v) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdiv):
+        cache = {}
+        new_faces = []
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                va, vb = verts[a], verts[b]
+                m = [(va[k] + vb[k]) / 2 for k in range(3)]
+                l = math.sqrt(sum(x * x for x in m))
+                verts.append(tuple(x / l for x in m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            new_faces += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = new_faces
+    p = np.array(verts, np.float32)
+    n = p.copy()
+    u = 0.5 + np.arctan2(p[:, 2], p[:, 0]) / (2 * np.pi)
+    v = np.arccos(np.clip(p[:, 1], -1, 1)) / np.pi
+    uv = np.stack([u, v], 1).astype(np.float32)
+    return p, n, uv, np.array(faces, np.uint32)
+
+
+def displaced_grid(n: int, rng: SceneRng, amplitude: float = 0.08):
+    waves = [(rng.uniform(1, 6), rng.uniform(1, 6), rng.uniform(0, 6.283), rng.uniform(0.3, 1.0)) for _ in range(4)]
+    xs = np.linspace(-1, 1, n + 1, dtype=np.float64)
+    X, Z = np.meshgrid(xs, xs, indexing="xy")
+
+    def height(x, z):
+        return amplitude * sum(a * np.sin(fx * x * 3.1416 + ph) * np.cos(fz * z * 3.1416 - ph) for fx, fz, ph, a in waves)
+
+    Y = height(X, Z)
+    e = 1e-4
+    dx = (height(X + e, Z) - height(X - e, Z)) / (2 * e)
+    dz = (height(X, Z + e) - height(X, Z - e)) / (2 * e)
+    nrm = np.stack([-dx, np.ones_like(dx), -dz], -1)
+    nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
+    p = np.stack([X, Y, Z], -1).reshape(-1, 3).astype(np.float32)
+    uv = np.stack([(X + 1) / 2, (Z + 1) / 2], -1).reshape(-1, 2).astype(np.float32)
+    idx = []
+    for j in range(n):
+        for i in range(n):
+            a = j * (n + 1) + i
+            b, c, d = a + 1, a + n + 1, a + n + 2
+            idx += [(a, c, b), (b, c, d)]
+    return p, nrm.reshape(-1, 3).astype(np.float32), uv, np.array(idx, np.uint32)
+
+
+def rounded_box(k: int, radius: float):
+    """Cube with rounded edges from a k x k grid per face: 12 k^2 triangles."""
+    pts, idx = [], []
+    faces = [(0, 1, 2, 1), (0, 1, 2, -1), (1, 2, 0, 1), (1, 2, 0, -1), (2, 0, 1, 1), (2, 0, 1, -1)]
+    for (ax, bx, nx, sgn) in faces:
+        base = len(pts)
+        for j in range(k + 1):
+            for i in range(k + 1):
+                c = [0.0, 0.0, 0.0]
+                c[ax] = -1 + 2 * i / k
+                c[bx] = -1 + 2 * j / k
+                c[nx] = float(sgn)
+                pts.append(c)
+        for j in range(k):
+            for i in range(k):
+                a = base + j * (k + 1) + i
+                b, cc, d = a + 1, a + k + 1, a + k + 2
+                if sgn > 0:
+                    idx += [(a, b, cc), (b, d, cc)]
+                else:
+                    idx += [(a, cc, b), (b, cc, d)]
+    c = np.array(pts, np.float64)
+    inner = np.clip(c, -(1 - radius), 1 - radius)
+    d = c - inner
+    dn = d / np.maximum(np.linalg.norm(d, axis=1, keepdims=True), 1e-12)
+    p = inner + radius * dn
+    uv = np.zeros((len(p), 2), np.float32)
+    uv[:, 0] = (c[:, 0] + c[:, 2] + 2) / 4
+    uv[:, 1] = (c[:, 1] + 1) / 2
+    return p.astype(np.float32), dn.astype(np.float32), uv, np.array(idx, np.uint32)
+
+
+def triangle(a, b, c):
+    p = np.array([a, b, c], np.float32)
+    nrm = np.cross(p[1] - p[0], p[2] - p[0])
+    nrm = (nrm / np.linalg.norm(nrm)).astype(np.float32)
+    return p, np.tile(nrm[None], (3, 1)), np.array([[0, 0], [1, 0], [0, 1]], np.float32), np.array([[0, 1, 2]], np.uint32)
+
+
+# ---------------------------------------------------------------- writers
+
+def write_gltf(path: Path, mesh, material: dict) -> None:
+    """One mesh, one primitive, one node, one material; external .bin."""
+    p, n, uv, idx = mesh
+    p = np.ascontiguousarray(p, np.float32)
+    n = np.ascontiguousarray(n, np.float32)
+    uv = np.ascontiguousarray(uv, np.float32)
+    idx = np.ascontiguousarray(idx, np.uint32).reshape(-1)
+    blobs = [p.tobytes(), n.tobytes(), uv.tobytes(), idx.tobytes()]
+    offsets, off = [], 0
+    for b in blobs:
+        offsets.append(off)
+        off += (len(b) + 3) // 4 * 4
+    binpath = path.with_suffix(".bin")
+    with open(binpath, "wb") as f:
+        for b in blobs:
+            f.write(b)
+            f.write(b"\0" * ((4 - len(b) % 4) % 4))
+    views = [{"buffer": 0, "byteOffset": o, "byteLength": len(b)} for o, b in zip(offsets, blobs)]
+    acc = [
+        {"bufferView": 0, "componentType": 5126, "count": len(p), "type": "VEC3",
+         "min": p.min(0).tolist(), "max": p.max(0).tolist()},
+        {"bufferView": 1, "componentType": 5126, "count": len(n), "type": "VEC3"},
+        {"bufferView": 2, "componentType": 5126, "count": len(uv), "type": "VEC2"},
+        {"bufferView": 3, "componentType": 5125, "count": len(idx), "type": "SCALAR"},
+    ]
+    base = [float(to_srgb(c)) for c in material.get("base", (0.8, 0.8, 0.8))] + [1.0]
+    mat = {"pbrMetallicRoughness": {"baseColorFactor": base, "metallicFactor": float(material.get("metallic", 0.0)),
+                                    "roughnessFactor": float(material.get("roughness", 1.0))}}
+    strength = float(material.get("emission_strength", 0.0))
+    if strength > 0:
+        mat["emissiveFactor"] = [1.0, 1.0, 1.0]
+        mat["extensions"] = {"KHR_materials_emissive_strength": {"emissiveStrength": strength}}
+    doc = {
+        "asset": {"version": "2.0", "generator": "pt_gb300.scenes"},
+        "scene": 0, "scenes": [{"nodes": [0]}], "nodes": [{"mesh": 0}],
+        "meshes": [{"name": path.stem, "primitives": [{"attributes": {"POSITION": 0, "NORMAL": 1, "TEXCOORD_0": 2},
+                                                        "indices": 3, "material": 0}]}],
+        "materials": [mat],
+        "accessors": acc, "bufferViews": views,
+        "buffers": [{"uri": binpath.name, "byteLength": off}],
+    }
+    if strength > 0:
+        doc["extensionsUsed"] = ["KHR_materials_emissive_strength"]
+    path.write_text(json.dumps(doc))
+
+
+def fmt(x: float) -> str:
+    return repr(float(np.float32(x)))
+
+
+class ScnWriter:
+    def __init__(self, camera: dict, env):
+        self.camera = camera
+        self.env = env
+        self.objects = []   # (identifier, relative path)
+        self.instances = []  # (identifier, [transform lines])
+
+    def add_object(self, ident: str, rel: str):
+        self.objects.append((ident, rel))
+
+    def add_instance(self, ident: str, scale=None, rotate=None, translate=None):
+        lines = []
+        if scale is not None:
+            lines.append("s " + " ".join(fmt(v) for v in scale))
+        if rotate is not None:
+            lines.append("r " + " ".join(fmt(v) for v in rotate))
+        if translate is not None:
+            lines.append("t " + " ".join(fmt(v) for v in translate))
+        self.instances.append((ident, lines))
+
+    def write(self, path: Path):
+        eye, target = np.array(self.camera["eye"], np.float64), np.array(self.camera["target"], np.float64)
+        out = ["camera:", "position " + " ".join(fmt(-v) for v in eye),
+               "lookdir " + " ".join(fmt(v) for v in (eye - target)), "fov " + fmt(self.camera.get("fov", 45.0))]
+        for key in ("near", "far", "focusdist", "lensradius", "exposure"):
+            if key in self.camera:
+                out.append(f"{key} {fmt(self.camera[key])}")
+        out.append("envcol " + " ".join(fmt(v) for v in self.env))
+        out.append("")
+        out.append("objects:")
+        for ident, rel in self.objects:
+            out.append(f"{ident} {rel}")
+        out.append("")
+        for ident, lines in self.instances:
+            out.append(ident)
+            out += lines
+            out.append("")
+        path.write_text("\n".join(out) + "\n")
+
+
+# ---------------------------------------------------------------- configurations
+
+def small_scene(out_dir: Path, seed: int = 0) -> Path:
+    out_dir = Path(out_dir)
+    out_dir.mkdir(parents=True, exist_ok=True)
+    rng = SceneRng(seed)
+    albedo = lambda: tuple(rng.uniform(0.2, 0.8) for _ in range(3))
+    write_gltf(out_dir / "ground.gltf", quad(20.0, 0.0, False), {"base": albedo(), "roughness": 1.0, "metallic": 0.0})
+    write_gltf(out_dir / "sphere.gltf", icosphere(3), {"base": albedo(), "roughness": 1.0, "metallic": 0.0})
+    write_gltf(out_dir / "light.gltf", quad(2.0, 6.0, True),
+               {"base": (0.0, 0.0, 0.0), "roughness": 1.0, "metallic": 0.0, "emission_strength": 10.0})
+    scn = ScnWriter({"eye": (-1.0, 2.0, -3.0), "target": (0.0, 0.75, 0.0), "fov": 60.0}, (0.375, 0.45, 0.9))
+    for name in ("ground", "sphere", "light"):
+        scn.add_object(name, f"{name}.gltf")
+    scn.add_instance("ground")
+    for _ in range(8):
+        x, z, s = rng.uniform(-4, 4), rng.uniform(-4, 4), rng.uniform(0.5, 1.5)
+        scn.add_instance("sphere", scale=(s, s, s), translate=(x, s, z))
+    scn.add_instance("light")
+    path = out_dir / "small.scn"
+    scn.write(path)
+    return path
+
+
+def mid_scene(out_dir: Path, seed: int = 1) -> Path:
+    out_dir = Path(out_dir)
+    out_dir.mkdir(parents=True, exist_ok=True)
+    rng = SceneRng(seed)
+    meshes = {
+        "grid0": displaced_grid(64, rng), "grid1": displaced_grid(64, rng),
+        "sphere0": icosphere(4), "sphere1": icosphere(4),
+        "box0": rounded_box(10, 0.15), "box1": rounded_box(10, 0.3),
+    }
+    palettes = {}
+    scn = ScnWriter({"eye": (0.0, 5.0, -22.0), "target": (0.0, 1.0, 0.0), "fov": 45.0, "focusdist": 8.0,
+                     "lensradius": 0.03}, (0.2, 0.25, 0.4))
+    for name, mesh in meshes.items():
+        palettes[name] = []
+        for k in range(4):
+            mat = {"base": tuple(rng.uniform(0.1, 0.9) for _ in range(3)), "roughness": rng.uniform(0.05, 1.0),
+                   "metallic": 1.0 if rng.next_float() < 0.3 else 0.0}
+            ident = f"{name}_m{k}"
+            write_gltf(out_dir / f"{ident}.gltf", mesh, mat)
+            palettes[name].append(ident)
+    used = set()
+    instances = []
+    # terrain tiles
+    for i, name in enumerate(("grid0", "grid1")):
+        instances.append((palettes[name][rng.next() % 4], (10.0, 10.0, 10.0), None, (-10.0 + 20.0 * i, 0.0, 0.0)))
+    for name in ("sphere0", "sphere1"):
+        s = rng.uniform(1.5, 3.0)
+        instances.append((palettes[name][rng.next() % 4], (s, s, s), None, (rng.uniform(-12, 12), s, rng.uniform(-4, 8))))
+    for i in range(196):
+        name = "box0" if i % 2 == 0 else "box1"
+        s = rng.uniform(0.3, 1.0)
+        axis = (rng.uniform(-1, 1), rng.uniform(-1, 1), rng.uniform(-1, 1))
+        angle = rng.uniform(1e-5, 2 * math.pi)
+        pos = (rng.uniform(-18, 18), s + rng.uniform(0.0, 1.5), rng.uniform(-8, 9))
+        instances.append((palettes[name][rng.next() % 4], (s, s, s), axis + (angle,), pos))
+    for ident, s, r, t in instances:
+        used.add(ident)
+    for name, idents in palettes.items():
+        for ident in idents:
+            if ident in used:
+                scn.add_object(ident, f"{ident}.gltf")
+    for ident, s, r, t in instances:
+        scn.add_instance(ident, scale=s, rotate=r, translate=t)
+    for e in range(32):
+        cx, cy, cz = rng.uniform(-16, 16), rng.uniform(6, 10), rng.uniform(-6, 10)
+        size = rng.uniform(0.6, 1.4)
+        a = (cx - size, cy, cz - size * 0.5)
+        b = (cx + size, cy, cz - size * 0.5)
+        c = (cx, cy, cz + size)
+        strength = math.exp(rng.uniform(math.log(1.0), math.log(100.0)))
+        ident = f"emitter{e}"
+        write_gltf(out_dir / f"{ident}.gltf", triangle(a, c, b),
+                   {"base": (0.0, 0.0, 0.0), "roughness": 1.0, "metallic": 0.0, "emission_strength": strength})
+        scn.add_object(ident, f"{ident}.gltf")
+        scn.add_instance(ident)
+    path = out_dir / "mid.scn"
+    scn.write(path)
+    return path
+
+
+def tiny_raw(kind: str = "two_tris") -> tuple[dict, dict]:
+    """Very small raw scenes for exhaustive parity tests (no files)."""
+    mats = []
+
+    def material(base, rough=0.5, metal=0.0, emission=0.0, alpha=1.0):
+        m = np.zeros(24, np.float32)
+        m[0:3] = base
+        m[3] = alpha
+        m[4:7] = 1.0 if emission > 0 else 0.0
+        m[7] = emission if emission > 0 else 1.0
+        m[8] = rough
+        m[9] = metal
+        bits = (1 << 13) if alpha < 1.0 else 0
+        m[11] = np.frombuffer(np.uint32(bits).tobytes(), np.float32)[0]
+        m[12:15] = 0.5
+        m[21] = 0.5
+        mats.append(m)
+        return len(mats) - 1
+
+    meshes = []
+    if kind == "two_tris":
+        meshes.append((quad(4.0, 0.0, False), material((0.7, 0.6, 0.5), 0.6, 0.0), [np.eye(4, dtype=np.float32)]))
+        meshes.append((quad(1.0, 2.0, True), material((0.0, 0.0, 0.0), emission=5.0), [np.eye(4, dtype=np.float32)]))
+    else:
+        raise ValueError(kind)
+    v, idx, ranges, mm, mio, inst = [], [], [], [], [0], []
+    voff = ioff = 0
+    for (p, n, uv, ix), mat, insts in meshes:
+        v.append(np.concatenate([p, n, uv], 1))
+        idx.append(ix.reshape(-1))
+        ranges.append((voff, ioff, len(ix), len(p)))
+        voff += len(p)
+        ioff += ix.size
+        mm.append(mat)
+        for M in insts:
+            inst.append(np.asarray(M, np.float32).T.reshape(-1))  # column-major
+        mio.append(mio[-1] + len(insts))
+    raw = {"vertices": np.concatenate(v).astype(np.float32), "indices": np.concatenate(idx).astype(np.uint32),
+           "meshes": np.array(ranges, np.uint32), "mesh_material": np.array(mm, np.uint32),
+           "mesh_instance_offset": np.array(mio, np.uint32), "instance_matrices": np.array(inst, np.float32),
+           "materials": np.array(mats, np.float32), "environment_colour": np.array([0.1, 0.15, 0.3], np.float32)}
+    cam = {"position": (0.0, -1.5, -4.0), "lookdir": (0.0, 0.35, -1.0), "fov_degrees": 50.0}
+    return raw, cam

@@ -1,0 +1,31 @@
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); runs the CUDA path through the C ABI")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def native_build():
+    """Make sure the oracle and the product library are built (fast no-op when up to date)."""
+    import oracle
+    from pt_gb300 import build as native
+    oracle.build()
+    native.build()
+    yield
+
+
+@pytest.fixture(scope="session")
+def has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
