@@ -740,6 +740,14 @@ struct or_scene {
         return {v[0], v[1], v[2]};
     }
     uint32_t lw(uint64_t i) const { return i < light.size() ? light[i] : 0u; } // robust buffer access
+    // Position for an index read from the light stream, with robust buffer
+    // access (zeros outside the vertex array).
+    V3 position_robust(uint64_t i) const
+    {
+        if (i >= vertices.size() / PT_VERTEX_FLOATS)
+            return {0.0f, 0.0f, 0.0f};
+        return position((uint32_t)i);
+    }
 };
 
 namespace {
@@ -1012,12 +1020,9 @@ V3 sample_light(const or_scene& s, Sampler& smp, V3 pt, V3& light_dir, float& li
             return v3(0, 0, 0);
         }
         const pt_instance_data& id = s.instances[instance_id].data;
-        Vertex va = s.vertex(id.vertex_index + s.lw(bin_offset + 0));
-        Vertex vb = s.vertex(id.vertex_index + s.lw(bin_offset + 1));
-        Vertex vc = s.vertex(id.vertex_index + s.lw(bin_offset + 2));
-        V3 pa = mul_point(id.transform, va.position);
-        V3 pb = mul_point(id.transform, vb.position);
-        V3 pc = mul_point(id.transform, vc.position);
+        V3 pa = mul_point(id.transform, s.position_robust((uint64_t)id.vertex_index + s.lw(bin_offset + 0)));
+        V3 pb = mul_point(id.transform, s.position_robust((uint64_t)id.vertex_index + s.lw(bin_offset + 1)));
+        V3 pc = mul_point(id.transform, s.position_robust((uint64_t)id.vertex_index + s.lw(bin_offset + 2)));
         V3 bary = random_barycentric(u12);
         V3 point = (bary.x * pa + bary.y * pb) + bary.z * pc;
         light_dir = point - pt;

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -155,6 +156,84 @@ struct pt_ctx {
 };
 
 static thread_local std::string g_create_error;
+
+// Host-side structural check of a freshly built acceleration structure
+// (enabled by PT_VALIDATE_BVH=1): every reference in range, every BLAS
+// covering each of its mesh's triangles exactly once, the TLAS covering each
+// instance exactly once, and no cycles.  Returns an empty string when valid.
+static std::string validate_accel(pt_ctx* c, const std::vector<uint32_t>& tri_base)
+{
+    const uint32_t T = c->tri_count, I = c->instance_count, M = c->mesh_count;
+    const size_t blas_nodes = T > 1 ? T - 1 : 0;
+    std::vector<BvhNode> nodes(c->nodes.n);
+    std::vector<TriRec> tris(T);
+    std::vector<int> roots(M);
+    std::vector<DevInstance> dinst(I);
+    if (cudaMemcpy(nodes.data(), c->nodes.p, nodes.size() * sizeof(BvhNode), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        (T && cudaMemcpy(tris.data(), c->tris.p, T * sizeof(TriRec), cudaMemcpyDeviceToHost) != cudaSuccess) ||
+        (M && cudaMemcpy(roots.data(), c->mesh_root.p, M * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) ||
+        (I && cudaMemcpy(dinst.data(), c->dinst.p, I * sizeof(DevInstance), cudaMemcpyDeviceToHost) != cudaSuccess))
+        return "copy-back failed";
+    std::vector<uint8_t> seen(std::max<size_t>(T, I), 0);
+    auto walk = [&](int root, size_t node_lo, size_t node_hi, uint32_t leaf_lo, uint32_t leaf_hi, uint32_t expect) -> std::string {
+        std::vector<int> st{root};
+        size_t internal = 0;
+        uint32_t leaves = 0;
+        while (!st.empty()) {
+            int r = st.back();
+            st.pop_back();
+            if (r >= 0) {
+                if ((size_t)r < node_lo || (size_t)r >= node_hi)
+                    return "node reference " + std::to_string(r) + " out of range";
+                if (++internal > (size_t)expect)
+                    return "cycle or duplicate nodes";
+                st.push_back(nodes[r].link.x);
+                st.push_back(nodes[r].link.y);
+            } else if (ref_is_leaf(r)) {
+                uint32_t f = leaf_first(r), n = leaf_count(r);
+                if (f < leaf_lo || f + n > leaf_hi)
+                    return "leaf range out of bounds";
+                for (uint32_t k = f; k < f + n; k++) {
+                    if (seen[k]++)
+                        return "primitive referenced twice";
+                }
+                leaves += n;
+            } else {
+                return "sentinel inside the tree";
+            }
+        }
+        return leaves == expect ? "" : "tree covers " + std::to_string(leaves) + " of " + std::to_string(expect) + " primitives";
+    };
+    for (uint32_t m = 0; m < M; m++) {
+        uint32_t n = tri_base[m + 1] - tri_base[m];
+        if (n == 0) {
+            if (roots[m] != REF_EMPTY)
+                return "empty mesh with a root";
+            continue;
+        }
+        std::string e = walk(roots[m], 0, blas_nodes, tri_base[m], tri_base[m + 1], n);
+        if (!e.empty())
+            return "mesh " + std::to_string(m) + ": " + e;
+        for (uint32_t k = tri_base[m]; k < tri_base[m + 1]; k++) {
+            uint32_t prim;
+            std::memcpy(&prim, &tris[k].v0.w, 4);
+            if (prim >= n)
+                return "mesh " + std::to_string(m) + ": primitive index out of range";
+        }
+    }
+    std::fill(seen.begin(), seen.end(), 0);
+    if (I > 0) {
+        std::string e = walk(c->tlas_root, blas_nodes, blas_nodes + (I > 1 ? I - 1 : 0), 0, I, I);
+        if (!e.empty())
+            return "TLAS: " + e;
+        std::vector<uint32_t> im(I);
+        cudaMemcpy(im.data(), c->inst_mesh.p, I * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        for (uint32_t i = 0; i < I; i++)
+            if (dinst[i].blas_root != roots[im[i]])
+                return "instance " + std::to_string(i) + " has the wrong BLAS root";
+    }
+    return "";
+}
 
 template <typename T>
 static cudaError_t upload(pt_ctx* c, DevBuf<T>& b, const T* src, size_t n)
@@ -409,6 +488,14 @@ int pt_build_accel(pt_ctx* c, pt_accel_info* info)
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->tlas_root = out.tlas_root;
+    const char* validate = std::getenv("PT_VALIDATE_BVH");
+    if (validate && validate[0] == '1') {
+        std::vector<uint32_t> tb(c->mesh_count + 1);
+        cudaMemcpy(tb.data(), c->mesh_tri_base.p, tb.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        std::string problem = validate_accel(c, tb);
+        if (!problem.empty())
+            return c->fail(PT_ERR_DEVICE, "BVH validation: " + problem);
+    }
     c->accel_ok = true;
     c->accel.blas_count = c->mesh_count;
     c->accel.tlas_nodes = c->instance_count > 1 ? c->instance_count - 1 : 0;
@@ -475,6 +562,10 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     a.s.light_words = c->light_words;
     a.s.light_count = c->light_count;
     a.s.instance_count = c->instance_count;
+    a.s.vertex_count = c->vertex_count;
+    // A traversal of a valid BVH visits each node at most once; the cap only
+    // stops a malformed tree from spinning.
+    a.s.max_iterations = 4u * (uint32_t)std::min<size_t>(c->nodes.n + c->tri_count + c->instance_count, 1u << 28) + 4096u;
     a.s.nodes = c->nodes.p;
     a.s.tris = c->tris.p;
     a.s.dinst = c->dinst.p;

@@ -72,6 +72,8 @@ struct DevScene {
     uint32_t light_words;
     uint32_t light_count;
     uint32_t instance_count;
+    uint32_t vertex_count;
+    uint32_t max_iterations; // traversal watchdog: loop iterations per ray
     const BvhNode* nodes;
     const TriRec* tris;
     const DevInstance* dinst;
@@ -253,7 +255,12 @@ static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d,
     uint32_t cur_inst = 0;
     if (ref == REF_EMPTY)
         return false;
-    while (true) {
+    for (uint32_t iter = 0;; iter++) {
+        if (iter >= s.max_iterations) {
+            // A well-formed BVH never gets here; a malformed one must not hang the GPU.
+            atomicOr(s.error_word, ERR_WATCHDOG);
+            break;
+        }
         if (ref >= 0) {
             float e0, e1;
             int c0, c1;
@@ -347,7 +354,12 @@ static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d,
     float throughput = 1.0f;
     if (ref == REF_EMPTY)
         return 1.0f;
-    while (true) {
+    for (uint32_t iter = 0;; iter++) {
+        if (iter >= s.max_iterations) {
+            // A well-formed BVH never gets here; a malformed one must not hang the GPU.
+            atomicOr(s.error_word, ERR_WATCHDOG);
+            break;
+        }
         if (ref >= 0) {
             float e0, e1;
             int c0, c1;

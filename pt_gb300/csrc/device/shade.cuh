@@ -48,8 +48,13 @@ struct NeeRequest {
 
 __device__ __forceinline__ void add_radiance(PathState& p, f3 r) { p.radiance = p.radiance + p.throughput * r; }
 
-__device__ __forceinline__ f3 vpos(const DevScene& s, uint32_t i)
+// Vertex position for an index taken from the light stream.  The reference
+// reads through robust buffer access (out-of-range reads return zero), which
+// this reproduces instead of reading outside the vertex array.
+__device__ __forceinline__ f3 vpos(const DevScene& s, uint64_t i)
 {
+    if (i >= (uint64_t)s.vertex_count)
+        return mk3(0.0f, 0.0f, 0.0f);
     float4 a = ldg4(s.vertices + 2 * (size_t)i);
     return mk3(a.x, a.y, a.z);
 }
@@ -136,7 +141,7 @@ __device__ __forceinline__ f3 sample_light(const DevScene& s, Sampler& smp, f3 p
         pdf = pdf * p;
         uint32_t instance_id = instance_offset + min(instance_count - 1, __float2uint_rz(ux * __uint2float_rn(instance_count)));
         if (instance_id >= s.instance_count) {
-            atomicOr(s.error_word, ERR_BAD_INDEX);
+            // outside the instance buffer: robust access yields no light
             light_dist = 0.0f;
             is_delta = true;
             return mk3(0.0f, 0.0f, 0.0f);
@@ -144,9 +149,9 @@ __device__ __forceinline__ f3 sample_light(const DevScene& s, Sampler& smp, f3 p
         const DevInstanceData* id = s.inst_data + instance_id;
         float4 t0 = ldg4(&id->t0), t1 = ldg4(&id->t1), t2 = ldg4(&id->t2);
         uint32_t vbase = __ldg(&id->vertex_index);
-        f3 pa = mul_point_rows(t0, t1, t2, vpos(s, vbase + lw(s, bin_offset + 0)));
-        f3 pb = mul_point_rows(t0, t1, t2, vpos(s, vbase + lw(s, bin_offset + 1)));
-        f3 pc = mul_point_rows(t0, t1, t2, vpos(s, vbase + lw(s, bin_offset + 2)));
+        f3 pa = mul_point_rows(t0, t1, t2, vpos(s, (uint64_t)vbase + lw(s, bin_offset + 0)));
+        f3 pb = mul_point_rows(t0, t1, t2, vpos(s, (uint64_t)vbase + lw(s, bin_offset + 1)));
+        f3 pc = mul_point_rows(t0, t1, t2, vpos(s, (uint64_t)vbase + lw(s, bin_offset + 2)));
         f3 bary = random_barycentric(u12);
         f3 point = (bary.x * pa + bary.y * pb) + bary.z * pc;
         light_dir = point - pt;

@@ -37,7 +37,12 @@ U32 = 0xFFFFFFFF
 
 
 class SceneRng:
-    """Xshiro128 (xoshiro128++) seeded with Splitmix32, as src/rng.cpp."""
+    """Xshiro128 (xoshiro128++) seeded with Splitmix32, as src/rng.cpp.
+
+    Seeded the way the reference's only call site does it
+    (lightsample.cpp:45-46, `Xshiro128 rng(seeder.next(), ... x4)`): with
+    GCC's right-to-left evaluation of the arguments, the state holds the four
+    Splitmix32 outputs in reverse order."""
 
     def __init__(self, seed: int):
         st = seed & U32
@@ -48,7 +53,7 @@ class SceneRng:
             z = ((z ^ (z >> 16)) * 0x85EBCA6B) & U32
             z = ((z ^ (z >> 13)) * 0xC2B2AE35) & U32
             s.append(z ^ (z >> 16))
-        self.s = s
+        self.s = s[::-1]
 
     def next(self) -> int:
         s = self.s

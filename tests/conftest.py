@@ -1,7 +1,11 @@
+import os
 import sys
 from pathlib import Path
 
 import pytest
+
+# every BVH built during the tests is checked on the host for structure
+os.environ.setdefault("PT_VALIDATE_BVH", "1")
 
 ROOT = Path(__file__).resolve().parent.parent
 if str(ROOT) not in sys.path:
