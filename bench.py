@@ -52,8 +52,10 @@ WORKLOAD = "mid scene: 1024x1024, 128 spp, max 8 bounces, ~260k tris / 200 insta
 #         + (N_node * 64 + N_tri * 36) * (1 + p_nee)
 # with N_node, N_tri the mean interior-node visits and triangle tests per ray
 # of the oracle's binned-SAH BVH2 over the first sample of the image, and
-# p_nee the shadow rays per segment (measured by tests/test_bseg.py).
-BSEG = {"mid": {"n_node": None, "n_tri": None, "p_nee": None}}
+# p_nee the shadow rays per segment (measured by tests/test_bseg.py, which
+# checks these constants against the oracle).
+BSEG = {"mid": {"n_node": 27.2106, "n_tri": 9.0453, "p_nee": 0.2336},
+        "small": {"n_node": 13.7945, "n_tri": 6.0748, "p_nee": 0.5218}}
 
 
 def bseg_bytes(m: dict) -> float | None:
@@ -296,29 +298,31 @@ def run_ours(args) -> None:
     value = total_segs / t_dev / 1e6
 
     # ---- end to end through the C ABI with host buffers
-    img = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.float32).pin_memory()
-    e2e_ctx = P.Context(device_index)
-    e2e_ctx.upload(pview)
-    e2e_ctx.build_accel()
-    e2e_ctx.render(params(4))
-    e2e_ctx.read_image(out=img.numpy())
-    if dist:
-        tdist.barrier()
-    torch.cuda.synchronize()
-    e0 = time.perf_counter()
-    for _ in range(args.steps):
+    t_e2e = float("nan")
+    if not args.no_e2e:
+        img = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.float32).pin_memory()
+        e2e_ctx = P.Context(device_index)
         e2e_ctx.upload(pview)
         e2e_ctx.build_accel()
-        e2e_ctx.render(params(), stats=False)
+        e2e_ctx.render(params(4))
         e2e_ctx.read_image(out=img.numpy())
-    torch.cuda.synchronize()
-    t_e2e = time.perf_counter() - e0
-    if dist:
-        t = torch.tensor([t_e2e], device=f"cuda:{device_index}")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+        if dist:
+            tdist.barrier()
+        torch.cuda.synchronize()
+        e0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_ctx.upload(pview)
+            e2e_ctx.build_accel()
+            e2e_ctx.render(params(), stats=False)
+            e2e_ctx.read_image(out=img.numpy())
+        torch.cuda.synchronize()
+        t_e2e = time.perf_counter() - e0
+        if dist:
+            t = torch.tensor([t_e2e], device=f"cuda:{device_index}")
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        e2e_ctx.close()
     e2e_value = total_segs / t_e2e / 1e6
-    e2e_ctx.close()
 
     if rank == 0:
         peaks = measured_peaks()
@@ -339,7 +343,11 @@ def run_ours(args) -> None:
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB write, outside the event pairs)",
                            "parallelism": f"replicas x{world} (disjoint sample ranges)", "kernel": "megakernel",
-                           "segments_per_step": int(segs_per_step), "accel_build_ms": info.build_ms},
+                           "segments_per_step": int(segs_per_step), "accel_build_ms": info.build_ms,
+                           "image": f"{WIDTH}x{HEIGHT}", "spp": SPP,
+                           "node_visits_per_ray": st.node_visits / max(1, st.segments + st.shadow_rays),
+                           "tri_tests_per_ray": st.tri_tests / max(1, st.segments + st.shadow_rays),
+                           "shadow_rays_per_segment": st.shadow_rays / max(1, st.segments)},
                 "e2e": {"value": e2e_value, "unit": "Mpath-segs/s", "h2d_bytes_per_step": int(scene_bytes),
                         "d2h_bytes_per_step": int(HEIGHT * WIDTH * 16), "ms_per_step": 1000.0 * t_e2e / args.steps,
                         "includes": "scene upload + BVH build + render + image read-back"},
@@ -362,7 +370,13 @@ def main():
     ap.add_argument("--kernel", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--width", type=int, default=1024, help="smaller images only for profiling captures")
+    ap.add_argument("--height", type=int, default=1024)
+    ap.add_argument("--spp", type=int, default=128)
     args = ap.parse_args()
+    global WIDTH, HEIGHT, SPP
+    WIDTH, HEIGHT, SPP = args.width, args.height, args.spp
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -162,6 +162,8 @@ typedef struct pt_render_stats {
     uint64_t segments;        /* traced primary + extension rays           */
     uint64_t shadow_rays;     /* traced NEE shadow rays                    */
     uint64_t paths;           /* pixel samples                             */
+    uint64_t node_visits;     /* BVH interior nodes whose children were tested */
+    uint64_t tri_tests;       /* ray/triangle tests                        */
     float milliseconds;       /* device time of the render (CUDA events)   */
     uint32_t kernel_launches; /* kernels launched by the call              */
     uint32_t kernel_used;     /* PT_KERNEL_MEGA or PT_KERNEL_WAVEFRONT     */

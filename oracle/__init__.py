@@ -90,6 +90,7 @@ def lib():
         L.or_meansq64.restype = C.c_double
         L.or_meansq64.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_uint32, C.c_uint32]
         L.or_max_threads.restype = C.c_int
+        L.or_tonemap.argtypes = [C.POINTER(C.c_float), C.c_uint64]
         _lib = L
     return _lib
 

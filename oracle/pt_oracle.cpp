@@ -1858,7 +1858,9 @@ double or_meansq(const float* ref, const float* img, uint32_t w, uint32_t h)
     for (size_t i = 0; i < (size_t)w * h * 4; i++) {
         if ((i % 4) == 3)
             continue;
-        double e = (double)img[i] - (double)ref[i];
+        // meansq.cpp:39: `double error = image[i] - reference[i];` — the
+        // difference is taken in float, then widened.
+        double e = (double)(img[i] - ref[i]);
         sse += e * e;
     }
     return sse / ((double)w * h * 3 - 1);
@@ -1877,3 +1879,38 @@ double or_meansq64(const double* ref, const float* img, uint32_t w, uint32_t h)
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------- tone map (tonemap.cs.hlsl:17-77)
+// ACES fit of the reference (src_is_srgb = false, dst_is_srgb = true, as
+// ptdispatch.cpp:29 configures it): sRGB encode with the reference's
+// threshold 0.00031308, sRGB->RRT matrix, RRT/ODT rational fit, ODT->sRGB
+// matrix, saturate.  Alpha is passed through.
+namespace {
+inline float to_srgb_f(float x) { return x <= 0.00031308f ? 12.92f * x : 1.055f * std::pow(x, 1.0f / 2.4f) - 0.055f; }
+} // namespace
+
+extern "C" void or_tonemap(float* rgba, uint64_t pixels)
+{
+    static const float A[3][3] = {{0.59719f, 0.35458f, 0.04823f}, {0.07600f, 0.90834f, 0.01566f}, {0.02840f, 0.13383f, 0.83777f}};
+    static const float B[3][3] = {{1.60475f, -0.53108f, -0.07367f}, {-0.10208f, 1.10813f, -0.00605f}, {-0.00327f, -0.07276f, 1.07602f}};
+    for (uint64_t p = 0; p < pixels; p++) {
+        float* c = rgba + 4 * p;
+        float s[3] = {to_srgb_f(c[0]), to_srgb_f(c[1]), to_srgb_f(c[2])};
+        float r[3], o[3];
+        for (int i = 0; i < 3; i++)
+            r[i] = (A[i][0] * s[0] + A[i][1] * s[1]) + A[i][2] * s[2];
+        for (int i = 0; i < 3; i++) {
+            float v = r[i];
+            float a = v * (v + 0.0245786f) - 0.000090537f;
+            float b = v * (0.983729f * v + 0.4329510f) + 0.238081f;
+            r[i] = a / b;
+        }
+        for (int i = 0; i < 3; i++)
+            o[i] = (B[i][0] * r[0] + B[i][1] * r[1]) + B[i][2] * r[2];
+        for (int i = 0; i < 3; i++)
+            c[i] = std::fmin(std::fmax(o[i], 0.0f), 1.0f); // saturate (NaN -> 0)
+        for (int i = 0; i < 3; i++)
+            if (std::isnan(o[i]))
+                c[i] = 0.0f;
+    }
+}

@@ -111,6 +111,9 @@ double or_meansq64(const double* reference_rgb_mean, const float* image_rgba, ui
 
 int or_max_threads(void);
 
+/* ACES tone map of tonemap.cs.hlsl:17-77 in place (src linear, dst sRGB). */
+void or_tonemap(float* rgba, uint64_t pixels);
+
 #ifdef __cplusplus
 }
 #endif

@@ -75,7 +75,7 @@ class RenderParams(C.Structure):
 
 class RenderStats(C.Structure):
     _fields_ = [("segments", C.c_uint64), ("shadow_rays", C.c_uint64), ("paths", C.c_uint64),
-                ("milliseconds", C.c_float), ("kernel_launches", C.c_uint32), ("kernel_used", C.c_uint32),
+                ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64), ("milliseconds", C.c_float), ("kernel_launches", C.c_uint32), ("kernel_used", C.c_uint32),
                 ("error_word", C.c_uint32)]
 
 

@@ -141,6 +141,8 @@ struct pt_ctx {
     bool have_fp64 = false;
     DevBuf<unsigned long long> counters;
     DevBuf<uint32_t> error_word;
+    DevBuf<float4> mse_ref;     // reference image for pt_mse_host
+    DevBuf<double> mse_partial; // [0] result, [1..] per-block partial sums
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
     int fail(int code, const std::string& msg)
@@ -274,7 +276,7 @@ pt_ctx* pt_create(int device)
     c->device = device;
     if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess ||
-        (e = c->counters.alloc(4)) != cudaSuccess || (e = c->error_word.alloc(1)) != cudaSuccess) {
+        (e = c->counters.alloc(8)) != cudaSuccess || (e = c->error_word.alloc(1)) != cudaSuccess) {
         g_create_error = std::string("context set-up: ") + cudaGetErrorString(e);
         delete c;
         return nullptr;
@@ -315,6 +317,8 @@ void pt_destroy(pt_ctx* c)
     c->sum64.release();
     c->counters.release();
     c->error_word.release();
+    c->mse_ref.release();
+    c->mse_partial.release();
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -586,7 +590,7 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     a.image = c->image.p;
     a.sum64 = fp64 ? c->sum64.p : nullptr;
     a.counters = c->counters.p;
-    cudaMemsetAsync(c->counters.p, 0, 4 * sizeof(unsigned long long), c->stream);
+    cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
     // Split long renders so no single launch covers more than 2^26 path samples.
     uint64_t pixels = (uint64_t)p->width * p->height;
     uint32_t per_launch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->samples, (1ull << 26) / pixels));
@@ -607,7 +611,7 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
         cudaError_t e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess)
             return c->cuda_fail(e, "render");
-        unsigned long long cnt[4];
+        unsigned long long cnt[8];
         uint32_t ew = 0;
         cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost);
         cudaMemcpy(&ew, c->error_word.p, sizeof(ew), cudaMemcpyDeviceToHost);
@@ -616,6 +620,8 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
         stats->segments = cnt[0];
         stats->shadow_rays = cnt[1];
         stats->paths = cnt[2];
+        stats->node_visits = cnt[3];
+        stats->tri_tests = cnt[4];
         stats->milliseconds = ms;
         stats->kernel_launches = launches;
         stats->kernel_used = PT_KERNEL_MEGA;
@@ -674,14 +680,34 @@ int pt_tonemap(pt_ctx* c)
 {
     if (!c)
         return PT_ERR_INVALID;
-    return c->fail(PT_ERR_UNSUPPORTED, "tone map not built yet");
+    if (!c->image.p)
+        return c->fail(PT_ERR_STATE, "nothing rendered");
+    cudaSetDevice(c->device);
+    cudaError_t e = launch_tonemap(c->image.p, c->width * c->height, c->stream);
+    if (e != cudaSuccess)
+        return c->cuda_fail(e, "tone map");
+    return PT_OK;
 }
 
 int pt_mse_host(pt_ctx* c, const float* ref, double* mse)
 {
     if (!c || !ref || !mse)
         return PT_ERR_INVALID;
-    return c->fail(PT_ERR_UNSUPPORTED, "device MSE not built yet");
+    if (!c->image.p)
+        return c->fail(PT_ERR_STATE, "nothing rendered");
+    cudaSetDevice(c->device);
+    size_t n = (size_t)c->width * c->height;
+    cudaError_t e;
+    if (c->mse_ref.n < n && (e = c->mse_ref.alloc(n)) != cudaSuccess)
+        return c->cuda_fail(e, "MSE reference allocation");
+    if (!c->mse_partial.p && (e = c->mse_partial.alloc(MSE_MAX_BLOCKS + 1)) != cudaSuccess)
+        return c->cuda_fail(e, "MSE scratch allocation");
+    if ((e = cudaMemcpyAsync(c->mse_ref.p, ref, n * sizeof(float4), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
+        (e = launch_mse(c->image.p, c->mse_ref.p, c->width, c->height, c->mse_partial.p + 1, c->mse_partial.p, c->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(mse, c->mse_partial.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
+        return c->cuda_fail(e, "MSE");
+    return PT_OK;
 }
 
 } // extern "C"

@@ -35,14 +35,14 @@ __device__ __forceinline__ int f2ord(float f)
 }
 __device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
 
-__device__ __forceinline__ uint64_t expand_bits16(uint32_t v)
+// Spread the 16 bits of v to every third bit (bit b -> bit 3b), 48 bits wide.
+__host__ __device__ __forceinline__ uint64_t expand_bits16(uint32_t v)
 {
     uint64_t x = v & 0xFFFFu;
-    x = (x | (x << 32)) & 0x0000FFFF0000FFFFull; // not needed for 16 bits but harmless
-    x = (x | (x << 16)) & 0x00FF0000FF0000FFull;
-    x = (x | (x << 8)) & 0xF00F00F00F00F00Full;
-    x = (x | (x << 4)) & 0x30C30C30C30C30C3ull;
-    x = (x | (x << 2)) & 0x9249249249249249ull;
+    x = (x | (x << 16)) & 0x0000FF0000FFull;
+    x = (x | (x << 8)) & 0x00F00F00F00Full;
+    x = (x | (x << 4)) & 0x0C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x249249249249ull;
     return x;
 }
 

@@ -12,7 +12,7 @@ struct RenderArgs {
     uint32_t width, height, sample_index, samples, max_bounces, rr_start;
     float4* image;          // RGBA32F running mean (the accumulation image)
     double* sum64;          // optional FP64 sums: rgb + sample count per pixel
-    unsigned long long* counters; // [0] segments, [1] shadow rays, [2] paths
+    unsigned long long* counters; // [0] segments, [1] shadow rays, [2] paths, [3] node visits, [4] triangle tests
 };
 
 // sample_camera_ray (sample.hlsli:258-280)

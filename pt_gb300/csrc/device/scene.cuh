@@ -218,6 +218,12 @@ struct Hit {
     uint32_t inst, prim;
 };
 
+// Traversal work of one ray: interior nodes whose child boxes were tested and
+// ray/triangle tests.
+struct TraceCounters {
+    uint32_t nodes, tris;
+};
+
 __device__ __forceinline__ bool better(float t, uint32_t inst, uint32_t prim, const Hit& h)
 {
     if (t < h.t)
@@ -229,14 +235,11 @@ __device__ __forceinline__ bool better(float t, uint32_t inst, uint32_t prim, co
 
 constexpr int STACK_SIZE = 96;
 
-struct TraceCounters {
-    uint32_t nodes, tris;
-};
-
 // Closest hit with the (t, instance, primitive) order of the oracle.  Returns
 // true on a hit.  The stack lives in local memory (L1-resident).
-static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h)
+static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
 {
+    uint32_t n_nodes = 0, n_tris = 0;
     h.t = tmax;
     h.inst = 0xFFFFFFFFu;
     h.prim = 0xFFFFFFFFu;
@@ -264,6 +267,7 @@ static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d,
         if (ref >= 0) {
             float e0, e1;
             int c0, c1;
+            n_nodes++;
             int m = node_children(s.nodes + ref, r, tmin, h.t, e0, e1, c0, c1);
             if (m == 3) {
                 int near = c0, far = c1;
@@ -314,6 +318,7 @@ static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d,
             ref = root;
             continue;
         }
+        n_tris += count;
         for (uint32_t k = 0; k < count; k++) {
             const TriRec* tr = s.tris + first + k;
             float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
@@ -331,14 +336,17 @@ static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d,
         }
         ref = stack[--sp];
     }
+    tc.nodes += n_nodes;
+    tc.tris += n_tris;
     return found;
 }
 
 // Shadow ray of shadowray.ah.hlsl / shadowray.ms.hlsl: the first opaque hit in
 // [tmin, tmax] occludes; transparent instances attenuate by (1 - alpha).
 // Returns the visibility throughput (0 = occluded).
-static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d, float tmin, float tmax)
+static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d, float tmin, float tmax, TraceCounters& tc)
 {
+    uint32_t n_nodes = 0, n_tris = 0;
     ObjRay world;
     world.o = o;
     world.d = d;
@@ -363,6 +371,7 @@ static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d,
         if (ref >= 0) {
             float e0, e1;
             int c0, c1;
+            n_nodes++;
             int m = node_children(s.nodes + ref, r, tmin, tmax, e0, e1, c0, c1);
             if (m == 3) {
                 int near = c0, far = c1;
@@ -417,20 +426,27 @@ static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d,
             ref = root;
             continue;
         }
+        n_tris += count;
         for (uint32_t k = 0; k < count; k++) {
             const TriRec* tr = s.tris + first + k;
             float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
             float t, b1, b2;
             if (watertight(r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), t, b1, b2) && t >= tmin && t <= tmax) {
-                if (opaque)
-                    return 0.0f;
+                if (opaque) {
+                    throughput = 0.0f;
+                    break;
+                }
                 throughput *= alpha_pass;
                 if (throughput < 1e-5f)
-                    return 0.0f;
+                    break;
             }
         }
+        if (throughput == 0.0f || throughput < 1e-5f)
+            break;
         ref = stack[--sp];
     }
+    tc.nodes += n_nodes;
+    tc.tris += n_tris;
     return throughput < 1e-5f ? 0.0f : throughput;
 }
 

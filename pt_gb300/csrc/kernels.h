@@ -14,6 +14,15 @@ struct DevInstanceData;
 
 cudaError_t launch_megakernel(const RenderArgs& a, cudaStream_t stream);
 
+// Output stage (post.cu).
+constexpr uint32_t MSE_MAX_BLOCKS = 152 * 8; // partial sums: one per block
+cudaError_t launch_tonemap(float4* img, uint32_t n, cudaStream_t stream);
+uint32_t mse_blocks(uint32_t pixels);
+// meansq of RGB: writes SSE / (w*h*3 - 1) to *out (device); `partial` holds
+// mse_blocks(w*h) doubles of scratch.
+cudaError_t launch_mse(const float4* img, const float4* ref, uint32_t width, uint32_t height, double* partial, double* out,
+                       cudaStream_t stream);
+
 // Two-level LBVH build on the device (Karras 2012 radix tree per segment).
 struct BvhBuildInput {
     // BLAS: all meshes at once, one key segment per mesh.

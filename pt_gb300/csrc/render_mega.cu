@@ -5,7 +5,8 @@
 
 namespace pt {
 
-__device__ __forceinline__ void shade_segment(const DevScene& s, PathState& pl, f3 ro, f3 rd, bool hit, const Hit& h, uint32_t& shadow_rays)
+__device__ __forceinline__ void shade_segment(const DevScene& s, PathState& pl, f3 ro, f3 rd, bool hit, const Hit& h, uint32_t& shadow_rays,
+                                              TraceCounters& tc)
 {
     if (!hit) {
         shade_miss(s, pl);
@@ -16,7 +17,7 @@ __device__ __forceinline__ void shade_segment(const DevScene& s, PathState& pl, 
     float vis = 0.0f;
     if (nee.trace) {
         shadow_rays++;
-        vis = trace_shadow(s, nee.origin, nee.dir, 0.0f, nee.tmax);
+        vis = trace_shadow(s, nee.origin, nee.dir, 0.0f, nee.tmax, tc);
     }
     finish_nee(pl.radiance, nee, vis);
 }
@@ -26,6 +27,7 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
     const uint32_t px = blockIdx.x * 16 + (threadIdx.x & 15);
     const uint32_t py = blockIdx.y * 8 + (threadIdx.x >> 4);
     uint32_t segments = 0, shadow_rays = 0, paths = 0;
+    TraceCounters tc{0u, 0u};
     if (px < a.width && py < a.height) {
         const size_t pix = (size_t)py * a.width + px;
         float4 acc = a.image[pix];
@@ -52,8 +54,8 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
             paths++;
             segments++;
             Hit h;
-            bool hit = trace_closest(s, ro, rd, a.near_plane, a.far_plane, h);
-            shade_segment(s, pl, ro, rd, hit, h, shadow_rays);
+            bool hit = trace_closest(s, ro, rd, a.near_plane, a.far_plane, h, tc);
+            shade_segment(s, pl, ro, rd, hit, h, shadow_rays, tc);
             if (!pl.final_segment) {
                 for (uint32_t seg = 1; seg <= a.max_bounces; seg++) {
                     sampler_start(pl.smp, px, py, si, seg + 1);
@@ -61,8 +63,8 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
                     rd = pl.next_d;
                     pl.final_segment = seg >= a.max_bounces;
                     segments++;
-                    hit = trace_closest(s, ro, rd, 0.0f, __int_as_float(0x7f800000), h);
-                    shade_segment(s, pl, ro, rd, hit, h, shadow_rays);
+                    hit = trace_closest(s, ro, rd, 0.0f, __int_as_float(0x7f800000), h, tc);
+                    shade_segment(s, pl, ro, rd, hit, h, shadow_rays, tc);
                     if (pl.final_segment)
                         break;
                     if (seg >= a.rr_start && russian_roulette(pl))
@@ -89,10 +91,14 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
     segments = __reduce_add_sync(mask, segments);
     shadow_rays = __reduce_add_sync(mask, shadow_rays);
     paths = __reduce_add_sync(mask, paths);
+    uint32_t nodes = __reduce_add_sync(mask, tc.nodes);
+    uint32_t tris = __reduce_add_sync(mask, tc.tris);
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(a.counters + 0, (unsigned long long)segments);
         atomicAdd(a.counters + 1, (unsigned long long)shadow_rays);
         atomicAdd(a.counters + 2, (unsigned long long)paths);
+        atomicAdd(a.counters + 3, (unsigned long long)nodes);
+        atomicAdd(a.counters + 4, (unsigned long long)tris);
     }
 }
 

@@ -410,5 +410,6 @@ def tiny_raw(kind: str = "two_tris") -> tuple[dict, dict]:
            "meshes": np.array(ranges, np.uint32), "mesh_material": np.array(mm, np.uint32),
            "mesh_instance_offset": np.array(mio, np.uint32), "instance_matrices": np.array(inst, np.float32),
            "materials": np.array(mats, np.float32), "environment_colour": np.array([0.1, 0.15, 0.3], np.float32)}
-    cam = {"position": (0.0, -1.5, -4.0), "lookdir": (0.0, 0.35, -1.0), "fov_degrees": 50.0}
+    # eye (0, 1.5, 4) looking at the origin: position -eye, lookdir eye - target
+    cam = {"position": (0.0, -1.5, -4.0), "lookdir": (0.0, 1.5, 4.0), "fov_degrees": 50.0}
     return raw, cam
