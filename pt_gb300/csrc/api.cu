@@ -141,6 +141,9 @@ struct pt_ctx {
     bool have_fp64 = false;
     DevBuf<unsigned long long> counters;
     DevBuf<uint32_t> error_word;
+    DevBuf<char> wave_state;    // wavefront path state
+    uint32_t wave_paths = 0;    // paths the wave state holds
+    int sm_count = 0;
     DevBuf<float4> mse_ref;     // reference image for pt_mse_host
     DevBuf<double> mse_partial; // [0] result, [1..] per-block partial sums
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -283,7 +286,9 @@ pt_ctx* pt_create(int device)
     }
     uint32_t table[4][32];
     sobol_table(table);
-    if ((e = render_init_tables(&table[0][0], c->stream)) != cudaSuccess) {
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if ((e = render_init_tables(&table[0][0], c->stream)) != cudaSuccess ||
+        (e = wave_init_tables(&table[0][0], c->stream)) != cudaSuccess) {
         g_create_error = std::string("sampler tables: ") + cudaGetErrorString(e);
         delete c;
         return nullptr;
@@ -319,6 +324,7 @@ void pt_destroy(pt_ctx* c)
     c->error_word.release();
     c->mse_ref.release();
     c->mse_partial.release();
+    c->wave_state.release();
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -591,18 +597,39 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     a.sum64 = fp64 ? c->sum64.p : nullptr;
     a.counters = c->counters.p;
     cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
-    // Split long renders so no single launch covers more than 2^26 path samples.
     uint64_t pixels = (uint64_t)p->width * p->height;
-    uint32_t per_launch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->samples, (1ull << 26) / pixels));
+    uint32_t kernel = p->kernel == PT_KERNEL_MEGA ? PT_KERNEL_MEGA : PT_KERNEL_WAVEFRONT;
     uint32_t launches = 0;
+    if (kernel == PT_KERNEL_WAVEFRONT) {
+        // Waves of k samples, k * pixels <= 2^21 paths (at least one sample).
+        uint64_t k = std::max<uint64_t>(1, std::min<uint64_t>(p->samples, (1ull << 21) / pixels));
+        uint64_t n = k * pixels;
+        if (c->wave_paths < n) {
+            cudaError_t e = c->wave_state.alloc(wave_state_bytes((uint32_t)n));
+            if (e != cudaSuccess)
+                return c->cuda_fail(e, "wavefront state allocation");
+            c->wave_paths = (uint32_t)n;
+        }
+    }
     cudaEventRecord(c->ev0, c->stream);
-    for (uint32_t done = 0; done < p->samples; done += per_launch) {
-        a.sample_index = p->sample_index + done;
-        a.samples = std::min(per_launch, p->samples - done);
-        cudaError_t e = launch_megakernel(a, c->stream);
+    if (kernel == PT_KERNEL_MEGA) {
+        // Split long renders so no single launch covers more than 2^26 path samples.
+        uint32_t per_launch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->samples, (1ull << 26) / pixels));
+        for (uint32_t done = 0; done < p->samples; done += per_launch) {
+            a.sample_index = p->sample_index + done;
+            a.samples = std::min(per_launch, p->samples - done);
+            cudaError_t e = launch_megakernel(a, c->stream);
+            if (e != cudaSuccess)
+                return c->cuda_fail(e, "render launch");
+            launches++;
+        }
+    } else {
+        a.sample_index = p->sample_index;
+        a.samples = p->samples;
+        uint32_t n_paths = (uint32_t)(std::min<uint64_t>(c->wave_paths / pixels, p->samples) * pixels);
+        cudaError_t e = launch_wavefront(a, c->wave_state.p, c->wave_state.n, n_paths, c->sm_count, &launches, c->stream);
         if (e != cudaSuccess)
-            return c->cuda_fail(e, "render launch");
-        launches++;
+            return c->cuda_fail(e, "wavefront launch");
     }
     cudaEventRecord(c->ev1, c->stream);
     c->samples_done = p->sample_index + p->samples;
@@ -624,7 +651,7 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
         stats->tri_tests = cnt[4];
         stats->milliseconds = ms;
         stats->kernel_launches = launches;
-        stats->kernel_used = PT_KERNEL_MEGA;
+        stats->kernel_used = kernel;
         stats->error_word = ew;
         if (ew != 0)
             return c->fail(PT_ERR_DEVICE, "device error word " + std::to_string(ew));

@@ -237,7 +237,7 @@ constexpr int STACK_SIZE = 96;
 
 // Closest hit with the (t, instance, primitive) order of the oracle.  Returns
 // true on a hit.  The stack lives in local memory (L1-resident).
-static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
+static __device__ __forceinline__ bool trace_closest_inl(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
 {
     uint32_t n_nodes = 0, n_tris = 0;
     h.t = tmax;
@@ -344,7 +344,7 @@ static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d,
 // Shadow ray of shadowray.ah.hlsl / shadowray.ms.hlsl: the first opaque hit in
 // [tmin, tmax] occludes; transparent instances attenuate by (1 - alpha).
 // Returns the visibility throughput (0 = occluded).
-static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d, float tmin, float tmax, TraceCounters& tc)
+static __device__ __forceinline__ float trace_shadow_inl(const DevScene& s, f3 o, f3 d, float tmin, float tmax, TraceCounters& tc)
 {
     uint32_t n_nodes = 0, n_tris = 0;
     ObjRay world;
@@ -448,6 +448,17 @@ static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d,
     tc.nodes += n_nodes;
     tc.tris += n_tris;
     return throughput < 1e-5f ? 0.0f : throughput;
+}
+
+// Out-of-line copies for the megakernel (keeps its code size down); the
+// wavefront traversal kernels inline the traversal instead.
+static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
+{
+    return trace_closest_inl(s, o, d, tmin, tmax, h, tc);
+}
+static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d, float tmin, float tmax, TraceCounters& tc)
+{
+    return trace_shadow_inl(s, o, d, tmin, tmax, tc);
 }
 
 } // namespace pt

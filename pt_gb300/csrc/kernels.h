@@ -14,6 +14,14 @@ struct DevInstanceData;
 
 cudaError_t launch_megakernel(const RenderArgs& a, cudaStream_t stream);
 
+// Wavefront path tracer (render_wave.cu).  `state` holds wave_state_bytes(n)
+// bytes of path state for up to n_paths_max paths (a multiple of the pixel
+// count); r.samples samples are rendered in waves of n_paths_max / pixels.
+size_t wave_state_bytes(uint32_t n_paths_max);
+cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
+                             uint32_t* launches, cudaStream_t stream);
+cudaError_t wave_init_tables(const uint32_t* table128, cudaStream_t stream);
+
 // Output stage (post.cu).
 constexpr uint32_t MSE_MAX_BLOCKS = 152 * 8; // partial sums: one per block
 cudaError_t launch_tonemap(float4* img, uint32_t n, cudaStream_t stream);

@@ -1,0 +1,397 @@
+// render_wave.cu — wavefront path tracer.
+//
+// A wave renders `k` consecutive samples of every pixel: N = k * W * H paths.
+// Path state lives in structure-of-arrays buffers indexed by path id; stages
+// exchange compact queues of path ids:
+//
+//   raygen      camera rays of all N paths (pathtrace.rg.hlsl:18-35)
+//   extend      closest hit of every queued path (TraceRay, rg.hlsl:35,51)
+//   shade       hit/miss shading up to the NEE shadow ray, BSDF sampling and
+//               Russian roulette (pathtrace.ch.hlsl:227-360, ms.hlsl,
+//               pathtrace.hlsli:118-139); pushes continuing paths and shadow
+//               requests with warp-aggregated atomics (ballot + popc)
+//   shadow      any-hit traversal + the light term (ch.hlsl:190-224)
+//   accumulate  running mean of the wave's samples in sample order
+//               (rg.hlsl:59-67), optional FP64 sums
+//
+// The per-segment sampler needs no stored state: the reference restarts it at
+// every segment from (pixel, sample, segment + 1) (rg.hlsl:45), so `shade`
+// restarts it itself.  Radiance terms are added in the reference's order: the
+// shadow stage of segment s runs before the shade stage of segment s + 1.
+// Queue lengths stay on the device; every kernel reads its own count, so the
+// host issues a fixed sequence of launches per wave (CUDA-graph friendly).
+#include "device/render.cuh"
+#include "kernels.h"
+
+namespace pt {
+
+struct WaveState {
+    // per path
+    float4* ray_o;      // xyz origin, w = tmin
+    float4* ray_d;      // xyz direction, w = tmax
+    float4* tp;         // throughput xyz, w = brdf pdf (< 0 on the first ray)
+    float4* rad;        // radiance xyz, w unused
+    uint32_t* seg;      // current segment index
+    float4* hit;        // t, b1, b2, bits(inst)
+    uint32_t* hit_prim; // primitive, ~0 for a miss
+    // NEE requests (per path, valid when queued in the shadow queue)
+    float4* nee_o;      // origin, w = tmax
+    float4* nee_d;      // direction, w = w (< 0: delta light)
+    float4* nee_e;      // emission, w = cos_i
+    float4* nee_b;      // brdf, w = pdf
+    float4* nee_tp;     // throughput before the BSDF update
+    // queues
+    uint32_t* queue[2];
+    uint32_t* shadow_queue;
+    uint32_t* counts;   // [0],[1] path queues, [2] shadow queue, [3] work fetch, [4] shadow fetch
+};
+
+struct WaveArgs {
+    RenderArgs r;
+    WaveState w;
+    uint32_t wave_first_sample; // sample index of path ids [0, W*H)
+    uint32_t wave_samples;      // k
+    uint32_t pixels;            // W * H
+    uint32_t n_paths;           // k * W * H
+};
+
+__device__ __forceinline__ void push_warp(uint32_t* queue, uint32_t* count, bool pred, uint32_t value)
+{
+    unsigned mask = __ballot_sync(__activemask(), pred);
+    if (mask == 0)
+        return;
+    unsigned lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == (unsigned)leader)
+        base = atomicAdd(count, (uint32_t)__popc(mask));
+    base = __shfl_sync(__activemask(), base, leader);
+    if (pred)
+        queue[base + __popc(mask & ((1u << lane) - 1u))] = value;
+}
+
+__global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs a)
+{
+    const RenderArgs& R = a.r;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n_paths; p += gridDim.x * blockDim.x) {
+        uint32_t j = p / a.pixels, pix = p - j * a.pixels;
+        uint32_t px = pix % R.width, py = pix / R.width;
+        uint32_t si = a.wave_first_sample + j;
+        Sampler smp;
+        sampler_start(smp, px, py, si, 0);
+        f2 u_pixel = sample_2d(smp);
+        f2 u_lens = sample_2d(smp);
+        f3 ro, rd;
+        camera_ray(R, px, py, u_pixel, u_lens, ro, rd);
+        a.w.ray_o[p] = make_float4(ro.x, ro.y, ro.z, R.near_plane);
+        a.w.ray_d[p] = make_float4(rd.x, rd.y, rd.z, R.far_plane);
+        a.w.tp[p] = make_float4(1.0f, 1.0f, 1.0f, -1.0f);
+        a.w.rad[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a.w.seg[p] = 0;
+        a.w.queue[0][p] = p;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.w.counts[0] = a.n_paths;
+        a.w.counts[1] = 0;
+        a.w.counts[2] = 0;
+        a.w.counts[3] = 0;
+        a.w.counts[4] = 0;
+    }
+}
+
+// Persistent traversal: warps fetch 32 queue entries at a time.
+__global__ void __launch_bounds__(128) k_wf_extend(WaveArgs a, uint32_t qi)
+{
+    const DevScene& s = a.r.s;
+    const uint32_t* queue = a.w.queue[qi];
+    const uint32_t count = *(volatile uint32_t*)&a.w.counts[qi];
+    unsigned lane = threadIdx.x & 31;
+    TraceCounters tc{0u, 0u};
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0)
+            base = atomicAdd(&a.w.counts[3], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count)
+            break;
+        uint32_t i = base + lane;
+        if (i < count) {
+            uint32_t p = queue[i];
+            float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
+            Hit h;
+            bool hit = trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
+            a.w.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
+            a.w.hit_prim[p] = hit ? h.prim : 0xFFFFFFFFu;
+        }
+    }
+    uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
+    uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
+    if (lane == 0) {
+        atomicAdd(a.r.counters + 3, (unsigned long long)nodes);
+        atomicAdd(a.r.counters + 4, (unsigned long long)tris);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_wf_shade(WaveArgs a, uint32_t qi)
+{
+    const RenderArgs& R = a.r;
+    const DevScene& s = R.s;
+    const uint32_t* qin = a.w.queue[qi];
+    uint32_t* qout = a.w.queue[qi ^ 1];
+    const uint32_t count = a.w.counts[qi];
+    uint32_t segments = 0, shadow_rays = 0;
+    // grid-stride over whole warps so the warp-wide pushes see full warps
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < count; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + (threadIdx.x & 31);
+        bool active = i < count;
+        bool cont = false, trace = false;
+        uint32_t p = active ? qin[i] : 0;
+        if (active) {
+            segments++;
+            uint32_t sg = a.w.seg[p];
+            uint32_t j = p / a.pixels, pix = p - j * a.pixels;
+            uint32_t px = pix % R.width, py = pix / R.width;
+            uint32_t si = a.wave_first_sample + j;
+            PathState pl;
+            float4 t4 = a.w.tp[p], r4 = a.w.rad[p];
+            pl.throughput = mk3(t4.x, t4.y, t4.z);
+            pl.brdf_pdf = t4.w;
+            pl.radiance = mk3(r4.x, r4.y, r4.z);
+            pl.final_segment = sg >= R.max_bounces;
+            sampler_start(pl.smp, px, py, si, sg + 1);
+            float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
+            f3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
+            uint32_t prim = a.w.hit_prim[p];
+            NeeRequest nee;
+            nee.add = false;
+            nee.trace = false;
+            if (prim == 0xFFFFFFFFu) {
+                shade_miss(s, pl);
+            } else {
+                float4 hh = a.w.hit[p];
+                Hit h;
+                h.t = hh.x;
+                h.b1 = hh.y;
+                h.b2 = hh.z;
+                h.inst = __float_as_uint(hh.w);
+                h.prim = prim;
+                shade_hit(s, pl, ro, rd, h, nee);
+            }
+            if (nee.add && !nee.trace)
+                finish_nee(pl.radiance, nee, 0.0f);
+            trace = nee.add && nee.trace;
+            if (trace) {
+                shadow_rays++;
+                a.w.nee_o[p] = make_float4(nee.origin.x, nee.origin.y, nee.origin.z, nee.tmax);
+                a.w.nee_d[p] = make_float4(nee.dir.x, nee.dir.y, nee.dir.z, nee.w);
+                a.w.nee_e[p] = make_float4(nee.emission.x, nee.emission.y, nee.emission.z, nee.cos_i);
+                a.w.nee_b[p] = make_float4(nee.brdf.x, nee.brdf.y, nee.brdf.z, nee.pdf);
+                a.w.nee_tp[p] = make_float4(nee.tp_before.x, nee.tp_before.y, nee.tp_before.z, 0.0f);
+            }
+            // continuation (rg.hlsl:38-55): RR from segment rr_start >= 1
+            if (!pl.final_segment) {
+                bool killed = false;
+                if (sg >= 1 && sg >= R.rr_start)
+                    killed = russian_roulette(pl);
+                cont = !killed && sg + 1 <= R.max_bounces;
+            }
+            a.w.tp[p] = make_float4(pl.throughput.x, pl.throughput.y, pl.throughput.z, pl.brdf_pdf);
+            a.w.rad[p] = make_float4(pl.radiance.x, pl.radiance.y, pl.radiance.z, 0.0f);
+            if (cont) {
+                a.w.seg[p] = sg + 1;
+                a.w.ray_o[p] = make_float4(pl.next_o.x, pl.next_o.y, pl.next_o.z, 0.0f);
+                a.w.ray_d[p] = make_float4(pl.next_d.x, pl.next_d.y, pl.next_d.z, __int_as_float(0x7f800000));
+            }
+        }
+        push_warp(qout, &a.w.counts[qi ^ 1], cont, p);
+        push_warp(a.w.shadow_queue, &a.w.counts[2], trace, p);
+    }
+    segments = __reduce_add_sync(0xffffffffu, segments);
+    shadow_rays = __reduce_add_sync(0xffffffffu, shadow_rays);
+    if ((threadIdx.x & 31) == 0 && (segments | shadow_rays)) {
+        atomicAdd(R.counters + 0, (unsigned long long)segments);
+        atomicAdd(R.counters + 1, (unsigned long long)shadow_rays);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_wf_shadow(WaveArgs a)
+{
+    const DevScene& s = a.r.s;
+    const uint32_t count = a.w.counts[2];
+    unsigned lane = threadIdx.x & 31;
+    TraceCounters tc{0u, 0u};
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0)
+            base = atomicAdd(&a.w.counts[4], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count)
+            break;
+        uint32_t i = base + lane;
+        if (i < count) {
+            uint32_t p = a.w.shadow_queue[i];
+            float4 o = a.w.nee_o[p], d = a.w.nee_d[p];
+            float vis = trace_shadow_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, o.w, tc);
+            NeeRequest nee;
+            nee.add = true;
+            nee.trace = true;
+            float4 e = a.w.nee_e[p], b = a.w.nee_b[p], t = a.w.nee_tp[p];
+            nee.emission = mk3(e.x, e.y, e.z);
+            nee.cos_i = e.w;
+            nee.brdf = mk3(b.x, b.y, b.z);
+            nee.pdf = b.w;
+            nee.w = d.w;
+            nee.tp_before = mk3(t.x, t.y, t.z);
+            float4 r4 = a.w.rad[p];
+            f3 rad = mk3(r4.x, r4.y, r4.z);
+            finish_nee(rad, nee, vis);
+            a.w.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        }
+    }
+    uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
+    uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
+    if (lane == 0) {
+        atomicAdd(a.r.counters + 3, (unsigned long long)nodes);
+        atomicAdd(a.r.counters + 4, (unsigned long long)tris);
+    }
+}
+
+// Clears the consumed queue count and the fetch counters between stages.
+__global__ void k_wf_reset(WaveArgs a, uint32_t qi)
+{
+    a.w.counts[qi] = 0;  // the queue just consumed by shade
+    a.w.counts[2] = 0;   // shadow queue consumed
+    a.w.counts[3] = 0;
+    a.w.counts[4] = 0;
+}
+
+__global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs a)
+{
+    const RenderArgs& R = a.r;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < a.pixels; pix += gridDim.x * blockDim.x) {
+        float4 acc = R.image[pix];
+        double s64[3] = {0.0, 0.0, 0.0};
+        if (R.sum64) {
+            s64[0] = R.sum64[4 * (size_t)pix + 0];
+            s64[1] = R.sum64[4 * (size_t)pix + 1];
+            s64[2] = R.sum64[4 * (size_t)pix + 2];
+        }
+        for (uint32_t j = 0; j < a.wave_samples; j++) {
+            float4 r4 = a.w.rad[(size_t)j * a.pixels + pix];
+            f3 r = correct_radiance(mk3(r4.x, r4.y, r4.z) * R.exposure);
+            accumulate(acc, r, a.wave_first_sample + j);
+            s64[0] += (double)r.x;
+            s64[1] += (double)r.y;
+            s64[2] += (double)r.z;
+        }
+        R.image[pix] = acc;
+        if (R.sum64) {
+            double* d = R.sum64 + 4 * (size_t)pix;
+            d[0] = s64[0];
+            d[1] = s64[1];
+            d[2] = s64[2];
+            d[3] += (double)a.wave_samples;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(R.counters + 2, (unsigned long long)a.n_paths);
+}
+
+size_t wave_state_bytes(uint32_t n_paths)
+{
+    return (size_t)n_paths * (16 * 11 + 4 * 5) + 4096;
+}
+
+static inline char* bump(char*& p, size_t bytes)
+{
+    uintptr_t a = ((uintptr_t)p + 255) & ~(uintptr_t)255;
+    p = (char*)(a + bytes);
+    return (char*)a;
+}
+
+cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
+                             uint32_t* launches, cudaStream_t st)
+{
+    if (state_bytes < wave_state_bytes(n_paths_max))
+        return cudaErrorInvalidValue;
+    WaveArgs a;
+    a.r = r;
+    char* p = (char*)state;
+    size_t n = n_paths_max;
+    a.w.ray_o = (float4*)bump(p, 16 * n);
+    a.w.ray_d = (float4*)bump(p, 16 * n);
+    a.w.tp = (float4*)bump(p, 16 * n);
+    a.w.rad = (float4*)bump(p, 16 * n);
+    a.w.seg = (uint32_t*)bump(p, 4 * n);
+    a.w.hit = (float4*)bump(p, 16 * n);
+    a.w.hit_prim = (uint32_t*)bump(p, 4 * n);
+    a.w.nee_o = (float4*)bump(p, 16 * n);
+    a.w.nee_d = (float4*)bump(p, 16 * n);
+    a.w.nee_e = (float4*)bump(p, 16 * n);
+    a.w.nee_b = (float4*)bump(p, 16 * n);
+    a.w.nee_tp = (float4*)bump(p, 16 * n);
+    a.w.queue[0] = (uint32_t*)bump(p, 4 * n);
+    a.w.queue[1] = (uint32_t*)bump(p, 4 * n);
+    a.w.shadow_queue = (uint32_t*)bump(p, 4 * n);
+    a.w.counts = (uint32_t*)bump(p, 64);
+    if ((size_t)(p - (char*)state) > state_bytes)
+        return cudaErrorInvalidValue;
+    a.pixels = r.width * r.height;
+    uint32_t k_max = n_paths_max / a.pixels;
+    if (k_max == 0)
+        return cudaErrorInvalidValue;
+    // persistent traversal grids: exactly the resident blocks of every SM
+    static int ext_per_sm = 0, sh_per_sm = 0;
+    if (ext_per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_wf_extend, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh_per_sm, k_wf_shadow, 128, 0);
+        if (ext_per_sm < 1)
+            ext_per_sm = 1;
+        if (sh_per_sm < 1)
+            sh_per_sm = 1;
+    }
+    const int trace_blocks = sm_count * ext_per_sm;
+    const int shadow_blocks = sm_count * sh_per_sm;
+    uint32_t nl = 0;
+    for (uint32_t done = 0; done < r.samples;) {
+        a.wave_samples = r.samples - done < k_max ? r.samples - done : k_max;
+        a.wave_first_sample = r.sample_index + done;
+        a.n_paths = a.wave_samples * a.pixels;
+        uint32_t grid = (a.n_paths + 255) / 256;
+        if (grid > (uint32_t)sm_count * 16)
+            grid = sm_count * 16;
+        k_wf_raygen<<<grid, 256, 0, st>>>(a);
+        nl++;
+        uint32_t qi = 0;
+        for (uint32_t sg = 0; sg <= r.max_bounces; sg++) {
+            k_wf_extend<<<trace_blocks, 128, 0, st>>>(a, qi);
+            uint32_t sgrid = (a.n_paths + 127) / 128;
+            if (sgrid > (uint32_t)sm_count * 16)
+                sgrid = sm_count * 16;
+            k_wf_shade<<<sgrid, 128, 0, st>>>(a, qi);
+            k_wf_shadow<<<shadow_blocks, 128, 0, st>>>(a);
+            k_wf_reset<<<1, 1, 0, st>>>(a, qi);
+            nl += 4;
+            qi ^= 1;
+        }
+        uint32_t agrid = (a.pixels + 255) / 256;
+        if (agrid > (uint32_t)sm_count * 16)
+            agrid = sm_count * 16;
+        k_wf_accumulate<<<agrid, 256, 0, st>>>(a);
+        nl++;
+        done += a.wave_samples;
+    }
+    if (launches)
+        *launches = nl;
+    return cudaGetLastError();
+}
+
+cudaError_t wave_init_tables(const uint32_t* table128, cudaStream_t stream)
+{
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_sobol, table128, sizeof(uint32_t) * 128, 0, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess)
+        return e;
+    return cudaStreamSynchronize(stream);
+}
+
+} // namespace pt

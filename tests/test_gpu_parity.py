@@ -15,6 +15,14 @@ from pt_gb300 import abi, scenes
 pytestmark = pytest.mark.gpu
 
 
+KERNELS = {"mega": abi.PT_KERNEL_MEGA, "wave": abi.PT_KERNEL_WAVEFRONT}
+
+
+@pytest.fixture(scope="module", params=sorted(KERNELS))
+def kernel(request):
+    return KERNELS[request.param]
+
+
 @pytest.fixture(scope="module")
 def ctx():
     c = P.Context(0)
@@ -54,19 +62,19 @@ def _assert_bitexact(gpu, ref):
         raise AssertionError(f"{len(ys)} pixels differ (first at x={xs[0]}, y={ys[0]}); max rel {rel.max():.3g}")
 
 
-def test_tiny_bitexact(ctx):
+def test_tiny_bitexact(ctx, kernel):
     raw, cam = scenes.tiny_raw("two_tris")
     hs = P.HostScene.from_raw(raw, cam)
     view = hs.pack()
-    params = hs.render_params(40, 30, 8, 6)
+    params = hs.render_params(40, 30, 8, 6, kernel=kernel)
     gpu, ref, st, ost = _render_both(ctx, view, params, brute=True)
     _assert_bitexact(gpu, ref)
     assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
 
 
-def test_small_scene_bitexact(ctx, small):
+def test_small_scene_bitexact(ctx, small, kernel):
     hs, view = small
-    params = hs.render_params(96, 96, 4, 8)
+    params = hs.render_params(96, 96, 4, 8, kernel=kernel)
     gpu, ref, st, ost = _render_both(ctx, view, params)
     _assert_bitexact(gpu, ref)
     assert st.segments == ost.segments
@@ -74,32 +82,32 @@ def test_small_scene_bitexact(ctx, small):
     assert st.paths == 96 * 96 * 4
 
 
-def test_mid_scene_bitexact(ctx, mid):
+def test_mid_scene_bitexact(ctx, mid, kernel):
     hs, view = mid
-    params = hs.render_params(64, 64, 2, 8)
+    params = hs.render_params(64, 64, 2, 8, kernel=kernel)
     gpu, ref, st, ost = _render_both(ctx, view, params)
     _assert_bitexact(gpu, ref)
     assert st.segments == ost.segments
 
 
-def test_progressive_equals_single_call(ctx, small):
+def test_progressive_equals_single_call(ctx, small, kernel):
     """Rendering spp in several calls gives the same running mean as one call
     (the reference dispatches one sample per submission, ptdispatch.cpp:101)."""
     hs, view = small
     ctx.upload(view)
     ctx.build_accel()
-    one = hs.render_params(48, 40, 6, 5)
+    one = hs.render_params(48, 40, 6, 5, kernel=kernel)
     ctx.render(one)
     a = ctx.read_image().copy()
     for start, n in ((0, 1), (1, 2), (3, 3)):
-        ctx.render(hs.render_params(48, 40, n, 5, sample_index=start))
+        ctx.render(hs.render_params(48, 40, n, 5, sample_index=start, kernel=kernel))
     b = ctx.read_image()
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
-def test_fp64_accumulation_matches_oracle(ctx, small):
+def test_fp64_accumulation_matches_oracle(ctx, small, kernel):
     hs, view = small
-    params = hs.render_params(40, 40, 5, 6, accum_mode=abi.PT_ACCUM_FP32_FP64)
+    params = hs.render_params(40, 40, 5, 6, accum_mode=abi.PT_ACCUM_FP32_FP64, kernel=kernel)
     ctx.upload(view)
     ctx.build_accel()
     ctx.render(params)
@@ -123,9 +131,9 @@ def test_deterministic(ctx, small):
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
-def test_zero_bounces_and_exposure(ctx, small):
+def test_zero_bounces_and_exposure(ctx, small, kernel):
     hs, view = small
-    params = hs.render_params(32, 32, 2, 0)
+    params = hs.render_params(32, 32, 2, 0, kernel=kernel)
     params.exposure = 2.5
     gpu, ref, st, _ = _render_both(ctx, view, params)
     _assert_bitexact(gpu, ref)
@@ -147,3 +155,29 @@ def test_invalid_calls(ctx):
         fresh.render(p)
     assert e.value.status == abi.PT_ERR_INVALID
     fresh.close()
+
+
+def test_wavefront_many_waves(ctx, small):
+    """More samples than one wave holds: waves must chain in sample order."""
+    hs, view = small
+    params = hs.render_params(1024, 1024, 3, 3, kernel=abi.PT_KERNEL_WAVEFRONT)
+    ctx.upload(view)
+    ctx.build_accel()
+    st = ctx.render(params)
+    assert st.error_word == 0 and st.paths == 3 * 1024 * 1024
+    gpu = ctx.read_image()
+    params.kernel = abi.PT_KERNEL_MEGA
+    ctx.render(params)
+    mega = ctx.read_image()
+    assert np.array_equal(gpu.view(np.uint32), mega.view(np.uint32))
+
+
+def test_kernels_agree_on_counts(ctx, mid):
+    hs, view = mid
+    ctx.upload(view)
+    ctx.build_accel()
+    a = ctx.render(hs.render_params(128, 96, 3, 8, kernel=abi.PT_KERNEL_MEGA))
+    b = ctx.render(hs.render_params(128, 96, 3, 8, kernel=abi.PT_KERNEL_WAVEFRONT))
+    assert (a.segments, a.shadow_rays, a.paths) == (b.segments, b.shadow_rays, b.paths)
+    assert a.node_visits == b.node_visits and a.tri_tests == b.tri_tests
+    assert b.kernel_used == abi.PT_KERNEL_WAVEFRONT and a.kernel_used == abi.PT_KERNEL_MEGA
