@@ -342,7 +342,8 @@ def run_ours(args) -> None:
                 "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB write, outside the event pairs)",
-                           "parallelism": f"replicas x{world} (disjoint sample ranges)", "kernel": "megakernel",
+                           "parallelism": f"replicas x{world} (disjoint sample ranges)",
+                           "kernel": {1: "megakernel", 2: "wavefront"}.get(st.kernel_used, str(st.kernel_used)),
                            "segments_per_step": int(segs_per_step), "accel_build_ms": info.build_ms,
                            "image": f"{WIDTH}x{HEIGHT}", "spp": SPP,
                            "node_visits_per_ray": st.node_visits / max(1, st.segments + st.shadow_rays),
