@@ -229,6 +229,29 @@ int pt_tonemap(pt_ctx* ctx);
  * (meansq.cpp:34-43): SSE over RGB / (w*h*3 - 1), reduced in FP64. */
 int pt_mse_host(pt_ctx* ctx, const float* reference_rgba, double* mse_out);
 
+/* Mean squared error for callers that cannot allocate device memory: code
+ * recording a CUDA stream capture (cudaMalloc is not allowed while capturing),
+ * host applications that own all device memory and forbid allocations inside
+ * plug-ins, and real-time loops that cannot risk the implicit device
+ * synchronisation of cudaMalloc/cudaFree.  This entry point has no counterpart
+ * in the reference.
+ *
+ * Same value as pt_mse_host (util/meansq semantics) for two caller-owned
+ * device images (RGBA float rows, 16-byte aligned, width * height pixels);
+ * the result is written to the caller-owned device double *mse_out,
+ * asynchronously on `stream` (a cudaStream_t, NULL = default stream).  It
+ * allocates nothing: its scratch is a fixed device array of
+ * PT_MSE_NOALLOC_SCRATCH_BYTES bytes inside the library, present on every GPU
+ * that loads it until the process exits.  The first call on a device (with
+ * that device current) looks up the array's address; make that first call
+ * before any stream capture.  All calls share the array: calls that overlap on
+ * the GPU race.  Images above PT_MSE_NOALLOC_MAX_PIXELS pixels are rejected
+ * with PT_ERR_UNSUPPORTED; null or misaligned pointers with PT_ERR_INVALID. */
+#define PT_MSE_NOALLOC_SCRATCH_BYTES 9728u
+#define PT_MSE_NOALLOC_MAX_PIXELS 2147483648ull
+int pt_mse_noalloc(const float* image_rgba, const float* reference_rgba, uint32_t width, uint32_t height, double* mse_out,
+                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,6 +115,7 @@ SIGNATURES = [
     ("pt_synchronize", C.c_int, [C.c_void_p]),
     ("pt_tonemap", C.c_int, [C.c_void_p]),
     ("pt_mse_host", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
+    ("pt_mse_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("pt_scene_last_error", C.c_char_p, []),
     ("pt_scene_load", C.c_void_p, [C.c_char_p]),
     ("pt_scene_from_raw", C.c_void_p, [C.POINTER(RawScene), C.POINTER(CameraDesc)]),

@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-f
               "--expt-relaxed-constexpr"] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["api.cu", "render_mega.cu", "render_wave.cu", "bvh_build.cu", "post.cu"]
+CU_SOURCES = ["api.cu", "render_mega.cu", "render_wave.cu", "bvh_build.cu", "post.cu", "noalloc.cu"]
 CPP_SOURCES = ["host/scene.cpp", "host/imageio.cpp"]
 HEADERS = list(CSRC.rglob("*.cuh")) + list(CSRC.rglob("*.h")) + list((HERE.parent / "include").glob("*.h"))
 
