@@ -131,7 +131,35 @@ SIGNATURES = [
     ("pt_read_hdr", C.c_int, [C.c_char_p, C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.c_uint32),
                               C.POINTER(C.c_uint32)]),
     ("pt_host_free", None, [C.c_void_p]),
+    # denoiser (include/pt_denoise.h)
+    ("pt_unet_param_count", C.c_size_t, []),
+    ("pt_unet_layer_shape", C.c_int, [C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    ("pt_unet_create", C.c_void_p, [C.c_int, C.c_uint32, C.c_uint32, C.c_uint32]),
+    ("pt_unet_destroy", None, [C.c_void_p]),
+    ("pt_unet_last_error", C.c_char_p, [C.c_void_p]),
+    ("pt_unet_set_params", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_size_t]),
+    ("pt_unet_get_params", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_size_t]),
+    ("pt_unet_get_grads", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_size_t]),
+    ("pt_unet_shape", None, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    ("pt_unet_input", C.c_void_p, [C.c_void_p]),
+    ("pt_unet_output", C.c_void_p, [C.c_void_p]),
+    ("pt_unet_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("pt_unet_backward", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
+    ("pt_unet_adam", C.c_int, [C.c_void_p, C.c_float, C.c_void_p]),
+    ("pt_nn_conv3x3", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p, C.c_void_p]),
+    ("pt_nn_conv3x3_dgrad", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("pt_nn_conv3x3_wgrad", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                      C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("pt_render_features", C.c_int, [C.c_void_p, C.POINTER(RenderParams)]),
+    ("pt_denoise_input", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("pt_denoise", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
 ]
+
+PT_IMAGE_DENOISED = 2
+PT_UNET_IN_CHANNELS = 16
+PT_UNET_OUT_CHANNELS = 16
 
 _lib = None
 

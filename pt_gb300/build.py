@@ -26,7 +26,10 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-f
               "--expt-relaxed-constexpr"] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["api.cu", "render_mega.cu", "render_wave.cu", "bvh_build.cu", "post.cu", "noalloc.cu"]
+CU_SOURCES = ["api.cu", "render_mega.cu", "render_wave.cu", "bvh_build.cu", "post.cu", "noalloc.cu", "features.cu",
+              "nn/conv.cu", "nn/ops.cu", "nn/unet.cu", "nn/api_nn.cu"]
+# The denoiser is not on the bit-exact path: let it contract multiply-adds.
+NN_FLAGS = [f for f in NVCC_FLAGS if f != "-fmad=false"]
 CPP_SOURCES = ["host/scene.cpp", "host/imageio.cpp"]
 HEADERS = list(CSRC.rglob("*.cuh")) + list(CSRC.rglob("*.h")) + list((HERE.parent / "include").glob("*.h"))
 
@@ -58,7 +61,8 @@ def build(verbose: bool = False) -> Path:
         obj = BUILD / (Path(src).stem + ".o")
         objs.append(obj)
         if _stale(obj, [CSRC / src] + HEADERS):
-            jobs.append((src, [NVCC] + NVCC_FLAGS + ["-c", str(CSRC / src), "-o", str(obj)]))
+            flags = NN_FLAGS if src.startswith("nn/") else NVCC_FLAGS
+            jobs.append((src, [NVCC] + flags + ["-c", str(CSRC / src), "-o", str(obj)]))
     for src in CPP_SOURCES + ["host/main.cpp"]:
         obj = BUILD / (Path(src).stem + ".o")
         if src != "host/main.cpp":

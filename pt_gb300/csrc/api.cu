@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/pt_denoise.h"
 #include "../../include/pt_gpu.h"
 #include "device/render.cuh"
 #include "kernels.h"
@@ -144,6 +145,9 @@ struct pt_ctx {
     DevBuf<char> wave_state;    // wavefront path state
     uint32_t wave_paths = 0;    // paths the wave state holds
     int sm_count = 0;
+    DevBuf<float4> feat_a, feat_n; // denoiser features: albedo + depth, normal
+    uint32_t feat_w = 0, feat_h = 0;
+    DevBuf<float4> denoised;    // last pt_denoise result
     DevBuf<float4> mse_ref;     // reference image for pt_mse_host
     DevBuf<double> mse_partial; // [0] result, [1..] per-block partial sums
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -544,25 +548,9 @@ static int ensure_image(pt_ctx* c, uint32_t w, uint32_t h, bool fp64, bool reset
     return PT_OK;
 }
 
-int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
+// Device view of the context's scene and the camera/image of `p`.
+static RenderArgs render_args(pt_ctx* c, const pt_render_params* p, bool fp64)
 {
-    if (!c || !p)
-        return PT_ERR_INVALID;
-    if (!c->accel_ok)
-        return c->fail(PT_ERR_STATE, "acceleration structure not built");
-    if (p->width == 0 || p->height == 0 || p->samples == 0)
-        return c->fail(PT_ERR_INVALID, "zero width, height or sample count");
-    if ((uint64_t)p->width * p->height > (1ull << 31))
-        return c->fail(PT_ERR_UNSUPPORTED, "image larger than 2^31 pixels");
-    if ((uint64_t)p->sample_index + p->samples > 0xFFFFFFFFull)
-        return c->fail(PT_ERR_INVALID, "sample index overflows 32 bits");
-    if (p->accum_mode > PT_ACCUM_FP32_FP64 || p->kernel > PT_KERNEL_WAVEFRONT)
-        return c->fail(PT_ERR_INVALID, "unknown accumulation mode or kernel");
-    cudaSetDevice(c->device);
-    bool fp64 = p->accum_mode == PT_ACCUM_FP32_FP64;
-    int rc = ensure_image(c, p->width, p->height, fp64, p->sample_index == 0);
-    if (rc != PT_OK)
-        return rc;
     RenderArgs a{};
     a.s.vertices = c->vertices.p;
     a.s.indices = c->indices.p;
@@ -596,6 +584,29 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     a.image = c->image.p;
     a.sum64 = fp64 ? c->sum64.p : nullptr;
     a.counters = c->counters.p;
+    return a;
+}
+
+int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
+{
+    if (!c || !p)
+        return PT_ERR_INVALID;
+    if (!c->accel_ok)
+        return c->fail(PT_ERR_STATE, "acceleration structure not built");
+    if (p->width == 0 || p->height == 0 || p->samples == 0)
+        return c->fail(PT_ERR_INVALID, "zero width, height or sample count");
+    if ((uint64_t)p->width * p->height > (1ull << 31))
+        return c->fail(PT_ERR_UNSUPPORTED, "image larger than 2^31 pixels");
+    if ((uint64_t)p->sample_index + p->samples > 0xFFFFFFFFull)
+        return c->fail(PT_ERR_INVALID, "sample index overflows 32 bits");
+    if (p->accum_mode > PT_ACCUM_FP32_FP64 || p->kernel > PT_KERNEL_WAVEFRONT)
+        return c->fail(PT_ERR_INVALID, "unknown accumulation mode or kernel");
+    cudaSetDevice(c->device);
+    bool fp64 = p->accum_mode == PT_ACCUM_FP32_FP64;
+    int rc = ensure_image(c, p->width, p->height, fp64, p->sample_index == 0);
+    if (rc != PT_OK)
+        return rc;
+    RenderArgs a = render_args(c, p, fp64);
     cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
     uint64_t pixels = (uint64_t)p->width * p->height;
     uint32_t kernel = p->kernel == PT_KERNEL_MEGA ? PT_KERNEL_MEGA : PT_KERNEL_WAVEFRONT;
@@ -668,6 +679,17 @@ int pt_read_image(pt_ctx* c, void* rgba, size_t pitch, int fp64)
         return c->fail(PT_ERR_STATE, "nothing rendered");
     cudaSetDevice(c->device);
     cudaError_t e;
+    if (fp64 == PT_IMAGE_DENOISED) {
+        if (!c->denoised.p || c->feat_w != c->width || c->feat_h != c->height)
+            return c->fail(PT_ERR_STATE, "no denoised image (call pt_denoise)");
+        if (pitch < (size_t)c->width * 16)
+            return c->fail(PT_ERR_INVALID, "pitch smaller than a row");
+        e = cudaMemcpy2DAsync(rgba, pitch, c->denoised.p, (size_t)c->width * 16, (size_t)c->width * 16, c->height,
+                              cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        return e == cudaSuccess ? PT_OK : c->cuda_fail(e, "denoised read-back");
+    }
     if (!fp64) {
         if (pitch < (size_t)c->width * 16)
             return c->fail(PT_ERR_INVALID, "pitch smaller than a row");
@@ -702,6 +724,92 @@ int pt_read_image(pt_ctx* c, void* rgba, size_t pitch, int fp64)
         }
     }
     return PT_OK;
+}
+
+int pt_render_features(pt_ctx* c, const pt_render_params* p)
+{
+    if (!c || !p)
+        return PT_ERR_INVALID;
+    if (!c->accel_ok)
+        return c->fail(PT_ERR_STATE, "acceleration structure not built");
+    if (p->width == 0 || p->height == 0 || p->samples == 0)
+        return c->fail(PT_ERR_INVALID, "zero width, height or sample count");
+    if ((uint64_t)p->width * p->height > (1ull << 31) || (uint64_t)p->sample_index + p->samples > 0xFFFFFFFFull)
+        return c->fail(PT_ERR_INVALID, "image or sample range too large");
+    cudaSetDevice(c->device);
+    const size_t pixels = (size_t)p->width * p->height;
+    if (c->feat_a.n < pixels) {
+        cudaError_t e = c->feat_a.alloc(pixels);
+        if (e == cudaSuccess)
+            e = c->feat_n.alloc(pixels);
+        if (e != cudaSuccess)
+            return c->cuda_fail(e, "feature buffers");
+    }
+    RenderArgs a = render_args(c, p, false);
+    a.sample_index = p->sample_index;
+    a.samples = p->samples;
+    cudaError_t e = launch_features(a, c->feat_a.p, c->feat_n.p, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+        return c->cuda_fail(e, "feature pass");
+    c->feat_w = p->width;
+    c->feat_h = p->height;
+    return PT_OK;
+}
+
+static int denoise_input(pt_ctx* c, uint32_t spp, uint16_t* input)
+{
+    if (!c->image.p || c->feat_w != c->width || c->feat_h != c->height)
+        return c->fail(PT_ERR_STATE, "render the image and its features (pt_render_features) first");
+    if (spp == 0)
+        return c->fail(PT_ERR_INVALID, "zero samples per pixel");
+    const float spp_feature = log2f((float)spp) / 8.0f;
+    cudaError_t e = launch_denoise_input(c->image.p, c->feat_a.p, c->feat_n.p, c->width * c->height, spp_feature, input, c->stream);
+    if (e != cudaSuccess)
+        return c->cuda_fail(e, "denoiser input");
+    return PT_OK;
+}
+
+int pt_denoise_input(pt_ctx* c, uint32_t spp, uint16_t* input, void* stream)
+{
+    if (!c || !input)
+        return PT_ERR_INVALID;
+    cudaSetDevice(c->device);
+    int rc = denoise_input(c, spp, input);
+    if (rc != PT_OK)
+        return rc;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess && stream)
+        e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? PT_OK : c->cuda_fail(e, "denoiser input");
+}
+
+int pt_denoise(pt_ctx* c, pt_unet* u, uint32_t spp)
+{
+    if (!c || !u)
+        return PT_ERR_INVALID;
+    uint32_t n = 0, h = 0, w = 0;
+    pt_unet_shape(u, &n, &h, &w);
+    if (n != 1 || h != c->height || w != c->width)
+        return c->fail(PT_ERR_INVALID, "denoiser shape differs from the image (batch 1, same height and width)");
+    cudaSetDevice(c->device);
+    int rc = denoise_input(c, spp, pt_unet_input(u));
+    if (rc != PT_OK)
+        return rc;
+    rc = pt_unet_forward(u, nullptr, c->stream);
+    if (rc != PT_OK)
+        return c->fail(rc, std::string("denoiser: ") + pt_unet_last_error(u));
+    const size_t pixels = (size_t)w * h;
+    if (c->denoised.n < pixels) {
+        cudaError_t e = c->denoised.alloc(pixels);
+        if (e != cudaSuccess)
+            return c->cuda_fail(e, "denoised image");
+    }
+    cudaError_t e = launch_denoise_output(pt_unet_output(u), (uint32_t)pixels, c->denoised.p, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? PT_OK : c->cuda_fail(e, "denoised image");
 }
 
 int pt_tonemap(pt_ctx* c)
