@@ -18,6 +18,10 @@ accumulation.  Synthetic, seeded scene data (pt_gb300.scenes.mid_scene).
           measured HBM copy bandwidth.
   cpu_baseline  the CPU oracle (the C++ restatement of the reference's shader
           math, OpenMP over pixels) on a bounded sample of the same workload.
+  time_to_mse  wall time (synchronised, same scene and image size) for plain
+          GPU accumulation and for the denoised pipeline (render + first-hit
+          features + U-Net) to reach MSE <= 1e-3 against a 4096-spp image
+          accumulated in FP64 on the GPU; `speedup` = plain / denoised.
 
 --impl reference runs the reference's CPU implementation of the path on the
 host cores: the reference's Vulkan tracer cannot run on this machine, so this
@@ -54,6 +58,10 @@ WORKLOAD = "mid scene: 1024x1024, 128 spp, max 8 bounces, ~260k tris / 200 insta
 # of the oracle's binned-SAH BVH2 over the first sample of the image, and
 # p_nee the shadow rays per segment (measured by tests/test_bseg.py, which
 # checks these constants against the oracle).
+MSE_TARGET = 1e-3
+REF_SPP = 4096
+DENOISE_SPP = (1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64)
+
 BSEG = {"mid": {"n_node": 27.2106, "n_tri": 9.0453, "p_nee": 0.2336},
         "small": {"n_node": 13.7945, "n_tri": 6.0748, "p_nee": 0.5218}}
 
@@ -233,6 +241,117 @@ def pinned_view(view):
     return v, keep, nbytes
 
 
+def meansq(a, ref) -> float:
+    """util/meansq/meansq.cpp:34-43 over RGB: sum of squared differences / (n - 1)."""
+    import numpy as np
+
+    d = a[..., :3].astype(np.float64) - ref[..., :3]
+    return float(np.sum(d * d) / (d.size - 1))
+
+
+def time_to_mse(ctx, hs, kernel: int, ref_spp: int) -> dict:
+    """Wall time (render + read of the converged-enough image, synchronised)
+    for plain accumulation and for the denoised pipeline to reach
+    MSE <= MSE_TARGET against an FP64-accumulated reference of ref_spp samples."""
+    import math
+    import numpy as np
+    from pt_gb300 import abi
+    from pt_gb300.denoise import WEIGHTS_DIR, UNet, load_params
+
+    def params(n, mode=abi.PT_ACCUM_FP32):
+        return hs.render_params(WIDTH, HEIGHT, n, BOUNCES, accum_mode=mode, kernel=kernel)
+
+    t0 = time.perf_counter()
+    ctx.render(params(ref_spp, abi.PT_ACCUM_FP32_FP64), stats=False)
+    ref = ctx.read_image(fp64=True)
+    ref_s = time.perf_counter() - t0
+    ref32 = np.ascontiguousarray(ref.astype(np.float32))
+
+    def plain(n):
+        ctx.synchronize()
+        t = time.perf_counter()
+        ctx.render(params(n), stats=False)
+        ctx.synchronize()
+        t = time.perf_counter() - t
+        return ctx.mse(ref32), t
+
+    plain(8)  # warm-up
+    m16, _ = plain(16)
+    n = max(1, int(math.ceil(16 * m16 / MSE_TARGET)))
+    m, t = plain(n)
+    while m > MSE_TARGET:
+        n = int(n * 1.08) + 1
+        m, t = plain(n)
+    while n > 1:
+        k = n - max(1, n // 25)
+        mk, tk = plain(k)
+        if mk > MSE_TARGET:
+            break
+        n, m, t = k, mk, tk
+    out = {"threshold": MSE_TARGET, "metric": "meansq over RGB (meansq.cpp)",
+           "reference": {"spp": ref_spp, "accumulation": "fp64 on the GPU", "seconds": round(ref_s, 3)},
+           "plain": {"spp": n, "seconds": t, "mse": m}}
+    wfile = WEIGHTS_DIR / "unet.bin"
+    if not wfile.exists():
+        out["denoised"] = None
+        out["denoised_unavailable"] = "no trained weights (run python -m pt_gb300.train_denoiser)"
+        return out
+    unet = UNet(1, HEIGHT, WIDTH)
+    unet.set_params(load_params(wfile))
+
+    def denoised(s):
+        p = params(s)
+        ctx.synchronize()
+        t = time.perf_counter()
+        ctx.render_denoised(unet, p)
+        ctx.synchronize()
+        t = time.perf_counter() - t
+        return meansq(ctx.read_denoised(), ref), t
+
+    denoised(4)  # warm-up
+    curve = {}
+    best = None
+    for s in DENOISE_SPP:
+        m, t = denoised(s)
+        curve[s] = {"mse": m, "seconds": t, "plain_mse": plain(s)[0]}
+        if m <= MSE_TARGET:
+            best = {"spp": s, "seconds": t, "mse": m}
+            break
+    out["denoised"] = best
+    out["denoised_curve"] = curve
+    out["speedup"] = (out["plain"]["seconds"] / best["seconds"]) if best else None
+    unet.close()
+    return out
+
+
+def run_denoise_profile(args) -> None:
+    """The denoised pipeline alone (mid scene, --denoise-profile spp), three
+    times after a warm-up: the command profiled for the denoiser's launch list."""
+    import pt_gb300 as P
+    from pt_gb300.denoise import WEIGHTS_DIR, UNet, init_params, load_params
+
+    td = tempfile.TemporaryDirectory()
+    hs = make_scene(Path(td.name))
+    ctx = P.Context(0)
+    ctx.upload(hs.pack())
+    ctx.build_accel()
+    unet = UNet(1, HEIGHT, WIDTH)
+    wfile = WEIGHTS_DIR / "unet.bin"
+    unet.set_params(load_params(wfile) if wfile.exists() else init_params(0))
+    p = hs.render_params(WIDTH, HEIGHT, args.denoise_profile, BOUNCES, kernel=args.kernel)
+    times = []
+    for i in range(4):
+        ctx.synchronize()
+        t = time.perf_counter()
+        ctx.render_denoised(unet, p)
+        ctx.synchronize()
+        times.append(time.perf_counter() - t)
+    print(json.dumps({"denoise_profile_spp": args.denoise_profile, "seconds": times[1:]}))
+    unet.close()
+    ctx.close()
+    td.cleanup()
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -338,6 +457,7 @@ def run_ours(args) -> None:
                 "bytes_per_segment": b}
         base = cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES), seconds_target=float(args.cpu_seconds)) \
             if not args.no_cpu else None
+        ttm = time_to_mse(ctx, hs, args.kernel, args.ref_spp) if not args.no_mse else None
         line = {"metric": METRIC, "value": value, "unit": "Mpath-segs/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -353,7 +473,7 @@ def run_ours(args) -> None:
                         "d2h_bytes_per_step": int(HEIGHT * WIDTH * 16), "ms_per_step": 1000.0 * t_e2e / args.steps,
                         "includes": "scene upload + BVH build + render + image read-back"},
                 "gpu_launches": int(launches_per_step * args.steps),
-                "roofline": roof, "cpu_baseline": base, "clocks": clocks.summary(),
+                "roofline": roof, "cpu_baseline": base, "clocks": clocks.summary(), "time_to_mse": ttm,
                 "wall_s_timed_region": wall}
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -372,6 +492,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mse", action="store_true", help="skip the time-to-MSE measurement")
+    ap.add_argument("--ref-spp", type=int, default=REF_SPP)
+    ap.add_argument("--denoise-profile", type=int, default=0, help="only run the denoised pipeline at this spp (profiling)")
     ap.add_argument("--width", type=int, default=1024, help="smaller images only for profiling captures")
     ap.add_argument("--height", type=int, default=1024)
     ap.add_argument("--spp", type=int, default=128)
@@ -382,6 +505,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.denoise_profile:
+        run_denoise_profile(args)
     else:
         run_ours(args)
 

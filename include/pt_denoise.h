@@ -24,11 +24,15 @@ extern "C" {
 #endif
 
 /* Network input: 16 bf16 channels per pixel.
- *   0-2  log(1 + radiance) of the noisy mean image
- *   3-5  first-hit base colour      6-8  first-hit world normal
- *   9    log(1 + hit distance) / 4  10   log2(samples per pixel) / 8
- *   11-15 zero
- * Network output: 16 fp32 channels, 0-2 = log(1 + radiance). */
+ *   0-2   log(1 + radiance) of the noisy mean image
+ *   3-5   first-hit base colour      6-8  first-hit world normal
+ *   9     log(1 + hit distance) / 4  10   log2(samples per pixel) / 8
+ *   11-13 noise estimate: sign(d) log(1 + |d|), d = snapshot mean - mean
+ *         (see pt_denoise_snapshot), zero without a snapshot
+ *   14    1 when a snapshot was used, else 0
+ *   15    zero
+ * Network output: 16 fp32 channels, 0-2 = log(1 + radiance), computed as the
+ * residual base plus the network's correction. */
 #define PT_UNET_IN_CHANNELS 16u
 #define PT_UNET_OUT_CHANNELS 16u
 
@@ -57,6 +61,10 @@ void pt_unet_shape(const pt_unet* u, uint32_t* batch, uint32_t* height, uint32_t
 uint16_t* pt_unet_input(pt_unet* u);
 /* Device buffer holding the last forward pass's fp32 [batch][h][w][16]. */
 const float* pt_unet_output(const pt_unet* u);
+/* Residual base, fp32 [batch][h][w][4] (device, zero after creation): added to
+ * output channels 0-3, so the network predicts a correction of
+ * log(1 + noisy radiance) that pt_denoise_input writes here in full FP32. */
+float* pt_unet_base(pt_unet* u);
 /* Forward pass; writes fp32 [batch][h][w][16] to `output` (device, may be
  * NULL to keep it internal). */
 int pt_unet_forward(pt_unet* u, float* output, void* stream);
@@ -86,9 +94,16 @@ int pt_nn_conv3x3_wgrad(const uint16_t* in, uint32_t n, uint32_t h, uint32_t w, 
  * base colour, world shading normal (facing the camera) and hit distance
  * (zero where the ray escapes).  Kept in the context. */
 int pt_render_features(pt_ctx* ctx, const pt_render_params* params);
+/* Keeps a copy of the context's current mean image (the first samples of the
+ * image being accumulated).  pt_denoise_input then derives a per-pixel noise
+ * estimate from it, as long as the image was continued (not restarted)
+ * since. */
+int pt_denoise_snapshot(pt_ctx* ctx);
 /* Packs the context's current mean image and features into a denoiser input
- * (bf16 [h][w][16], device) for an image of `spp` samples per pixel. */
-int pt_denoise_input(pt_ctx* ctx, uint32_t spp, uint16_t* input, void* stream);
+ * (bf16 [h][w][16], device) for an image of `spp` samples per pixel, and when
+ * `base` is not NULL its residual base (fp32 [h][w][4]: log(1 + radiance),
+ * 0). */
+int pt_denoise_input(pt_ctx* ctx, uint32_t spp, uint16_t* input, float* base, void* stream);
 /* Packs, runs the network (batch 1, same size as the image) and stores
  * expm1(max(out, 0)) as the context's denoised RGBA image, read back with
  * pt_read_image(ctx, rgba, pitch, PT_IMAGE_DENOISED). */

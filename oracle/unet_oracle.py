@@ -41,13 +41,14 @@ def split_params(p: np.ndarray):
 
 def init_params(seed: int = 0) -> np.ndarray:
     """He-normal weights (fan-in 9 * c_in), zero biases; the output layer is
-    scaled by 0.1 and its unused channels 3..15 are zero."""
+    scaled by 0.02 (the network starts close to the identity on its
+    residual base) and its unused channels 3..15 are zero."""
     rng = np.random.default_rng(seed)
     parts = []
     for li, (ci, co, _) in enumerate(LAYERS):
         w = rng.standard_normal((9, ci, co)) * np.sqrt(2.0 / (9 * ci))
         if li == len(LAYERS) - 1:
-            w *= 0.1
+            w *= 0.02
             w[:, :, 3:] = 0.0
         parts += [w.ravel(), np.zeros(co)]
     return np.concatenate(parts).astype(np.float32)
@@ -95,7 +96,7 @@ def conv3x3_wgrad(x: np.ndarray, g: np.ndarray) -> np.ndarray:
     return dw
 
 
-def pool2(x):
+def _pool2(x):
     n, h, w, c = x.shape
     return x.reshape(n, h // 2, 2, w // 2, 2, c).mean(axis=(2, 4))
 
@@ -114,14 +115,31 @@ def up2_backward(g):
 
 
 # ---------------------------------------------------------------- network
-def forward(params: np.ndarray, x: np.ndarray):
-    """Returns (out [n, h, w, 16], cache)."""
+def _keep(a):
+    return a
+
+
+def _store_bf16(a):
+    return bf16(a).astype(np.float64)
+
+
+def forward(params: np.ndarray, x: np.ndarray, bf16_storage: bool = False, base: np.ndarray | None = None):
+    """Returns (out [n, h, w, 16], cache).  `base` ([n, h, w, 4], the residual
+    base of pt_unet_base) is added to output channels 0-3.  With bf16_storage every tensor the
+    library stores as BF16 (layer outputs, pooled maps, gradients) is rounded
+    to BF16 where the library rounds it; the output layer stays FP32."""
+    q = _store_bf16 if bf16_storage else _keep
     P = [(w.astype(np.float64), b.astype(np.float64)) for w, b in split_params(params)]
-    c = {"x0": x.astype(np.float64)}
+    c = {"x0": x.astype(np.float64), "q": q}
 
     def layer(i, inp):
         pre = conv3x3(inp, *P[i])
-        return np.maximum(pre, 0.0) if LAYERS[i][2] else pre
+        if i == len(LAYERS) - 1:
+            return pre
+        return q(np.maximum(pre, 0.0) if LAYERS[i][2] else pre)
+
+    def pool2(a):
+        return q(_pool2(a))
 
     c["e0a"] = layer(0, c["x0"])
     c["e0b"] = layer(1, c["e0a"])
@@ -144,6 +162,8 @@ def forward(params: np.ndarray, x: np.ndarray):
     c["d0a"] = layer(12, c["cat0"])
     c["d0b"] = layer(13, c["d0a"])
     c["out"] = layer(14, c["d0b"])
+    if base is not None:
+        c["out"][..., :4] += base
     c["P"] = P
     return c["out"], c
 
@@ -163,8 +183,9 @@ def loss_and_grad_out(out: np.ndarray, target: np.ndarray):
 
 def backward(cache, target: np.ndarray):
     """Returns (loss, flat fp64 gradient in parameter order)."""
-    c, P = cache, cache["P"]
+    c, P, q = cache, cache["P"], cache["q"]
     loss, g_out = loss_and_grad_out(c["out"], target)
+    g_out = q(g_out)
     grads = [None] * len(LAYERS)
 
     def lay(i, inp, g_pre):
@@ -172,26 +193,26 @@ def backward(cache, target: np.ndarray):
         return conv3x3_dgrad(g_pre, P[i][0])
 
     def relu_mask(g, z):
-        return g * (z > 0)
+        return q(g * (z > 0))
 
     g = lay(14, c["d0b"], g_out)
     g = lay(13, c["d0a"], relu_mask(g, c["d0b"]))
-    g_cat0 = lay(12, c["cat0"], relu_mask(g, c["d0a"]))
+    g_cat0 = q(lay(12, c["cat0"], relu_mask(g, c["d0a"])))
     g = relu_mask(up2_backward(g_cat0[..., :64]), c["d1b"])
     g = lay(11, c["d1a"], g)
-    g_cat1 = lay(10, c["cat1"], relu_mask(g, c["d1a"]))
+    g_cat1 = q(lay(10, c["cat1"], relu_mask(g, c["d1a"])))
     g = relu_mask(up2_backward(g_cat1[..., :96]), c["d2b"])
     g = lay(9, c["d2a"], g)
-    g_cat2 = lay(8, c["cat2"], relu_mask(g, c["d2a"]))
+    g_cat2 = q(lay(8, c["cat2"], relu_mask(g, c["d2a"])))
     g = relu_mask(up2_backward(g_cat2[..., :128]), c["b3b"])
     g = lay(7, c["b3a"], g)
-    g_p3 = lay(6, c["p3"], relu_mask(g, c["b3a"]))
+    g_p3 = q(lay(6, c["p3"], relu_mask(g, c["b3a"])))
     g = relu_mask(g_cat2[..., 128:] + pool2_backward(g_p3), c["e2b"])
     g = lay(5, c["e2a"], g)
-    g_p2 = lay(4, c["p2"], relu_mask(g, c["e2a"]))
+    g_p2 = q(lay(4, c["p2"], relu_mask(g, c["e2a"])))
     g = relu_mask(g_cat1[..., 96:] + pool2_backward(g_p2), c["e1b"])
     g = lay(3, c["e1a"], g)
-    g_p1 = lay(2, c["p1"], relu_mask(g, c["e1a"]))
+    g_p1 = q(lay(2, c["p1"], relu_mask(g, c["e1a"])))
     g = relu_mask(g_cat0[..., 64:] + pool2_backward(g_p1), c["e0b"])
     g = lay(1, c["e0a"], g)
     lay(0, c["x0"], relu_mask(g, c["e0a"]))

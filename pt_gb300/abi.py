@@ -143,6 +143,7 @@ SIGNATURES = [
     ("pt_unet_shape", None, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     ("pt_unet_input", C.c_void_p, [C.c_void_p]),
     ("pt_unet_output", C.c_void_p, [C.c_void_p]),
+    ("pt_unet_base", C.c_void_p, [C.c_void_p]),
     ("pt_unet_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("pt_unet_backward", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
     ("pt_unet_adam", C.c_int, [C.c_void_p, C.c_float, C.c_void_p]),
@@ -153,7 +154,8 @@ SIGNATURES = [
     ("pt_nn_conv3x3_wgrad", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                       C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("pt_render_features", C.c_int, [C.c_void_p, C.POINTER(RenderParams)]),
-    ("pt_denoise_input", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("pt_denoise_snapshot", C.c_int, [C.c_void_p]),
+    ("pt_denoise_input", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("pt_denoise", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
 ]
 

@@ -148,6 +148,56 @@ class Context:
         _check(lib().pt_read_image(self._h, out.ctypes.data, out.strides[0], 1 if fp64 else 0), self._h)
         return out
 
+    def read_denoised(self, out: np.ndarray | None = None) -> np.ndarray:
+        """The image of the last denoise() (RGBA float32)."""
+        if out is None:
+            out = np.empty((self.height, self.width, 4), dtype=np.float32)
+        _check(lib().pt_read_image(self._h, out.ctypes.data, out.strides[0], abi.PT_IMAGE_DENOISED), self._h)
+        return out
+
+    def render_features(self, params: abi.RenderParams) -> None:
+        """First-hit albedo / normal / depth of the camera rays of `params`' samples."""
+        _check(lib().pt_render_features(self._h, C.byref(params)), self._h)
+
+    def denoise_snapshot(self) -> None:
+        """Keeps the current mean image; the denoiser input then carries a noise estimate."""
+        _check(lib().pt_denoise_snapshot(self._h), self._h)
+
+    def render_noisy(self, params: abi.RenderParams, feature_rays: int = 1) -> None:
+        """The denoiser's input side: params.samples samples in two halves (a
+        snapshot after the first half gives the noise estimate) and first-hit
+        features of `feature_rays` camera rays."""
+        s, first = params.samples, params.sample_index
+        try:
+            if s >= 2:
+                params.samples = s // 2
+                self.render(params, stats=False)
+                self.denoise_snapshot()
+                params.sample_index = first + s // 2
+                params.samples = s - s // 2
+                self.render(params, stats=False)
+            else:
+                self.render(params, stats=False)
+            params.sample_index = first
+            params.samples = max(1, min(feature_rays, s))
+            self.render_features(params)
+        finally:
+            params.sample_index, params.samples = first, s
+
+    def render_denoised(self, unet, params: abi.RenderParams, feature_rays: int = 1) -> None:
+        """render_noisy, then the network; read the result with read_denoised()."""
+        self.render_noisy(params, feature_rays)
+        self.denoise(unet, params.samples)
+
+    def denoise_input(self, spp: int, dst_ptr: int, base_ptr: int | None = None) -> None:
+        """Packs the current image and features into a bf16 [h, w, 16] device
+        buffer (and the fp32 [h, w, 4] residual base when base_ptr is given)."""
+        _check(lib().pt_denoise_input(self._h, spp, dst_ptr, base_ptr, None), self._h)
+
+    def denoise(self, unet, spp: int) -> None:
+        """Runs `unet` (a pt_gb300.denoise.UNet of batch 1 and this image's size)."""
+        _check(lib().pt_denoise(self._h, unet.handle, spp), self._h)
+
     def mse(self, reference: np.ndarray) -> float:
         ref = np.ascontiguousarray(reference, dtype=np.float32)
         v = C.c_double()

@@ -148,6 +148,9 @@ struct pt_ctx {
     DevBuf<float4> feat_a, feat_n; // denoiser features: albedo + depth, normal
     uint32_t feat_w = 0, feat_h = 0;
     DevBuf<float4> denoised;    // last pt_denoise result
+    DevBuf<float4> half;        // pt_denoise_snapshot: mean image of the first samples
+    uint32_t half_w = 0, half_h = 0, half_spp = 0, half_epoch = 0;
+    uint32_t image_epoch = 0;   // counts fresh renders (sample_index 0)
     DevBuf<float4> mse_ref;     // reference image for pt_mse_host
     DevBuf<double> mse_partial; // [0] result, [1..] per-block partial sums
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -606,6 +609,8 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     int rc = ensure_image(c, p->width, p->height, fp64, p->sample_index == 0);
     if (rc != PT_OK)
         return rc;
+    if (p->sample_index == 0)
+        c->image_epoch++;
     RenderArgs a = render_args(c, p, fp64);
     cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
     uint64_t pixels = (uint64_t)p->width * p->height;
@@ -758,25 +763,52 @@ int pt_render_features(pt_ctx* c, const pt_render_params* p)
     return PT_OK;
 }
 
-static int denoise_input(pt_ctx* c, uint32_t spp, uint16_t* input)
+int pt_denoise_snapshot(pt_ctx* c)
+{
+    if (!c)
+        return PT_ERR_INVALID;
+    if (!c->image.p || c->samples_done == 0)
+        return c->fail(PT_ERR_STATE, "nothing rendered");
+    cudaSetDevice(c->device);
+    const size_t pixels = (size_t)c->width * c->height;
+    if (c->half.n < pixels) {
+        cudaError_t e = c->half.alloc(pixels);
+        if (e != cudaSuccess)
+            return c->cuda_fail(e, "snapshot buffer");
+    }
+    cudaError_t e = cudaMemcpyAsync(c->half.p, c->image.p, pixels * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream);
+    if (e != cudaSuccess)
+        return c->cuda_fail(e, "snapshot");
+    c->half_w = c->width;
+    c->half_h = c->height;
+    c->half_spp = c->samples_done;
+    c->half_epoch = c->image_epoch;
+    return PT_OK;
+}
+
+static int denoise_input(pt_ctx* c, uint32_t spp, uint16_t* input, float* base)
 {
     if (!c->image.p || c->feat_w != c->width || c->feat_h != c->height)
         return c->fail(PT_ERR_STATE, "render the image and its features (pt_render_features) first");
     if (spp == 0)
         return c->fail(PT_ERR_INVALID, "zero samples per pixel");
     const float spp_feature = log2f((float)spp) / 8.0f;
-    cudaError_t e = launch_denoise_input(c->image.p, c->feat_a.p, c->feat_n.p, c->width * c->height, spp_feature, input, c->stream);
+    // the snapshot counts only if it holds the first samples of this very image
+    const bool have_half = c->half.p && c->half_w == c->width && c->half_h == c->height && c->half_epoch == c->image_epoch &&
+                           c->half_spp < c->samples_done;
+    cudaError_t e = launch_denoise_input(c->image.p, have_half ? c->half.p : nullptr, c->feat_a.p, c->feat_n.p,
+                                         c->width * c->height, spp_feature, input, base, c->stream);
     if (e != cudaSuccess)
         return c->cuda_fail(e, "denoiser input");
     return PT_OK;
 }
 
-int pt_denoise_input(pt_ctx* c, uint32_t spp, uint16_t* input, void* stream)
+int pt_denoise_input(pt_ctx* c, uint32_t spp, uint16_t* input, float* base, void* stream)
 {
     if (!c || !input)
         return PT_ERR_INVALID;
     cudaSetDevice(c->device);
-    int rc = denoise_input(c, spp, input);
+    int rc = denoise_input(c, spp, input, base);
     if (rc != PT_OK)
         return rc;
     cudaError_t e = cudaStreamSynchronize(c->stream);
@@ -794,7 +826,7 @@ int pt_denoise(pt_ctx* c, pt_unet* u, uint32_t spp)
     if (n != 1 || h != c->height || w != c->width)
         return c->fail(PT_ERR_INVALID, "denoiser shape differs from the image (batch 1, same height and width)");
     cudaSetDevice(c->device);
-    int rc = denoise_input(c, spp, pt_unet_input(u));
+    int rc = denoise_input(c, spp, pt_unet_input(u), pt_unet_base(u));
     if (rc != PT_OK)
         return rc;
     rc = pt_unet_forward(u, nullptr, c->stream);

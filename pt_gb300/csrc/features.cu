@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(128) k_features(RenderArgs a, float4* feat_a, 
             f3 ro, rd;
             camera_ray(a, px, py, u_pixel, u_lens, ro, rd);
             Hit h;
-            if (!trace_closest(a.s, ro, rd, a.near_plane, a.far_plane, h, tc))
+            if (!trace_closest_inl(a.s, ro, rd, a.near_plane, a.far_plane, h, tc))
                 continue;
             const DevInstanceData* id = a.s.inst_data + h.inst;
             const DevMaterial* mat = a.s.materials + __ldg(&id->material_index);
@@ -62,15 +62,32 @@ __device__ __forceinline__ uint32_t bf2(float a, float b)
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-__global__ void k_denoise_input(const float4* img, const float4* fa, const float4* fn, uint32_t pixels, float spp_feature,
-                                uint16_t* out)
+// Noise estimate: the mean of the first samples minus the mean of all of them
+// (half the difference of two independent half-sample means), signed log.
+__device__ __forceinline__ float slog(float x)
+{
+    return copysignf(log1pf(fabsf(x)), x);
+}
+
+__global__ void k_denoise_input(const float4* img, const float4* half, const float4* fa, const float4* fn, uint32_t pixels,
+                                float spp_feature, uint16_t* out, float4* base)
 {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < pixels; p += gridDim.x * blockDim.x) {
         const float4 c = img[p], a = fa[p], n = fn[p];
         const float r = log1pf(fmaxf(c.x, 0.0f)), g = log1pf(fmaxf(c.y, 0.0f)), b = log1pf(fmaxf(c.z, 0.0f));
+        float dr = 0.0f, dg = 0.0f, db = 0.0f, have = 0.0f;
+        if (half) {
+            const float4 h = half[p];
+            dr = slog(h.x - c.x);
+            dg = slog(h.y - c.y);
+            db = slog(h.z - c.z);
+            have = 1.0f;
+        }
         uint4* o = reinterpret_cast<uint4*>(out + (size_t)p * 16);
         o[0] = make_uint4(bf2(r, g), bf2(b, a.x), bf2(a.y, a.z), bf2(n.x, n.y));
-        o[1] = make_uint4(bf2(n.z, log1pf(a.w) * 0.25f), bf2(spp_feature, 0.0f), 0u, 0u);
+        o[1] = make_uint4(bf2(n.z, log1pf(a.w) * 0.25f), bf2(spp_feature, dr), bf2(dg, db), bf2(have, 0.0f));
+        if (base)
+            base[p] = make_float4(r, g, b, 0.0f);
     }
 }
 
@@ -96,10 +113,11 @@ cudaError_t launch_features(const RenderArgs& a, float4* feat_a, float4* feat_n,
     return cudaGetLastError();
 }
 
-cudaError_t launch_denoise_input(const float4* img, const float4* fa, const float4* fn, uint32_t pixels, float spp_feature,
-                                 uint16_t* out, cudaStream_t st)
+cudaError_t launch_denoise_input(const float4* img, const float4* half, const float4* fa, const float4* fn, uint32_t pixels,
+                                 float spp_feature, uint16_t* out, float* base, cudaStream_t st)
 {
-    k_denoise_input<<<grid_for(pixels, 256), 256, 0, st>>>(img, fa, fn, pixels, spp_feature, out);
+    k_denoise_input<<<grid_for(pixels, 256), 256, 0, st>>>(img, half, fa, fn, pixels, spp_feature, out,
+                                                           reinterpret_cast<float4*>(base));
     return cudaGetLastError();
 }
 

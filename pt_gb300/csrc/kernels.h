@@ -24,8 +24,8 @@ cudaError_t wave_init_tables(const uint32_t* table128, cudaStream_t stream);
 
 // Denoiser features and packing (features.cu).
 cudaError_t launch_features(const RenderArgs& a, float4* feat_a, float4* feat_n, cudaStream_t stream);
-cudaError_t launch_denoise_input(const float4* img, const float4* fa, const float4* fn, uint32_t pixels, float spp_feature,
-                                 uint16_t* out, cudaStream_t stream);
+cudaError_t launch_denoise_input(const float4* img, const float4* half, const float4* fa, const float4* fn, uint32_t pixels,
+                                 float spp_feature, uint16_t* out, float* base, cudaStream_t stream);
 cudaError_t launch_denoise_output(const float* out32, uint32_t pixels, float4* img, cudaStream_t stream);
 
 // Output stage (post.cu).

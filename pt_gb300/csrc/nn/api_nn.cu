@@ -174,6 +174,11 @@ const float* pt_unet_output(const pt_unet* u)
     return u ? u->net.output() : nullptr;
 }
 
+float* pt_unet_base(pt_unet* u)
+{
+    return u ? u->net.base() : nullptr;
+}
+
 int pt_unet_forward(pt_unet* u, float* output, void* stream)
 {
     if (!u)

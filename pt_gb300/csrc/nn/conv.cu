@@ -35,6 +35,7 @@ struct ConvParams {
     float* out_f32;
     const uint16_t* mask;
     int mask_pitch, mask_c0;
+    const float* residual;
     int n, h, w, tx, ty, tiles_x, tiles_y;
     int stages;
     uint32_t tmem_cols;
@@ -170,6 +171,13 @@ __global__ void __launch_bounds__(128) k_conv3x3(const __grid_constant__ CUtenso
             }
         }
         if (p.out_f32) {
+            if (p.residual && j == 0) {
+                const float4 r4 = *reinterpret_cast<const float4*>(p.residual + pix * 4);
+                v[0] += r4.x;
+                v[1] += r4.y;
+                v[2] += r4.z;
+                v[3] += r4.w;
+            }
             float4* o = reinterpret_cast<float4*>(p.out_f32 + pix * p.out_pitch + j * 16);
 #pragma unroll
             for (int k = 0; k < 4; k++)
@@ -279,9 +287,10 @@ __global__ void __launch_bounds__(128) k_wgrad(const __grid_constant__ CUtensorM
             const uint32_t sa = smem_addr(smem + (size_t)s * stage_bytes);
             const uint32_t sb = sa + a_bytes;
             for (int ks = 0; ks < 4; ks++) {
-                // MN-major: lbo = 1024 between 8-row groups of M/N, sbo = 128 between 8-pixel groups of K
-                uint64_t ad = smem_desc(sa + (uint32_t)ks * 256u, 1024u, 128u);
-                uint64_t bd = smem_desc(sb + (uint32_t)ks * 256u, 1024u, 128u);
+                // MN-major, no swizzle: lbo = 128 between 8-pixel groups of K,
+                // sbo = 1024 between 8-channel groups of M/N
+                uint64_t ad = smem_desc(sa + (uint32_t)ks * 256u, 128u, 1024u);
+                uint64_t bd = smem_desc(sb + (uint32_t)ks * 256u, 128u, 1024u);
                 mma_bf16(tmem, ad, bd, idesc, (i | ks) != 0);
             }
             mma_commit(&empty[s]);
@@ -428,6 +437,7 @@ cudaError_t conv3x3(const ConvCall& c, uint32_t* error, cudaStream_t st)
     p.mask = c.mask ? c.mask->p : nullptr;
     p.mask_pitch = c.mask ? c.mask->pitch : 0;
     p.mask_c0 = c.mask_c0;
+    p.residual = c.out_f32 ? c.residual : nullptr;
     p.n = c.in.n;
     p.h = c.in.h;
     p.w = c.in.w;

@@ -36,7 +36,8 @@ inline size_t packed_elems(int cin, int cout) { return (size_t)9 * cin * cout; }
 // `mask` the result is multiplied by (mask[mask_c0 + c] > 0).  `wpk` holds the
 // weights packed by pack_weights (forward layout for a forward pass, the
 // data-gradient layout for a backward pass; nout is then the layer's c_in).
-// `in_map` must cover `in` with the conv tile box.
+// `in_map` must cover `in` with the conv tile box.  With out_f32, `residual`
+// (fp32, 4 per pixel, may be null) is added to output channels 0-3.
 struct ConvCall {
     const CUtensorMap* in_map;
     Act in;
@@ -50,6 +51,7 @@ struct ConvCall {
     float* out_f32;
     const Act* mask;
     int mask_c0;
+    const float* residual; // fp32 [pixel][4] added to output channels 0-3 (with out_f32 only)
 };
 cudaError_t conv3x3(const ConvCall& c, uint32_t* error, cudaStream_t st);
 

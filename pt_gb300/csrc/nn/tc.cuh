@@ -108,9 +108,9 @@ __device__ __forceinline__ void tc_fence_after()
 }
 
 // Shared-memory matrix descriptor, no swizzle.  `lbo` and `sbo` are byte
-// strides between 8x16-byte core matrices: for K-major operands lbo steps
-// along K and sbo along M/N; for MN-major operands lbo steps along M/N and
-// sbo along K.  Bits 46-47 hold the descriptor version (1).
+// strides between 8x16-byte core matrices: without swizzling, lbo steps
+// along K and sbo along M/N for K-major and MN-major operands alike.
+// Bits 46-47 hold the descriptor version (1).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
 {
     return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |

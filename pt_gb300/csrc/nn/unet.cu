@@ -166,6 +166,7 @@ bool UNet::init(int device, int n, int h, int w, std::string& err)
             return false;
     const size_t P = param_count();
     out32_ = static_cast<float*>(alloc((size_t)n * h * w * OUT_CHANNELS * sizeof(float)));
+    base32_ = static_cast<float*>(alloc((size_t)n * h * w * 4 * sizeof(float)));
     params_ = static_cast<float*>(alloc(P * sizeof(float)));
     grads_ = static_cast<float*>(alloc(P * sizeof(float)));
     adam_m_ = static_cast<float*>(alloc(P * sizeof(float)));
@@ -179,7 +180,7 @@ bool UNet::init(int device, int n, int h, int w, std::string& err)
     wbwd_ = static_cast<uint16_t*>(alloc(packed * 2));
     loss_acc_ = static_cast<double*>(alloc(sizeof(double)));
     error_ = static_cast<uint32_t*>(alloc(sizeof(uint32_t)));
-    if (!out32_ || !params_ || !grads_ || !adam_m_ || !adam_v_ || !wfwd_ || !wbwd_ || !loss_acc_ || !error_) {
+    if (!out32_ || !base32_ || !params_ || !grads_ || !adam_m_ || !adam_v_ || !wfwd_ || !wbwd_ || !loss_acc_ || !error_) {
         err = "device allocation of denoiser parameters failed";
         return false;
     }
@@ -187,6 +188,7 @@ bool UNet::init(int device, int n, int h, int w, std::string& err)
     cudaMemset(adam_m_, 0, P * sizeof(float));
     cudaMemset(adam_v_, 0, P * sizeof(float));
     cudaMemset(error_, 0, sizeof(uint32_t));
+    cudaMemset(base32_, 0, (size_t)n * h * w * 4 * sizeof(float));
     if (cudaDeviceSynchronize() != cudaSuccess) {
         err = "denoiser initialisation failed";
         return false;
@@ -348,6 +350,7 @@ cudaError_t UNet::forward(cudaStream_t st)
     c.out = d0b_.a;
     c.out.pitch = OUT_CHANNELS;
     c.out_f32 = out32_;
+    c.residual = base32_;
     return conv3x3(c, error_, st);
 }
 

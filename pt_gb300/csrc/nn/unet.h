@@ -2,7 +2,9 @@
 // (channels 32 / 64 / 96 / 128, two convolutions per level, 2x2 average
 // pooling down, nearest upsampling up, skip connections by concatenation)
 // mapping 16 input feature channels to 16 output channels of which the first
-// three are log(1 + radiance).
+// three are log(1 + radiance).  The output layer adds an FP32 residual base
+// (the caller's log(1 + noisy radiance)) so that pixels the network leaves
+// alone keep full precision.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -51,6 +53,8 @@ class UNet {
 
     // Input: bf16 [n][h][w][16] (device).  Output fp32 [n][h][w][16] in output().
     uint16_t* input() { return x0_.a.p; }
+    // fp32 [n][h][w][4] added to output channels 0-3 (zero unless set).
+    float* base() { return base32_; }
     const float* output() const { return out32_; }
     cudaError_t forward(cudaStream_t st);
     // Gradients of the loss against `target` (fp32 linear RGBA [n][h][w][4],
@@ -78,6 +82,7 @@ class UNet {
     // activations
     Buf x0_, e0a_, cat0_, p1_, e1a_, cat1_, p2_, e2a_, cat2_, p3_, b3a_, b3b_, d2a_, d2b_, d1a_, d1b_, d0a_, d0b_;
     float* out32_ = nullptr;
+    float* base32_ = nullptr;
     // gradients
     Buf g_out_, g_d0b_, g_d0a_, g_cat0_, g_d1b_, g_d1a_, g_cat1_, g_d2b_, g_d2a_, g_cat2_, g_b3b_, g_b3a_, g_p3_, g_e2b_, g_e2a_,
         g_p2_, g_e1b_, g_e1a_, g_p1_, g_e0b_, g_e0a_;

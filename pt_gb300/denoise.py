@@ -35,14 +35,15 @@ def param_count() -> int:
 
 def init_params(seed: int = 0) -> np.ndarray:
     """He-normal weights (fan-in 9 * c_in), zero biases; the output layer is
-    scaled by 0.1 and its channels 3..15 (unused) are zero."""
+    scaled by 0.02 (the network starts close to the identity on its
+    residual base) and its channels 3..15 (unused) are zero."""
     rng = np.random.default_rng(seed)
     shapes = layer_shapes()
     parts = []
     for li, (ci, co) in enumerate(shapes):
         w = rng.standard_normal((9, ci, co)) * np.sqrt(2.0 / (9 * ci))
         if li == len(shapes) - 1:
-            w *= 0.1
+            w *= 0.02
             w[:, :, 3:] = 0.0
         parts += [w.ravel(), np.zeros(co)]
     return np.concatenate(parts).astype(np.float32)
@@ -127,6 +128,12 @@ class UNet:
         import torch
 
         return device_tensor(self.output_ptr, (self.batch, self.height, self.width, 16), torch.float32)
+
+    def base_tensor(self):
+        """The fp32 [batch, h, w, 4] residual base added to output channels 0-3."""
+        import torch
+
+        return device_tensor(int(self._lib.pt_unet_base(self._h)), (self.batch, self.height, self.width, 4), torch.float32)
 
     def set_params(self, params: np.ndarray) -> None:
         p = np.ascontiguousarray(params, dtype=np.float32)

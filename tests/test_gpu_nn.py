@@ -129,26 +129,41 @@ def _weights_bf16(p):
 
 
 def test_unet_gradients_match_oracle():
+    """Forward, loss and every layer's gradient of the whole network.
+
+    Against an oracle that rounds to BF16 wherever the library stores BF16
+    the only differences left are FP32 accumulation order and the rare BF16
+    rounding it flips: 2 % per layer.  Against the exact FP64 network the
+    BF16 storage of ~30 activation and gradient tensors moves the gradients
+    of the middle layers by up to ~10 % (the oracle alone shows this): 20 %."""
     n, h, w = 2, 16, 24
     p, x, t = _net_inputs(3, n, h, w)
     net = UNet(n, h, w)
     net.set_params(p)
     net.input_tensor().copy_(dev(x, torch.bfloat16))
+    base = np.random.default_rng(4).uniform(0, 1.5, (n, h, w, 4)).astype(np.float32)
+    base[..., 3] = 0
+    net.base_tensor().copy_(dev(base, torch.float32))
     tgt = dev(t, torch.float32)
     net.forward()
     loss = net.backward(tgt.data_ptr())
     g = net.grads().astype(np.float64)
     got_out = net.output_tensor().cpu().numpy().astype(np.float64)
-
-    ref_out, cache = U.forward(_weights_bf16(p), x.astype(np.float64))
-    ref_loss, ref_g = U.backward(cache, t)
-    assert np.abs(got_out - ref_out).max() <= 0.03 * np.abs(ref_out).max() + 1e-3
-    assert abs(loss - ref_loss) <= 0.02 * ref_loss
+    pw = _weights_bf16(p)
     offs = np.cumsum([0] + [9 * ci * co + co for ci, co, _ in U.LAYERS])
-    for li in range(len(U.LAYERS)):
-        a, b = g[offs[li]:offs[li + 1]], ref_g[offs[li]:offs[li + 1]]
-        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
-        assert rel < 0.05, f"layer {li}: relative gradient error {rel:.3g}"
+    report = []
+    for storage, tol_out, tol_loss, tol_g in ((True, 0.005, 0.002, 0.02), (False, 0.03, 0.02, 0.20)):
+        ref_out, cache = U.forward(pw, x.astype(np.float64), bf16_storage=storage, base=base.astype(np.float64))
+        ref_loss, ref_g = U.backward(cache, t)
+        assert np.abs(got_out - ref_out).max() <= tol_out * np.abs(ref_out).max() + 1e-4
+        assert abs(loss - ref_loss) <= tol_loss * ref_loss
+        rels = []
+        for li in range(len(U.LAYERS)):
+            a, b = g[offs[li]:offs[li + 1]], ref_g[offs[li]:offs[li + 1]]
+            rels.append(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+        report.append(rels)
+        assert max(rels) < tol_g, f"bf16_storage={storage}: per-layer relative gradient error {np.round(rels, 4)}"
+    print("per-layer relative gradient error (bf16-storage oracle, fp64 oracle):", np.round(report, 4))
 
 
 def test_training_reduces_loss():
