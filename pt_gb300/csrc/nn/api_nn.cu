@@ -80,6 +80,29 @@ struct Scratch {
     }
 };
 
+int sm_count()
+{
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+// One convolution through the selected kernel; the halo map is made per call.
+cudaError_t run(pt::nn::ConvCall& c, const Act& in, bool rows, cudaStream_t st, uint32_t* err)
+{
+    if (!rows)
+        return pt::nn::conv3x3(c, err, st);
+    CUtensorMap halo;
+    const char* why = nullptr;
+    const int mt = pt::nn::rows_per_tile(c.nout);
+    if (!pt::nn::encode_act_map(&halo, in, 130, mt + 2, &why)) {
+        g_layer_error = why;
+        return cudaErrorInvalidValue;
+    }
+    return pt::nn::conv3x3_rows(c, &halo, sm_count(), err, st);
+}
+
 bool shape_ok(uint32_t n, uint32_t h, uint32_t w, uint32_t pitch, uint32_t c0, uint32_t c)
 {
     return n && h && w && pitch % 16 == 0 && c0 % 8 == 0 && c % 16 == 0 && c0 + c <= pitch && c > 0;
@@ -242,7 +265,9 @@ int pt_nn_conv3x3(const uint16_t* in, uint32_t n, uint32_t h, uint32_t w, uint32
     CUtensorMap tile;
     if (!map_for(&tile, nullptr, a, g_layer_error))
         return PT_ERR_INVALID;
-    if (pt::nn::pack_weights(weights, (int)c_in, (int)c_out, s.fwd, s.bwd, st) != cudaSuccess)
+    const bool rows = pt::nn::use_rows_kernel();
+    if ((rows ? pt::nn::pack_weights_rows(weights, (int)c_in, (int)c_out, s.fwd, s.bwd, st)
+              : pt::nn::pack_weights(weights, (int)c_in, (int)c_out, s.fwd, s.bwd, st)) != cudaSuccess)
         return PT_ERR_CUDA;
     pt::nn::ConvCall c{};
     c.in_map = &tile;
@@ -256,7 +281,7 @@ int pt_nn_conv3x3(const uint16_t* in, uint32_t n, uint32_t h, uint32_t w, uint32
     c.out = a;
     c.out.p = out;
     c.out.pitch = (int)c_out;
-    if (pt::nn::conv3x3(c, s.err, st) != cudaSuccess)
+    if (run(c, a, rows, st, s.err) != cudaSuccess)
         return PT_ERR_CUDA;
     return s.finish(st);
 }
@@ -279,7 +304,9 @@ int pt_nn_conv3x3_dgrad(const uint16_t* grad_out, uint32_t n, uint32_t h, uint32
     CUtensorMap tile;
     if (!map_for(&tile, nullptr, g, g_layer_error))
         return PT_ERR_INVALID;
-    if (pt::nn::pack_weights(weights, (int)c_in, (int)c_out, s.fwd, s.bwd, st) != cudaSuccess)
+    const bool rows = pt::nn::use_rows_kernel();
+    if ((rows ? pt::nn::pack_weights_rows(weights, (int)c_in, (int)c_out, s.fwd, s.bwd, st)
+              : pt::nn::pack_weights(weights, (int)c_in, (int)c_out, s.fwd, s.bwd, st)) != cudaSuccess)
         return PT_ERR_CUDA;
     Act m = g;
     m.p = const_cast<uint16_t*>(mask);
@@ -294,7 +321,7 @@ int pt_nn_conv3x3_dgrad(const uint16_t* grad_out, uint32_t n, uint32_t h, uint32
     c.out.p = grad_in;
     c.out.pitch = (int)c_in;
     c.mask = mask ? &m : nullptr;
-    if (pt::nn::conv3x3(c, s.err, st) != cudaSuccess)
+    if (run(c, g, rows, st, s.err) != cudaSuccess)
         return PT_ERR_CUDA;
     return s.finish(st);
 }
@@ -320,10 +347,7 @@ int pt_nn_conv3x3_wgrad(const uint16_t* in, uint32_t n, uint32_t h, uint32_t w, 
     CUtensorMap xc, gc;
     if (!map_for(nullptr, &xc, x, g_layer_error) || !map_for(nullptr, &gc, g, g_layer_error))
         return PT_ERR_INVALID;
-    int sms = 152;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int sms = sm_count();
     pt::nn::WgradCall c{};
     c.x_map = &xc;
     c.x_c0 = (int)c0;

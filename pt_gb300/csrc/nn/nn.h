@@ -55,6 +55,17 @@ struct ConvCall {
 };
 cudaError_t conv3x3(const ConvCall& c, uint32_t* error, cudaStream_t st);
 
+// The same convolution with halo reuse (conv_rows.cu): persistent CTAs over
+// tiles of rows_per_tile(nout) rows x 128 pixels; `halo_map` must cover `in`
+// with a box of 8 channels x 130 x (rows_per_tile + 2) pixels
+// (encode_act_map(map, in, 130, rows + 2)), `c.wpk` the weights packed by
+// pack_weights_rows.
+int rows_per_tile(int nout);
+cudaError_t pack_weights_rows(const float* w, int cin, int cout, uint16_t* fwd, uint16_t* bwd, cudaStream_t st);
+cudaError_t conv3x3_rows(const ConvCall& c, const CUtensorMap* halo_map, int sm_count, uint32_t* error, cudaStream_t st);
+// True unless PT_CONV_KERNEL=tap selects the one-tile-per-CTA kernel.
+bool use_rows_kernel();
+
 // dw[tap][ci][co] += sum_p x[p + offset(tap)][x_c0 + ci] * g[p][g_c0 + co]
 // over all pixels (dw must be zeroed by the caller).  Maps use the wgrad box.
 struct WgradCall {

@@ -131,7 +131,17 @@ bool UNet::make(Buf& b, int level, int channels, std::string& err)
         err = why;
         return false;
     }
+    for (int k = 0; k < 4; k++)
+        if (!encode_act_map(&b.halo[k], b.a, 130, (1 << k) + 2, &why)) {
+            err = why;
+            return false;
+        }
     return true;
+}
+
+static int halo_index(int rows)
+{
+    return rows >= 8 ? 3 : rows >= 4 ? 2 : rows >= 2 ? 1 : 0;
 }
 
 bool UNet::init(int device, int n, int h, int w, std::string& err)
@@ -178,9 +188,13 @@ bool UNet::init(int device, int n, int h, int w, std::string& err)
     }
     wfwd_ = static_cast<uint16_t*>(alloc(packed * 2));
     wbwd_ = static_cast<uint16_t*>(alloc(packed * 2));
+    wrfwd_ = static_cast<uint16_t*>(alloc(packed * 2));
+    wrbwd_ = static_cast<uint16_t*>(alloc(packed * 2));
+    rows_ = use_rows_kernel();
     loss_acc_ = static_cast<double*>(alloc(sizeof(double)));
     error_ = static_cast<uint32_t*>(alloc(sizeof(uint32_t)));
-    if (!out32_ || !base32_ || !params_ || !grads_ || !adam_m_ || !adam_v_ || !wfwd_ || !wbwd_ || !loss_acc_ || !error_) {
+    if (!out32_ || !base32_ || !params_ || !grads_ || !adam_m_ || !adam_v_ || !wfwd_ || !wbwd_ || !wrfwd_ || !wrbwd_ ||
+        !loss_acc_ || !error_) {
         err = "device allocation of denoiser parameters failed";
         return false;
     }
@@ -244,13 +258,23 @@ uint32_t UNet::device_error()
 cudaError_t UNet::repack(cudaStream_t st)
 {
     for (int l = 0; l < N_LAYERS; l++) {
-        cudaError_t e = pack_weights(params_ + weight_offset(l), LAYERS[l].cin, LAYERS[l].cout, wfwd_ + packed_off_[l],
-                                     wbwd_ + packed_off_[l], st);
+        cudaError_t e = rows_ ? pack_weights_rows(params_ + weight_offset(l), LAYERS[l].cin, LAYERS[l].cout,
+                                                  wrfwd_ + packed_off_[l], wrbwd_ + packed_off_[l], st)
+                              : pack_weights(params_ + weight_offset(l), LAYERS[l].cin, LAYERS[l].cout,
+                                             wfwd_ + packed_off_[l], wbwd_ + packed_off_[l], st);
         if (e != cudaSuccess)
             return e;
     }
     packed_ok_ = true;
     return cudaSuccess;
+}
+
+cudaError_t UNet::run_conv(ConvCall& c, Buf& in, const uint16_t* rows_wpk, cudaStream_t st)
+{
+    if (!rows_)
+        return conv3x3(c, error_, st);
+    c.wpk = rows_wpk;
+    return conv3x3_rows(c, &in.halo[halo_index(rows_per_tile(c.nout))], sm_count_, error_, st);
 }
 
 cudaError_t UNet::conv(int l, Buf& in, int c0, Buf& out, int out_c0, cudaStream_t st)
@@ -266,7 +290,7 @@ cudaError_t UNet::conv(int l, Buf& in, int c0, Buf& out, int out_c0, cudaStream_
     c.relu = LAYERS[l].relu;
     c.out = out.a;
     c.out_c0 = out_c0;
-    return conv3x3(c, error_, st);
+    return run_conv(c, in, wrfwd_ + packed_off_[l], st);
 }
 
 cudaError_t UNet::dgrad(int l, Buf& g, Buf& out, const Buf* mask, int mask_c0, cudaStream_t st)
@@ -284,7 +308,7 @@ cudaError_t UNet::dgrad(int l, Buf& g, Buf& out, const Buf* mask, int mask_c0, c
     c.out_c0 = 0;
     c.mask = mask ? &mask->a : nullptr;
     c.mask_c0 = mask_c0;
-    return conv3x3(c, error_, st);
+    return run_conv(c, g, wrbwd_ + packed_off_[l], st);
 }
 
 cudaError_t UNet::wgrad(int l, Buf& x, int x_c0, Buf& g, cudaStream_t st)
@@ -351,7 +375,7 @@ cudaError_t UNet::forward(cudaStream_t st)
     c.out.pitch = OUT_CHANNELS;
     c.out_f32 = out32_;
     c.residual = base32_;
-    return conv3x3(c, error_, st);
+    return run_conv(c, d0b_, wrfwd_ + packed_off_[14], st);
 }
 
 cudaError_t UNet::backward(const float* target, double* loss, cudaStream_t st)

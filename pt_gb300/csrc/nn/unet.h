@@ -67,11 +67,13 @@ class UNet {
     struct Buf {
         Act a;
         CUtensorMap tile, chunk;
+        CUtensorMap halo[4]; // halo boxes for 1, 2, 4 and 8 rows per tile
     };
 
   private:
     bool make(Buf& b, int level, int channels, std::string& err);
     cudaError_t conv(int layer, Buf& in, int c0, Buf& out, int out_c0, cudaStream_t st);
+    cudaError_t run_conv(ConvCall& c, Buf& in, const uint16_t* rows_wpk, cudaStream_t st);
     cudaError_t dgrad(int layer, Buf& g, Buf& out, const Buf* mask, int mask_c0, cudaStream_t st);
     cudaError_t wgrad(int layer, Buf& x, int x_c0, Buf& g, cudaStream_t st);
     cudaError_t repack(cudaStream_t st);
@@ -88,7 +90,9 @@ class UNet {
         g_p2_, g_e1b_, g_e1a_, g_p1_, g_e0b_, g_e0a_;
     // parameters
     float *params_ = nullptr, *grads_ = nullptr, *adam_m_ = nullptr, *adam_v_ = nullptr;
-    uint16_t *wfwd_ = nullptr, *wbwd_ = nullptr;
+    uint16_t *wfwd_ = nullptr, *wbwd_ = nullptr;   // per-tap kernel layouts
+    uint16_t *wrfwd_ = nullptr, *wrbwd_ = nullptr; // halo kernel layouts
+    bool rows_ = true;
     size_t packed_off_[N_LAYERS] = {};
     bool packed_ok_ = false;
     int adam_t_ = 0;

@@ -17,6 +17,17 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["rows", "tap"], autouse=True)
+def conv_kernel(request, monkeypatch):
+    """Every test runs on both convolution kernels: the persistent halo-reuse
+    kernel (default) and the one-tile-per-CTA kernel (PT_CONV_KERNEL=tap)."""
+    if request.param == "tap":
+        monkeypatch.setenv("PT_CONV_KERNEL", "tap")
+    else:
+        monkeypatch.delenv("PT_CONV_KERNEL", raising=False)
+    return request.param
+
+
 def dev(a, dtype):
     return torch.from_numpy(np.ascontiguousarray(a, np.float32)).to("cuda").to(dtype).contiguous()
 
