@@ -338,7 +338,8 @@ def run_denoise_profile(args) -> None:
     unet = UNet(1, HEIGHT, WIDTH)
     wfile = WEIGHTS_DIR / "unet.bin"
     unet.set_params(load_params(wfile) if wfile.exists() else init_params(0))
-    p = hs.render_params(WIDTH, HEIGHT, args.denoise_profile, BOUNCES, kernel=args.kernel)
+    s = args.denoise_profile
+    p = hs.render_params(WIDTH, HEIGHT, s, BOUNCES, kernel=args.kernel)
     times = []
     for i in range(4):
         ctx.synchronize()
@@ -346,7 +347,24 @@ def run_denoise_profile(args) -> None:
         ctx.render_denoised(unet, p)
         ctx.synchronize()
         times.append(time.perf_counter() - t)
-    print(json.dumps({"denoise_profile_spp": args.denoise_profile, "seconds": times[1:]}))
+    # the same pipeline stage by stage (synchronised after each)
+    stages = {}
+
+    def stage(name, fn):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        ctx.synchronize()
+        stages[name] = stages.get(name, 0.0) + time.perf_counter() - t0
+
+    for i in range(3):
+        stage("render_with_features_and_snapshot", lambda: ctx.render_noisy(hs.render_params(WIDTH, HEIGHT, s, BOUNCES,
+                                                                                          kernel=args.kernel)))
+        stage("network", lambda: ctx.denoise(unet, s))
+    one = hs.render_params(WIDTH, HEIGHT, s, BOUNCES, kernel=args.kernel)
+    stage("plain_render_same_spp", lambda: ctx.render(one, stats=False))
+    stages = {k: v / 3 if k != "plain_render_same_spp" else v for k, v in stages.items()}
+    print(json.dumps({"denoise_profile_spp": s, "seconds": times[1:], "stages_s": stages}))
     unet.close()
     ctx.close()
     td.cleanup()

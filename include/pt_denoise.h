@@ -94,11 +94,21 @@ int pt_nn_conv3x3_wgrad(const uint16_t* in, uint32_t n, uint32_t h, uint32_t w, 
  * base colour, world shading normal (facing the camera) and hit distance
  * (zero where the ray escapes).  Kept in the context. */
 int pt_render_features(pt_ctx* ctx, const pt_render_params* params);
+/* Copies the feature image (width x height of the last features) to host:
+ * albedo_depth gets base colour + hit distance, normal the shading normal,
+ * 4 floats per pixel each (either may be NULL). */
+int pt_read_features(pt_ctx* ctx, float* albedo_depth, float* normal);
 /* Keeps a copy of the context's current mean image (the first samples of the
  * image being accumulated).  pt_denoise_input then derives a per-pixel noise
  * estimate from it, as long as the image was continued (not restarted)
  * since. */
 int pt_denoise_snapshot(pt_ctx* ctx);
+/* Arms the same snapshot for the moment the image holds `samples` samples:
+ * the next pt_render whose sample range reaches that count writes the running
+ * mean at that sample into the snapshot (bitwise what pt_denoise_snapshot
+ * would copy after stopping there), so a whole denoiser input takes one
+ * render call.  0 disarms. */
+int pt_denoise_snapshot_at(pt_ctx* ctx, uint32_t samples);
 /* Packs the context's current mean image and features into a denoiser input
  * (bf16 [h][w][16], device) for an image of `spp` samples per pixel, and when
  * `base` is not NULL its residual base (fp32 [h][w][4]: log(1 + radiance),

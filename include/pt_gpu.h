@@ -154,8 +154,15 @@ typedef struct pt_render_params {
     uint32_t accum_mode;   /* PT_ACCUM_*  */
     uint32_t kernel;       /* PT_KERNEL_* */
     uint32_t rr_start;     /* first segment with Russian roulette; 1 = reference */
-    uint32_t reserved[3];
+    uint32_t flags;        /* PT_RENDER_* (0 = the reference's behaviour)        */
+    uint32_t reserved[2];
 } pt_render_params;
+
+/* pt_render_params.flags: also accumulate, over every sample of the image, the
+ * first-hit features the denoiser reads (base colour, shading normal facing
+ * the camera, hit distance; zero where the camera ray escapes), as running
+ * means like the image.  The rendered image is unchanged. */
+#define PT_RENDER_FEATURES 1u
 
 /* Counters of the last pt_render call. */
 typedef struct pt_render_stats {
@@ -211,6 +218,17 @@ int pt_build_accel(pt_ctx* ctx, pt_accel_info* info_out /* may be NULL */);
  * PathTracer::set_camera/set_samples/set_max_bounces/update_uniforms
  * (pathtrace.cpp:381-516).  Asynchronous unless stats_out is non-NULL. */
 int pt_render(pt_ctx* ctx, const pt_render_params* params, pt_render_stats* stats_out);
+
+/* Progressive rendering without a window (the reference's interactive loop,
+ * headless): pt_set_camera keeps params (camera, image size, bounces, mode,
+ * kernel) in the context and restarts accumulation at sample 0, as
+ * PathTracer::set_camera resets sample_index (pathtrace.cpp:381-396);
+ * pt_render_next then adds `samples` samples to the running mean and advances
+ * the sample index (PathTracer::update_uniforms, pathtrace.cpp:511-516;
+ * PathTraceDispatcher::render's per-frame submission, ptdispatch.cpp:97-134).
+ * params->sample_index and params->samples are ignored by pt_set_camera. */
+int pt_set_camera(pt_ctx* ctx, const pt_render_params* params);
+int pt_render_next(pt_ctx* ctx, uint32_t samples, pt_render_stats* stats_out);
 
 /* Copy the accumulated image to host memory as RGBA rows of `pitch_bytes`
  * bytes (float when fp64 == 0, double when fp64 == 1).  Replaces the copy

@@ -70,7 +70,7 @@ class RenderParams(C.Structure):
                 ("exposure", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("sample_index", C.c_uint32), ("samples", C.c_uint32), ("max_bounces", C.c_uint32),
                 ("accum_mode", C.c_uint32), ("kernel", C.c_uint32), ("rr_start", C.c_uint32),
-                ("reserved", C.c_uint32 * 3)]
+                ("flags", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 class RenderStats(C.Structure):
@@ -111,6 +111,8 @@ SIGNATURES = [
     ("pt_upload_scene", C.c_int, [C.c_void_p, C.POINTER(SceneView)]),
     ("pt_build_accel", C.c_int, [C.c_void_p, C.POINTER(AccelInfo)]),
     ("pt_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(RenderStats)]),
+    ("pt_set_camera", C.c_int, [C.c_void_p, C.POINTER(RenderParams)]),
+    ("pt_render_next", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(RenderStats)]),
     ("pt_read_image", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]),
     ("pt_synchronize", C.c_int, [C.c_void_p]),
     ("pt_tonemap", C.c_int, [C.c_void_p]),
@@ -154,12 +156,15 @@ SIGNATURES = [
     ("pt_nn_conv3x3_wgrad", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                       C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("pt_render_features", C.c_int, [C.c_void_p, C.POINTER(RenderParams)]),
+    ("pt_read_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("pt_denoise_snapshot", C.c_int, [C.c_void_p]),
+    ("pt_denoise_snapshot_at", C.c_int, [C.c_void_p, C.c_uint32]),
     ("pt_denoise_input", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("pt_denoise", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
 ]
 
 PT_IMAGE_DENOISED = 2
+PT_RENDER_FEATURES = 1
 PT_UNET_IN_CHANNELS = 16
 PT_UNET_OUT_CHANNELS = 16
 

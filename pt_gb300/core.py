@@ -135,6 +135,17 @@ class Context:
         self.width, self.height = params.width, params.height
         return st if stats else None
 
+    def set_camera(self, params: abi.RenderParams) -> None:
+        """Keeps camera and image settings and restarts accumulation (PathTracer::set_camera)."""
+        _check(lib().pt_set_camera(self._h, C.byref(params)), self._h)
+        self.width, self.height = params.width, params.height
+
+    def render_next(self, samples: int = 1, stats: bool = True):
+        """Adds `samples` samples to the running mean of the set camera."""
+        st = abi.RenderStats()
+        _check(lib().pt_render_next(self._h, samples, C.byref(st) if stats else None), self._h)
+        return st if stats else None
+
     def synchronize(self) -> None:
         _check(lib().pt_synchronize(self._h), self._h)
 
@@ -159,34 +170,33 @@ class Context:
         """First-hit albedo / normal / depth of the camera rays of `params`' samples."""
         _check(lib().pt_render_features(self._h, C.byref(params)), self._h)
 
+    def read_features(self):
+        """(albedo + hit distance, shading normal) of the last features, [h, w, 4] float32 each."""
+        a = np.empty((self.height, self.width, 4), np.float32)
+        n = np.empty_like(a)
+        _check(lib().pt_read_features(self._h, a.ctypes.data, n.ctypes.data), self._h)
+        return a, n
+
     def denoise_snapshot(self) -> None:
         """Keeps the current mean image; the denoiser input then carries a noise estimate."""
         _check(lib().pt_denoise_snapshot(self._h), self._h)
 
-    def render_noisy(self, params: abi.RenderParams, feature_rays: int = 1) -> None:
-        """The denoiser's input side: params.samples samples in two halves (a
-        snapshot after the first half gives the noise estimate) and first-hit
-        features of `feature_rays` camera rays."""
-        s, first = params.samples, params.sample_index
+    def render_noisy(self, params: abi.RenderParams) -> None:
+        """The denoiser's input side in one render: params.samples samples with
+        the first-hit features of every sample (PT_RENDER_FEATURES) and a
+        snapshot armed at half of them (the noise estimate)."""
+        s, flags = params.samples, params.flags
         try:
             if s >= 2:
-                params.samples = s // 2
-                self.render(params, stats=False)
-                self.denoise_snapshot()
-                params.sample_index = first + s // 2
-                params.samples = s - s // 2
-                self.render(params, stats=False)
-            else:
-                self.render(params, stats=False)
-            params.sample_index = first
-            params.samples = max(1, min(feature_rays, s))
-            self.render_features(params)
+                _check(lib().pt_denoise_snapshot_at(self._h, params.sample_index + s // 2), self._h)
+            params.flags = flags | abi.PT_RENDER_FEATURES
+            self.render(params, stats=False)
         finally:
-            params.sample_index, params.samples = first, s
+            params.flags = flags
 
-    def render_denoised(self, unet, params: abi.RenderParams, feature_rays: int = 1) -> None:
+    def render_denoised(self, unet, params: abi.RenderParams) -> None:
         """render_noisy, then the network; read the result with read_denoised()."""
-        self.render_noisy(params, feature_rays)
+        self.render_noisy(params)
         self.denoise(unet, params.samples)
 
     def denoise_input(self, spp: int, dst_ptr: int, base_ptr: int | None = None) -> None:

@@ -145,11 +145,15 @@ struct pt_ctx {
     DevBuf<char> wave_state;    // wavefront path state
     uint32_t wave_paths = 0;    // paths the wave state holds
     int sm_count = 0;
+    pt_render_params camera{};  // pt_set_camera state
+    bool camera_set = false;
+    uint32_t next_sample = 0;
     DevBuf<float4> feat_a, feat_n; // denoiser features: albedo + depth, normal
     uint32_t feat_w = 0, feat_h = 0;
     DevBuf<float4> denoised;    // last pt_denoise result
     DevBuf<float4> half;        // pt_denoise_snapshot: mean image of the first samples
     uint32_t half_w = 0, half_h = 0, half_spp = 0, half_epoch = 0;
+    uint32_t snapshot_armed = 0; // pt_denoise_snapshot_at: take it at this many samples (0 = off)
     uint32_t image_epoch = 0;   // counts fresh renders (sample_index 0)
     DevBuf<float4> mse_ref;     // reference image for pt_mse_host
     DevBuf<double> mse_partial; // [0] result, [1..] per-block partial sums
@@ -612,6 +616,33 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     if (p->sample_index == 0)
         c->image_epoch++;
     RenderArgs a = render_args(c, p, fp64);
+    if (p->flags & ~PT_RENDER_FEATURES)
+        return c->fail(PT_ERR_INVALID, "unknown render flags");
+    const bool features = (p->flags & PT_RENDER_FEATURES) != 0;
+    if (features) {
+        const size_t px = (size_t)p->width * p->height;
+        if (c->feat_a.n < px) {
+            cudaError_t e = c->feat_a.alloc(px);
+            if (e == cudaSuccess)
+                e = c->feat_n.alloc(px);
+            if (e != cudaSuccess)
+                return c->cuda_fail(e, "feature buffers");
+        }
+        a.feat_a = c->feat_a.p;
+        a.feat_n = c->feat_n.p;
+    }
+    // an armed snapshot is taken inside this render when its sample range reaches it
+    const bool snap = c->snapshot_armed > p->sample_index && c->snapshot_armed <= p->sample_index + p->samples;
+    if (snap) {
+        const size_t px = (size_t)p->width * p->height;
+        if (c->half.n < px) {
+            cudaError_t e = c->half.alloc(px);
+            if (e != cudaSuccess)
+                return c->cuda_fail(e, "snapshot buffer");
+        }
+        a.snapshot = c->half.p;
+        a.snapshot_after = c->snapshot_armed;
+    }
     cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
     uint64_t pixels = (uint64_t)p->width * p->height;
     uint32_t kernel = p->kernel == PT_KERNEL_MEGA ? PT_KERNEL_MEGA : PT_KERNEL_WAVEFRONT;
@@ -651,6 +682,17 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     cudaEventRecord(c->ev1, c->stream);
     c->samples_done = p->sample_index + p->samples;
     c->have_fp64 = fp64;
+    if (features) {
+        c->feat_w = p->width;
+        c->feat_h = p->height;
+    }
+    if (snap) {
+        c->half_w = p->width;
+        c->half_h = p->height;
+        c->half_spp = c->snapshot_armed;
+        c->half_epoch = c->image_epoch;
+        c->snapshot_armed = 0;
+    }
     if (stats) {
         cudaError_t e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess)
@@ -674,6 +716,33 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
             return c->fail(PT_ERR_DEVICE, "device error word " + std::to_string(ew));
     }
     return PT_OK;
+}
+
+int pt_set_camera(pt_ctx* c, const pt_render_params* p)
+{
+    if (!c || !p)
+        return PT_ERR_INVALID;
+    if (p->width == 0 || p->height == 0)
+        return c->fail(PT_ERR_INVALID, "zero width or height");
+    c->camera = *p;
+    c->camera_set = true;
+    c->next_sample = 0;
+    return PT_OK;
+}
+
+int pt_render_next(pt_ctx* c, uint32_t samples, pt_render_stats* stats)
+{
+    if (!c)
+        return PT_ERR_INVALID;
+    if (!c->camera_set)
+        return c->fail(PT_ERR_STATE, "no camera set (pt_set_camera)");
+    pt_render_params p = c->camera;
+    p.sample_index = c->next_sample;
+    p.samples = samples;
+    int rc = pt_render(c, &p, stats);
+    if (rc == PT_OK)
+        c->next_sample += samples;
+    return rc;
 }
 
 int pt_read_image(pt_ctx* c, void* rgba, size_t pitch, int fp64)
@@ -783,6 +852,32 @@ int pt_denoise_snapshot(pt_ctx* c)
     c->half_h = c->height;
     c->half_spp = c->samples_done;
     c->half_epoch = c->image_epoch;
+    return PT_OK;
+}
+
+int pt_read_features(pt_ctx* c, float* albedo_depth, float* normal)
+{
+    if (!c)
+        return PT_ERR_INVALID;
+    if (!c->feat_a.p || c->feat_w == 0)
+        return c->fail(PT_ERR_STATE, "no features rendered");
+    cudaSetDevice(c->device);
+    const size_t bytes = (size_t)c->feat_w * c->feat_h * sizeof(float4);
+    cudaError_t e = cudaSuccess;
+    if (albedo_depth)
+        e = cudaMemcpyAsync(albedo_depth, c->feat_a.p, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && normal)
+        e = cudaMemcpyAsync(normal, c->feat_n.p, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? PT_OK : c->cuda_fail(e, "feature read-back");
+}
+
+int pt_denoise_snapshot_at(pt_ctx* c, uint32_t samples)
+{
+    if (!c)
+        return PT_ERR_INVALID;
+    c->snapshot_armed = samples;
     return PT_OK;
 }
 

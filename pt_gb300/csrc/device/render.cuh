@@ -12,6 +12,10 @@ struct RenderArgs {
     uint32_t width, height, sample_index, samples, max_bounces, rr_start;
     float4* image;          // RGBA32F running mean (the accumulation image)
     double* sum64;          // optional FP64 sums: rgb + sample count per pixel
+    float4* snapshot;       // optional: the running mean once it holds snapshot_after samples
+    uint32_t snapshot_after;
+    float4* feat_a;         // optional first-hit feature means: base colour + hit distance
+    float4* feat_n;         //   and shading normal (PT_RENDER_FEATURES)
     unsigned long long* counters; // [0] segments, [1] shadow rays, [2] paths, [3] node visits, [4] triangle tests
 };
 

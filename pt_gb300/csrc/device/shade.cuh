@@ -184,6 +184,41 @@ __device__ __forceinline__ f3 sample_light(const DevScene& s, Sampler& smp, f3 p
 }
 
 // Miss shader (pathtrace.ms.hlsl:6-11).
+// First-hit features for the denoiser: base colour and the interpolated
+// shading normal in world space, turned to face the ray.
+__device__ __forceinline__ void hit_features(const DevScene& s, const Hit& h, f3 rd, f3& albedo, f3& normal)
+{
+    const DevInstanceData* id = s.inst_data + h.inst;
+    const DevMaterial* mat = s.materials + __ldg(&id->material_index);
+    const uint32_t vbase = __ldg(&id->vertex_index), ibase = __ldg(&id->index_index);
+    const uint32_t i0 = __ldg(s.indices + ibase + h.prim * 3 + 0);
+    const uint32_t i1 = __ldg(s.indices + ibase + h.prim * 3 + 1);
+    const uint32_t i2 = __ldg(s.indices + ibase + h.prim * 3 + 2);
+    VertexF va = vfetch(s, vbase + i0), vb = vfetch(s, vbase + i1), vc = vfetch(s, vbase + i2);
+    const float ba = (1.0f - h.b1) - h.b2;
+    f3 on = normalize((ba * va.n + h.b1 * vb.n) + h.b2 * vc.n);
+    float4 n0 = ldg4(&id->n0), n1 = ldg4(&id->n1), n2 = ldg4(&id->n2);
+    normal = normalize(mul3_rows(n0, n1, n2, on));
+    if (dot(normal, rd) > 0.0f)
+        normal = -normal;
+    float4 bc = ldg4(&mat->base_colour);
+    albedo = mk3(bc.x, bc.y, bc.z);
+}
+
+// Running mean of a feature vector, the image's accumulation rule.
+__device__ __forceinline__ void feature_mean(float4& acc, float4 v, uint32_t si)
+{
+    if (si == 0) {
+        acc = v;
+    } else {
+        float n = __uint2float_rn(si + 1u);
+        acc.x = acc.x + (v.x - acc.x) / n;
+        acc.y = acc.y + (v.y - acc.y) / n;
+        acc.z = acc.z + (v.z - acc.z) / n;
+        acc.w = acc.w + (v.w - acc.w) / n;
+    }
+}
+
 __device__ __forceinline__ void shade_miss(const DevScene& s, PathState& pl)
 {
     add_radiance(pl, s.env);

@@ -32,22 +32,10 @@ __global__ void __launch_bounds__(128) k_features(RenderArgs a, float4* feat_a, 
             Hit h;
             if (!trace_closest_inl(a.s, ro, rd, a.near_plane, a.far_plane, h, tc))
                 continue;
-            const DevInstanceData* id = a.s.inst_data + h.inst;
-            const DevMaterial* mat = a.s.materials + __ldg(&id->material_index);
-            const uint32_t vbase = __ldg(&id->vertex_index), ibase = __ldg(&id->index_index);
-            const uint32_t i0 = __ldg(a.s.indices + ibase + h.prim * 3 + 0);
-            const uint32_t i1 = __ldg(a.s.indices + ibase + h.prim * 3 + 1);
-            const uint32_t i2 = __ldg(a.s.indices + ibase + h.prim * 3 + 2);
-            VertexF va = vfetch(a.s, vbase + i0), vb = vfetch(a.s, vbase + i1), vc = vfetch(a.s, vbase + i2);
-            const float ba = (1.0f - h.b1) - h.b2;
-            f3 on = normalize((ba * va.n + h.b1 * vb.n) + h.b2 * vc.n);
-            float4 n0 = ldg4(&id->n0), n1 = ldg4(&id->n1), n2 = ldg4(&id->n2);
-            f3 wn = normalize(mul3_rows(n0, n1, n2, on));
-            if (dot(wn, rd) > 0.0f)
-                wn = -wn;
-            float4 bc = ldg4(&mat->base_colour);
-            alb = alb + mk3(bc.x, bc.y, bc.z);
-            nrm = nrm + wn;
+            f3 ha, hn;
+            hit_features(a.s, h, rd, ha, hn);
+            alb = alb + ha;
+            nrm = nrm + hn;
             depth += h.t;
         }
         const float inv = 1.0f / (float)a.samples;

@@ -39,6 +39,11 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
             s64[2] = a.sum64[4 * pix + 2];
         }
         const DevScene& s = a.s;
+        float4 fa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), fn = fa;
+        if (a.feat_a) {
+            fa = a.feat_a[pix];
+            fn = a.feat_n[pix];
+        }
         for (uint32_t si = a.sample_index; si < a.sample_index + a.samples; si++) {
             PathState pl;
             pl.radiance = mk3(0.0f, 0.0f, 0.0f);
@@ -55,6 +60,13 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
             segments++;
             Hit h;
             bool hit = trace_closest(s, ro, rd, a.near_plane, a.far_plane, h, tc);
+            if (a.feat_a) {
+                f3 alb = mk3(0.0f, 0.0f, 0.0f), nrm = alb;
+                if (hit)
+                    hit_features(s, h, rd, alb, nrm);
+                feature_mean(fa, make_float4(alb.x, alb.y, alb.z, hit ? h.t : 0.0f), si);
+                feature_mean(fn, make_float4(nrm.x, nrm.y, nrm.z, 0.0f), si);
+            }
             shade_segment(s, pl, ro, rd, hit, h, shadow_rays, tc);
             if (!pl.final_segment) {
                 for (uint32_t seg = 1; seg <= a.max_bounces; seg++) {
@@ -73,11 +85,17 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
             }
             f3 r = correct_radiance(pl.radiance * a.exposure);
             accumulate(acc, r, si);
+            if (a.snapshot && si + 1 == a.snapshot_after)
+                a.snapshot[pix] = acc;
             s64[0] += (double)r.x;
             s64[1] += (double)r.y;
             s64[2] += (double)r.z;
         }
         a.image[pix] = acc;
+        if (a.feat_a) {
+            a.feat_a[pix] = fa;
+            a.feat_n[pix] = fn;
+        }
         if (a.sum64) {
             double* d = a.sum64 + 4 * pix;
             d[0] = s64[0];

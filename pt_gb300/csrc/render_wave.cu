@@ -40,6 +40,8 @@ struct WaveState {
     float4* nee_e;      // emission, w = cos_i
     float4* nee_b;      // brdf, w = pdf
     float4* nee_tp;     // throughput before the BSDF update
+    float4* f_a;        // first-hit features (PT_RENDER_FEATURES): base colour, hit distance
+    float4* f_n;        //   shading normal
     // queues
     uint32_t* queue[2];
     uint32_t* shadow_queue;
@@ -166,6 +168,10 @@ __global__ void __launch_bounds__(128) k_wf_shade(WaveArgs a, uint32_t qi)
             nee.add = false;
             nee.trace = false;
             if (prim == 0xFFFFFFFFu) {
+                if (sg == 0 && R.feat_a) {
+                    a.w.f_a[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    a.w.f_n[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                }
                 shade_miss(s, pl);
             } else {
                 float4 hh = a.w.hit[p];
@@ -175,6 +181,12 @@ __global__ void __launch_bounds__(128) k_wf_shade(WaveArgs a, uint32_t qi)
                 h.b2 = hh.z;
                 h.inst = __float_as_uint(hh.w);
                 h.prim = prim;
+                if (sg == 0 && R.feat_a) {
+                    f3 alb, nrm;
+                    hit_features(s, h, rd, alb, nrm);
+                    a.w.f_a[p] = make_float4(alb.x, alb.y, alb.z, h.t);
+                    a.w.f_n[p] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+                }
                 shade_hit(s, pl, ro, rd, h, nee);
             }
             if (nee.add && !nee.trace)
@@ -276,10 +288,23 @@ __global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs a)
             s64[1] = R.sum64[4 * (size_t)pix + 1];
             s64[2] = R.sum64[4 * (size_t)pix + 2];
         }
+        float4 fa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), fn = fa;
+        if (R.feat_a) {
+            fa = R.feat_a[pix];
+            fn = R.feat_n[pix];
+            for (uint32_t j = 0; j < a.wave_samples; j++) {
+                feature_mean(fa, a.w.f_a[(size_t)j * a.pixels + pix], a.wave_first_sample + j);
+                feature_mean(fn, a.w.f_n[(size_t)j * a.pixels + pix], a.wave_first_sample + j);
+            }
+            R.feat_a[pix] = fa;
+            R.feat_n[pix] = fn;
+        }
         for (uint32_t j = 0; j < a.wave_samples; j++) {
             float4 r4 = a.w.rad[(size_t)j * a.pixels + pix];
             f3 r = correct_radiance(mk3(r4.x, r4.y, r4.z) * R.exposure);
             accumulate(acc, r, a.wave_first_sample + j);
+            if (R.snapshot && a.wave_first_sample + j + 1 == R.snapshot_after)
+                R.snapshot[pix] = acc;
             s64[0] += (double)r.x;
             s64[1] += (double)r.y;
             s64[2] += (double)r.z;
@@ -299,7 +324,7 @@ __global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs a)
 
 size_t wave_state_bytes(uint32_t n_paths)
 {
-    return (size_t)n_paths * (16 * 11 + 4 * 5) + 4096;
+    return (size_t)n_paths * (16 * 13 + 4 * 5) + 4096;
 }
 
 static inline char* bump(char*& p, size_t bytes)
@@ -330,6 +355,8 @@ cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_byte
     a.w.nee_e = (float4*)bump(p, 16 * n);
     a.w.nee_b = (float4*)bump(p, 16 * n);
     a.w.nee_tp = (float4*)bump(p, 16 * n);
+    a.w.f_a = (float4*)bump(p, 16 * n);
+    a.w.f_n = (float4*)bump(p, 16 * n);
     a.w.queue[0] = (uint32_t*)bump(p, 4 * n);
     a.w.queue[1] = (uint32_t*)bump(p, 4 * n);
     a.w.shadow_queue = (uint32_t*)bump(p, 4 * n);

@@ -106,6 +106,12 @@ def test_input_packing_and_snapshot_rules(ctx):
     fresh.denoise_input(4, buf.data_ptr())
     x = buf.float().cpu().numpy()
     assert np.all(x[..., 14] == 1) and np.abs(x[..., 11:14]).max() > 0
+    two_calls = buf.clone()
+    # the armed snapshot, taken inside one 4-sample render, gives the same input bit for bit
+    assert abi.lib().pt_denoise_snapshot_at(fresh._h, 2) == abi.PT_OK
+    fresh.render(hs.render_params(40, 32, 4, 4))
+    fresh.denoise_input(4, buf.data_ptr())
+    assert torch.equal(buf.view(torch.int16), two_calls.view(torch.int16))
     # a fresh image invalidates the snapshot
     fresh.render(hs.render_params(40, 32, 4, 4))
     fresh.denoise_input(4, buf.data_ptr())
@@ -117,3 +123,28 @@ def test_input_packing_and_snapshot_rules(ctx):
     assert e.value.status == abi.PT_ERR_INVALID
     u.close()
     fresh.close()
+
+
+def test_features_accumulated_in_render(ctx, tmp_path):
+    """PT_RENDER_FEATURES: the same feature means from the wavefront and the
+    megakernel, the image unchanged by the flag, and the features close to the
+    stand-alone pass over the same camera rays."""
+    hs = P.HostScene.load(scenes.small_scene(tmp_path / "f", seed=0))
+    ctx.upload(hs.pack())
+    ctx.build_accel()
+    out = {}
+    for name, kern in (("wave", abi.PT_KERNEL_WAVEFRONT), ("mega", abi.PT_KERNEL_MEGA)):
+        p = hs.render_params(64, 48, 5, 6, kernel=kern)
+        ctx.render(p)
+        plain = ctx.read_image().copy()
+        p.flags = abi.PT_RENDER_FEATURES
+        ctx.render(p)
+        assert np.array_equal(plain.view(np.uint32), ctx.read_image().view(np.uint32))
+        out[name] = ctx.read_features()
+    for a, b in zip(out["wave"], out["mega"]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    ctx.render_features(hs.render_params(64, 48, 5, 6))
+    sa, sn = ctx.read_features()
+    fa, fn = out["wave"]
+    assert np.allclose(fa, sa, rtol=1e-5, atol=1e-6) and np.allclose(fn, sn, rtol=1e-5, atol=1e-6)
+    assert fa[..., 3].max() > 0 and np.abs(fn[..., :3]).max() > 0.5

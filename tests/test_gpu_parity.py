@@ -181,3 +181,27 @@ def test_kernels_agree_on_counts(ctx, mid):
     assert (a.segments, a.shadow_rays, a.paths) == (b.segments, b.shadow_rays, b.paths)
     assert a.node_visits == b.node_visits and a.tri_tests == b.tri_tests
     assert b.kernel_used == abi.PT_KERNEL_WAVEFRONT and a.kernel_used == abi.PT_KERNEL_MEGA
+
+
+def test_camera_sweep_progressive(ctx, small):
+    """pt_set_camera restarts accumulation; pt_render_next continues it: frames
+    of 1 + 2 + 3 samples equal one 6-sample render, and a second camera starts
+    from sample 0 again (pathtrace.cpp:381-396, 511-516)."""
+    hs, view = small
+    ctx.upload(view)
+    ctx.build_accel()
+    cam = hs.render_params(48, 40, 1, 5)
+    ctx.set_camera(cam)
+    for n in (1, 2, 3):
+        ctx.render_next(n)
+    swept = ctx.read_image().copy()
+    ctx.render(hs.render_params(48, 40, 6, 5))
+    assert np.array_equal(swept.view(np.uint32), ctx.read_image().view(np.uint32))
+    other = hs.render_params(48, 40, 1, 5)
+    other.exposure = 2.0
+    ctx.set_camera(other)
+    ctx.render_next(2)
+    a = ctx.read_image().copy()
+    other.samples = 2
+    ctx.render(other)
+    assert np.array_equal(a.view(np.uint32), ctx.read_image().view(np.uint32))
