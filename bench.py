@@ -465,12 +465,18 @@ def run_ours(args) -> None:
         peaks = measured_peaks()
         b = bseg_bytes(BSEG["mid"])
         achieved = (b * segs_per_step / (t_dev / args.steps) / 1e9) if b else None
+        # DRAM bytes of a render step: ncu's dram__bytes (read + write) of every
+        # render kernel of a smaller capture of the same scene, per path segment,
+        # times this step's segments (profiles/traffic.json says which capture)
         traffic = None
         tfile = ROOT / "profiles" / "traffic.json"
         if tfile.exists():
-            traffic = json.loads(tfile.read_text()).get("mid_megakernel_bytes_per_launch")
+            per_seg = json.loads(tfile.read_text()).get("mid_wavefront", {}).get("dram_bytes_per_segment")
+            if per_seg:
+                traffic = per_seg * segs_per_step
         roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": traffic,
+                "traffic_unit": "bytes per step (all render kernels)", "algorithmic_bytes": b * segs_per_step if b else None,
                 "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)" if peaks["source"] == "measured" else "fallback",
                 "bytes_per_segment": b}
         base = cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES), seconds_target=float(args.cpu_seconds)) \

@@ -105,6 +105,20 @@ typedef struct pt_material {
  * 9 of the reference (src/pathtrace/pathtrace.cpp:36-69) plus the per-instance
  * data the reference hands to the driver's acceleration-structure build
  * (src/pathtrace/accstruct.cpp:186-218). */
+/* One texture (TextureData, src/scene/texturedata.cpp:30-60): 8-bit texels,
+ * 1, 2 or 4 channels (3-channel images are stored as 4 with alpha 255),
+ * rows from the top of the image; srgb = 1 when the colour channels are
+ * sRGB-encoded (VK_FORMAT_R8G8B8A8_SRGB: base colour and emission maps,
+ * scene.cpp:42-48).  Sampled bilinearly with REPEAT addressing at level 0
+ * (src/graphics/sampler.cpp:8-22). */
+typedef struct pt_texture {
+    uint64_t offset; /* byte offset of texel (0, 0) in the texel array */
+    uint32_t width;
+    uint32_t height;
+    uint32_t channels; /* 1, 2 or 4 */
+    uint32_t srgb;     /* 0 or 1 */
+} pt_texture;
+
 typedef struct pt_scene_view {
     const float* vertices;   /* vertex_count * PT_VERTEX_FLOATS */
     uint32_t vertex_count;
@@ -125,6 +139,11 @@ typedef struct pt_scene_view {
     uint32_t light_word_count;
     uint32_t light_count;        /* bins of the top-level light alias table */
     float environment_colour[3]; /* linear (already sRGB-decoded) */
+    /* Textures referenced by materials' map bits (may be empty). */
+    const uint8_t* texels;
+    uint64_t texel_bytes;
+    const pt_texture* textures;
+    uint32_t texture_count;
 } pt_scene_view;
 
 /* Accumulation modes. */

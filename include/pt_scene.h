@@ -40,6 +40,11 @@ typedef struct pt_raw_scene {
     const float* directional_lights; /* 6 floats each: direction, colour */
     uint32_t directional_light_count;
     float environment_colour[3];
+    /* Textures (see pt_texture in pt_gpu.h); materials name them by index. */
+    const uint8_t* texels;
+    uint64_t texel_bytes;
+    const pt_texture* textures;
+    uint32_t texture_count;
 } pt_raw_scene;
 
 /* Camera description as parsed from a .scn camera section
@@ -104,6 +109,13 @@ int pt_write_png(const char* path, const float* rgba, uint32_t width, uint32_t h
  * like the stb_image reader util/meansq uses; *rgba is malloc'ed, release it
  * with pt_host_free. */
 int pt_read_hdr(const char* path, float** rgba, uint32_t* width, uint32_t* height);
+
+/* Decodes a PNG image as the reference's texture loader keeps it (stb_image
+ * with the file's channel count, 3 widened to 4; texturedata.cpp:30-48):
+ * *texels (release with pt_host_free) holds width * height * channels bytes,
+ * rows from the top.  *file_channels is the file's own channel count. */
+int pt_png_decode(const uint8_t* data, size_t size, uint8_t** texels, uint32_t* width, uint32_t* height,
+                  uint32_t* channels, uint32_t* file_channels);
 
 /* Release memory returned by pt_read_hdr. */
 void pt_host_free(void* p);

@@ -52,6 +52,11 @@ class Material(C.Structure):
                 ("sheen", C.c_float * 4), ("cc_ccrgh_aniso", C.c_float * 4)]
 
 
+class Texture(C.Structure):
+    _fields_ = [("offset", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32), ("channels", C.c_uint32),
+                ("srgb", C.c_uint32)]
+
+
 class SceneView(C.Structure):
     _fields_ = [("vertices", C.POINTER(C.c_float)), ("vertex_count", C.c_uint32),
                 ("indices", C.POINTER(C.c_uint32)), ("index_count", C.c_uint32),
@@ -61,7 +66,9 @@ class SceneView(C.Structure):
                 ("instance_count", C.c_uint32),
                 ("materials", C.POINTER(Material)), ("material_count", C.c_uint32),
                 ("light_words", C.POINTER(C.c_uint32)), ("light_word_count", C.c_uint32), ("light_count", C.c_uint32),
-                ("environment_colour", C.c_float * 3)]
+                ("environment_colour", C.c_float * 3),
+                ("texels", C.POINTER(C.c_uint8)), ("texel_bytes", C.c_uint64), ("textures", C.POINTER(Texture)),
+                ("texture_count", C.c_uint32)]
 
 
 class RenderParams(C.Structure):
@@ -93,7 +100,9 @@ class RawScene(C.Structure):
                 ("materials", C.POINTER(Material)), ("material_count", C.c_uint32),
                 ("point_lights", C.POINTER(C.c_float)), ("point_light_count", C.c_uint32),
                 ("directional_lights", C.POINTER(C.c_float)), ("directional_light_count", C.c_uint32),
-                ("environment_colour", C.c_float * 3)]
+                ("environment_colour", C.c_float * 3),
+                ("texels", C.POINTER(C.c_uint8)), ("texel_bytes", C.c_uint64), ("textures", C.POINTER(Texture)),
+                ("texture_count", C.c_uint32)]
 
 
 class CameraDesc(C.Structure):
@@ -133,6 +142,8 @@ SIGNATURES = [
     ("pt_read_hdr", C.c_int, [C.c_char_p, C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.c_uint32),
                               C.POINTER(C.c_uint32)]),
     ("pt_host_free", None, [C.c_void_p]),
+    ("pt_png_decode", C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_uint32),
+                                C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     # denoiser (include/pt_denoise.h)
     ("pt_unet_param_count", C.c_size_t, []),
     ("pt_unet_layer_shape", C.c_int, [C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),

@@ -300,6 +300,23 @@ def raw_to_struct(raw: dict):
     env = raw.get("environment_colour", (0.0, 0.0, 0.0))
     for k in range(3):
         rs.environment_colour[k] = float(env[k])
+    # textures: raw["textures"] = [(uint8 array [h, w, c], srgb)], c in 1, 2, 4
+    texs = raw.get("textures", [])
+    if texs:
+        parts, descs, off = [], (abi.Texture * len(texs))(), 0
+        for i, (img, srgb) in enumerate(texs):
+            img = np.ascontiguousarray(img, dtype=np.uint8)
+            h, w = img.shape[:2]
+            c = 1 if img.ndim == 2 else img.shape[2]
+            descs[i].offset, descs[i].width, descs[i].height, descs[i].channels, descs[i].srgb = off, w, h, c, int(srgb)
+            parts.append(img.reshape(-1))
+            off += img.size
+        texels = np.ascontiguousarray(np.concatenate(parts))
+        keep += [texels, descs]
+        rs.texels = _ptr(texels, C.c_uint8)
+        rs.texel_bytes = texels.size
+        rs.textures = descs
+        rs.texture_count = len(texs)
     return rs, keep
 
 
@@ -320,6 +337,10 @@ def struct_to_raw(rs: abi.RawScene) -> dict:
         "point_lights": a(rs.point_lights, rs.point_light_count * 6, np.float32).reshape(-1, 6),
         "directional_lights": a(rs.directional_lights, rs.directional_light_count * 6, np.float32).reshape(-1, 6),
         "environment_colour": np.array(list(rs.environment_colour), np.float32),
+        "textures": [(np.ctypeslib.as_array(rs.texels, shape=(rs.texel_bytes,))[
+                          t.offset:t.offset + t.width * t.height * t.channels].reshape(
+                          (t.height, t.width) if t.channels == 1 else (t.height, t.width, t.channels)).copy(), bool(t.srgb))
+                     for t in (rs.textures[i] for i in range(rs.texture_count))],
     }
 
 

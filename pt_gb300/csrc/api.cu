@@ -21,7 +21,7 @@
 #include "kernels.h"
 
 namespace pt {
-cudaError_t render_init_tables(const uint32_t* table128, cudaStream_t stream);
+cudaError_t render_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
 }
 
 using namespace pt;
@@ -120,6 +120,9 @@ struct pt_ctx {
     DevBuf<uint32_t> indices;
     DevBuf<DevInstanceData> inst_data;
     DevBuf<DevMaterial> materials;
+    DevBuf<uint8_t> texels;
+    DevBuf<DevTexture> textures;
+    uint32_t texture_count = 0;
     DevBuf<uint32_t> light;
     DevBuf<uint32_t> mesh_vertex_offset, mesh_index_offset, mesh_tri_base, inst_mesh;
     DevBuf<DevInstance> dinst;
@@ -298,8 +301,15 @@ pt_ctx* pt_create(int device)
     uint32_t table[4][32];
     sobol_table(table);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
-    if ((e = render_init_tables(&table[0][0], c->stream)) != cudaSuccess ||
-        (e = wave_init_tables(&table[0][0], c->stream)) != cudaSuccess) {
+    // sRGB decode of 8-bit texels (the _SRGB formats), evaluated in FP64 and rounded once
+    float srgb[256];
+    for (int i = 0; i < 256; i++) {
+        const double v = i / 255.0;
+        srgb[i] = (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
+    }
+    if ((e = render_init_tables(&table[0][0], srgb, c->stream)) != cudaSuccess ||
+        (e = wave_init_tables(&table[0][0], srgb, c->stream)) != cudaSuccess ||
+        (e = features_init_tables(&table[0][0], srgb, c->stream)) != cudaSuccess) {
         g_create_error = std::string("sampler tables: ") + cudaGetErrorString(e);
         delete c;
         return nullptr;
@@ -399,12 +409,15 @@ int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
     tb[v->mesh_count] = (uint32_t)tris;
     if (v->instance_count >= (1u << 28))
         return c->fail(PT_ERR_UNSUPPORTED, "more than 2^28 instances");
-    // materials: textures are outside this build
-    for (uint32_t i = 0; i < v->material_count; i++) {
-        uint32_t bits;
-        std::memcpy(&bits, &v->materials[i].rough_metal_normal_map_bits[3], 4);
-        if (bits & (PT_ANY_MAP_BITS & ~PT_MATERIAL_IS_TRANSPARENT_BIT))
-            return c->fail(PT_ERR_UNSUPPORTED, "material " + std::to_string(i) + " uses texture maps");
+    // textures: every texel of every texture inside the texel array
+    if (v->texture_count && (!v->textures || !v->texels))
+        return c->fail(PT_ERR_INVALID, "textures without texel data");
+    for (uint32_t i = 0; i < v->texture_count; i++) {
+        const pt_texture& t = v->textures[i];
+        if (t.width == 0 || t.height == 0 || t.width > (1u << 16) || t.height > (1u << 16) ||
+            !(t.channels == 1 || t.channels == 2 || t.channels == 4) ||
+            t.offset + (uint64_t)t.width * t.height * t.channels > v->texel_bytes)
+            return c->fail(PT_ERR_INVALID, "texture " + std::to_string(i) + " is malformed");
     }
     // instances
     c->h_dinst.assign(v->instance_count, DevInstance{});
@@ -439,6 +452,7 @@ int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
     cudaError_t e;
     static_assert(sizeof(DevInstanceData) == sizeof(pt_instance_data), "InstanceData layout");
     static_assert(sizeof(DevMaterial) == sizeof(pt_material), "PbrMaterial layout");
+    static_assert(sizeof(DevTexture) == sizeof(pt_texture), "texture descriptor layout");
     if ((e = upload(c, c->vertices, (const float4*)v->vertices, 2 * (size_t)v->vertex_count)) != cudaSuccess ||
         (e = upload(c, c->indices, v->indices, v->index_count)) != cudaSuccess ||
         (e = upload(c, c->inst_data, (const DevInstanceData*)v->instances, v->instance_count)) != cudaSuccess ||
@@ -448,7 +462,9 @@ int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
         (e = upload(c, c->mesh_index_offset, io.data(), io.size())) != cudaSuccess ||
         (e = upload(c, c->mesh_tri_base, tb.data(), tb.size())) != cudaSuccess ||
         (e = upload(c, c->inst_mesh, v->instance_mesh, v->instance_count)) != cudaSuccess ||
-        (e = upload(c, c->dinst, c->h_dinst.data(), c->h_dinst.size())) != cudaSuccess)
+        (e = upload(c, c->dinst, c->h_dinst.data(), c->h_dinst.size())) != cudaSuccess ||
+        (e = upload(c, c->texels, v->texels, (size_t)v->texel_bytes)) != cudaSuccess ||
+        (e = upload(c, c->textures, (const DevTexture*)v->textures, v->texture_count)) != cudaSuccess)
         return c->cuda_fail(e, "scene upload");
     if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
         return c->cuda_fail(e, "scene upload");
@@ -458,6 +474,7 @@ int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
     c->tri_count = (uint32_t)tris;
     c->instance_count = v->instance_count;
     c->material_count = v->material_count;
+    c->texture_count = v->texture_count;
     c->light_words = v->light_word_count;
     c->light_count = v->light_count;
     std::memcpy(c->env, v->environment_colour, sizeof(c->env));
@@ -568,6 +585,9 @@ static RenderArgs render_args(pt_ctx* c, const pt_render_params* p, bool fp64)
     a.s.light_count = c->light_count;
     a.s.instance_count = c->instance_count;
     a.s.vertex_count = c->vertex_count;
+    a.s.texels = c->texels.p;
+    a.s.textures = c->textures.p;
+    a.s.texture_count = c->texture_count;
     // A traversal of a valid BVH visits each node at most once; the cap only
     // stops a malformed tree from spinning.
     a.s.max_iterations = 4u * (uint32_t)std::min<size_t>(c->nodes.n + c->tri_count + c->instance_count, 1u << 28) + 4096u;

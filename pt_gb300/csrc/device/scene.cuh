@@ -63,6 +63,12 @@ struct DevInstanceData {
     float4 n0, n1, n2;     // normal matrix rows
 };
 
+// pt_texture (include/pt_gpu.h): 8-bit texels, 1 / 2 / 4 channels.
+struct DevTexture {
+    unsigned long long offset;
+    uint32_t width, height, channels, srgb;
+};
+
 struct DevScene {
     const float4* vertices;
     const uint32_t* indices;
@@ -74,6 +80,9 @@ struct DevScene {
     uint32_t instance_count;
     uint32_t vertex_count;
     uint32_t max_iterations; // traversal watchdog: loop iterations per ray
+    const uint8_t* texels;   // textures (may be empty)
+    const DevTexture* textures;
+    uint32_t texture_count;
     const BvhNode* nodes;
     const TriRec* tris;
     const DevInstance* dinst;
@@ -88,6 +97,94 @@ constexpr uint32_t ERR_WATCHDOG = 4u;
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 __device__ __forceinline__ int4 ldg4i(const int4* p) { return __ldg(p); }
+
+// Material map bits (constants.h of the reference; include/pt_gpu.h).
+constexpr uint32_t MAP_BASE_COLOUR = 1u << 0;
+constexpr uint32_t MAP_EMISSION = 1u << 1;
+constexpr uint32_t MAP_ROUGHNESS = 1u << 2;
+constexpr uint32_t MAP_METALNESS = 1u << 3;
+constexpr uint32_t MAP_ROUGHNESS_METALNESS = 1u << 4;
+constexpr uint32_t MAP_SPECULAR = 1u << 5;
+constexpr uint32_t MAP_SHEEN = 1u << 7;
+constexpr uint32_t MAP_CLEARCOAT = 1u << 9;
+constexpr uint32_t MAP_NORMAL = 1u << 12;
+
+// sRGB-to-linear decode of 8-bit values (the _SRGB texture formats), filled
+// from the host's FP64 evaluation of the sRGB curve (one copy per translation
+// unit, uploaded by that unit's table initialiser).
+static __constant__ float c_srgb[256];
+
+__device__ __forceinline__ float4 texel(const DevScene& s, const DevTexture& t, uint32_t x, uint32_t y)
+{
+    const uint8_t* p = s.texels + t.offset + ((unsigned long long)y * t.width + x) * t.channels;
+    if (t.channels == 4) {
+        const uint8_t r = p[0], g = p[1], b = p[2], a = p[3]; // byte loads: texture offsets need no alignment
+        if (t.srgb)
+            return make_float4(c_srgb[r], c_srgb[g], c_srgb[b], (float)a / 255.0f);
+        return make_float4((float)r / 255.0f, (float)g / 255.0f, (float)b / 255.0f, (float)a / 255.0f);
+    }
+    if (t.channels == 2)
+        return make_float4((float)p[0] / 255.0f, (float)p[1] / 255.0f, 0.0f, 1.0f);
+    return make_float4((float)p[0] / 255.0f, 0.0f, 0.0f, 1.0f);
+}
+
+// SampleLevel(uv, 0) with the reference's sampler (linear filtering, REPEAT,
+// level 0; src/graphics/sampler.cpp:8-22): uv is wrapped to [0, 1), texel
+// centres sit at (i + 0.5) / size, the four neighbours wrap, and the weights
+// combine as (1-a)(1-b) t00 + a(1-b) t10 + (1-a)b t01 + ab t11 in that order.
+// Out-of-range texture indices read zero.
+__device__ __forceinline__ float4 sample_texture(const DevScene& s, uint32_t index, f2 uv)
+{
+    if (index >= s.texture_count)
+        return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const DevTexture t = s.textures[index];
+    float u = uv.x - floorf(uv.x), v = uv.y - floorf(uv.y);
+    if (!(u >= 0.0f && u < 1.0f))
+        u = 0.0f;
+    if (!(v >= 0.0f && v < 1.0f))
+        v = 0.0f;
+    const float x = u * (float)t.width - 0.5f, y = v * (float)t.height - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float a = x - fx, b = y - fy;
+    int x0 = (int)fx, y0 = (int)fy;
+    if (x0 < 0)
+        x0 += (int)t.width;
+    if (y0 < 0)
+        y0 += (int)t.height;
+    if (x0 >= (int)t.width)
+        x0 = (int)t.width - 1;
+    if (y0 >= (int)t.height)
+        y0 = (int)t.height - 1;
+    const uint32_t x1 = (uint32_t)x0 + 1 == t.width ? 0u : (uint32_t)x0 + 1;
+    const uint32_t y1 = (uint32_t)y0 + 1 == t.height ? 0u : (uint32_t)y0 + 1;
+    const float4 t00 = texel(s, t, x0, y0), t10 = texel(s, t, x1, y0), t01 = texel(s, t, x0, y1), t11 = texel(s, t, x1, y1);
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    return make_float4(((w00 * t00.x + w10 * t10.x) + w01 * t01.x) + w11 * t11.x,
+                       ((w00 * t00.y + w10 * t10.y) + w01 * t01.y) + w11 * t11.y,
+                       ((w00 * t00.z + w10 * t10.z) + w01 * t01.z) + w11 * t11.z,
+                       ((w00 * t00.w + w10 * t10.w) + w01 * t01.w) + w11 * t11.w);
+}
+
+// Texture coordinate of a point of a triangle (get_vertex_attributes,
+// geometry.hlsli:38-47); indices outside the vertex array read zero.
+__device__ __forceinline__ f2 vertex_uv(const DevScene& s, unsigned long long i)
+{
+    if (i >= (unsigned long long)s.vertex_count)
+        return f2{0.0f, 0.0f};
+    const float4 b = __ldg(s.vertices + 2 * (size_t)i + 1);
+    return f2{b.z, b.w};
+}
+
+__device__ __forceinline__ f2 hit_uv(const DevScene& s, uint32_t inst, uint32_t prim, float b1, float b2)
+{
+    const DevInstanceData* id = s.inst_data + inst;
+    const uint32_t vbase = __ldg(&id->vertex_index), ibase = __ldg(&id->index_index);
+    const f2 ua = vertex_uv(s, (unsigned long long)vbase + __ldg(s.indices + ibase + prim * 3 + 0));
+    const f2 ub = vertex_uv(s, (unsigned long long)vbase + __ldg(s.indices + ibase + prim * 3 + 1));
+    const f2 uc = vertex_uv(s, (unsigned long long)vbase + __ldg(s.indices + ibase + prim * 3 + 2));
+    const float ba = (1.0f - b1) - b2;
+    return f2{(ba * ua.x + b1 * ub.x) + b2 * uc.x, (ba * ua.y + b1 * ub.y) + b2 * uc.y};
+}
 
 // Light-stream word with robust-buffer-access semantics (out of range reads 0).
 __device__ __forceinline__ uint32_t lw(const DevScene& s, uint32_t i) { return i < s.light_words ? __ldg(s.light + i) : 0u; }
@@ -358,6 +455,8 @@ static __device__ __forceinline__ float trace_shadow_inl(const DevScene& s, f3 o
     int ref = s.tlas_root;
     bool in_blas = false;
     bool opaque = true;
+    bool alpha_map = false; // transparent instance whose alpha comes from a base colour map
+    uint32_t alpha_tex = 0, alpha_inst = 0;
     float alpha_pass = 1.0f;
     float throughput = 1.0f;
     if (ref == REF_EMPTY)
@@ -413,6 +512,9 @@ static __device__ __forceinline__ float trace_shadow_inl(const DevScene& s, f3 o
             opaque = (flags & 1u) != 0;
             if (!opaque) {
                 uint32_t mi = __ldg(&s.inst_data[first].material_index);
+                alpha_map = (__float_as_uint(__ldg(&s.materials[mi].rmn.w)) & MAP_BASE_COLOUR) != 0;
+                alpha_tex = __float_as_uint(__ldg(&s.materials[mi].base_colour.x));
+                alpha_inst = first;
                 alpha_pass = 1.0f - __ldg(&s.materials[mi].base_colour.w);
             }
             to_object(di, o, d, r);
@@ -436,6 +538,9 @@ static __device__ __forceinline__ float trace_shadow_inl(const DevScene& s, f3 o
                     throughput = 0.0f;
                     break;
                 }
+                // shadowray.ah.hlsl:29-34: throughput *= 1 - base colour alpha at the hit
+                if (alpha_map)
+                    alpha_pass = 1.0f - sample_texture(s, alpha_tex, hit_uv(s, alpha_inst, __float_as_uint(a.w), b1, b2)).w;
                 throughput *= alpha_pass;
                 if (throughput < 1e-5f)
                     break;

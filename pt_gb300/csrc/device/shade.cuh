@@ -118,10 +118,68 @@ __device__ __forceinline__ float light_pdf(const DevScene& s, uint32_t emitter_i
     return p;
 }
 
-__device__ __forceinline__ f3 material_emission(const DevMaterial* m)
+// Material getters of material.hlsli:23-102: a set map bit replaces the
+// constant with the texture sampled at uv.
+__device__ __forceinline__ uint32_t map_bits(const DevMaterial* m)
+{
+    return __float_as_uint(__ldg(&m->rmn.w));
+}
+
+__device__ __forceinline__ f3 material_emission(const DevScene& s, const DevMaterial* m, f2 uv)
 {
     float4 e = ldg4(&m->emission);
+    if (map_bits(m) & MAP_EMISSION) {
+        float4 t = sample_texture(s, __float_as_uint(e.x), uv);
+        return mk3(t.x, t.y, t.z) * e.w;
+    }
     return mk3(e.x, e.y, e.z) * e.w;
+}
+
+__device__ __forceinline__ float4 material_base_colour(const DevScene& s, const DevMaterial* m, f2 uv)
+{
+    float4 bc = ldg4(&m->base_colour);
+    return (map_bits(m) & MAP_BASE_COLOUR) ? sample_texture(s, __float_as_uint(bc.x), uv) : bc;
+}
+
+__device__ __forceinline__ void material_rough_metal_normal(const DevScene& s, const DevMaterial* m, f2 uv, float& roughness,
+                                                            float& metalness, f3& normal)
+{
+    const float4 rmn = ldg4(&m->rmn);
+    const uint32_t bits = __float_as_uint(rmn.w);
+    if (bits & MAP_ROUGHNESS_METALNESS) {
+        const float4 t = sample_texture(s, __float_as_uint(rmn.x), uv);
+        roughness = t.y;
+        metalness = t.z;
+    } else {
+        roughness = (bits & MAP_ROUGHNESS) ? sample_texture(s, __float_as_uint(rmn.x), uv).x : rmn.x;
+        metalness = (bits & MAP_METALNESS) ? sample_texture(s, __float_as_uint(rmn.y), uv).x : rmn.y;
+    }
+    if (bits & MAP_NORMAL) {
+        const float4 t = sample_texture(s, __float_as_uint(rmn.z), uv);
+        normal = normalize(mk3(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f));
+    } else {
+        normal = mk3(0.0f, 0.0f, 1.0f);
+    }
+}
+
+__device__ __forceinline__ f3 material_rgb(const DevScene& s, const float4* field, bool mapped, f2 uv)
+{
+    const float4 v = ldg4(field);
+    if (mapped) {
+        const float4 t = sample_texture(s, __float_as_uint(v.x), uv);
+        return mk3(t.x, t.y, t.z);
+    }
+    return mk3(v.x, v.y, v.z);
+}
+
+// onb (util.hlsli:57-64): orthonormal basis around n (Duff et al. 2017).
+__device__ __forceinline__ void onb(f3 n, f3& x, f3& y)
+{
+    const float sg = n.z < 0.0f ? -1.0f : 1.0f;
+    const float a = -1.0f / (sg + n.z);
+    const float b = (n.x * n.y) * a;
+    x = mk3(1.0f + ((sg * n.x) * n.x) * a, sg * b, -sg * n.x);
+    y = mk3(b, sg + (n.y * n.y) * a, -n.y);
 }
 
 __device__ __forceinline__ f3 sample_light(const DevScene& s, Sampler& smp, f3 pt, f3& light_dir, float& light_dist, float& pdf,
@@ -154,6 +212,9 @@ __device__ __forceinline__ f3 sample_light(const DevScene& s, Sampler& smp, f3 p
         f3 pc = mul_point_rows(t0, t1, t2, vpos(s, (uint64_t)vbase + lw(s, bin_offset + 2)));
         f3 bary = random_barycentric(u12);
         f3 point = (bary.x * pa + bary.y * pb) + bary.z * pc;
+        const unsigned long long ia = (unsigned long long)vbase + lw(s, bin_offset + 0);
+        const unsigned long long ib = (unsigned long long)vbase + lw(s, bin_offset + 1);
+        const unsigned long long ic = (unsigned long long)vbase + lw(s, bin_offset + 2);
         light_dir = point - pt;
         light_dist = 1.0f;
         f3 tn = cross(pb - pa, pc - pa);
@@ -164,7 +225,14 @@ __device__ __forceinline__ f3 sample_light(const DevScene& s, Sampler& smp, f3 p
         is_delta = false;
         if (!isfinite(pdf))
             return mk3(0.0f, 0.0f, 0.0f);
-        return material_emission(s.materials + __ldg(&id->material_index));
+        // lightsample.hlsli:106-108: emission at the point's texture coordinate
+        const DevMaterial* lm = s.materials + __ldg(&id->material_index);
+        f2 luv = {0.0f, 0.0f};
+        if (map_bits(lm) & MAP_EMISSION) {
+            const f2 ua = vertex_uv(s, ia), ub = vertex_uv(s, ib), uc = vertex_uv(s, ic);
+            luv = f2{(bary.x * ua.x + bary.y * ub.x) + bary.z * uc.x, (bary.x * ua.y + bary.y * ub.y) + bary.z * uc.y};
+        }
+        return material_emission(s, lm, luv);
     } else if (light_type == LIGHT_TYPE_POINT) {
         f3 lp = mk3(__uint_as_float(lw(s, bin_offset + 1)), __uint_as_float(lw(s, bin_offset + 2)), __uint_as_float(lw(s, bin_offset + 3)));
         light_dir = lp - pt;
@@ -201,7 +269,8 @@ __device__ __forceinline__ void hit_features(const DevScene& s, const Hit& h, f3
     normal = normalize(mul3_rows(n0, n1, n2, on));
     if (dot(normal, rd) > 0.0f)
         normal = -normal;
-    float4 bc = ldg4(&mat->base_colour);
+    const f2 uv = {(ba * va.uv.x + h.b1 * vb.uv.x) + h.b2 * vc.uv.x, (ba * va.uv.y + h.b1 * vb.uv.y) + h.b2 * vc.uv.y};
+    const float4 bc = material_base_colour(s, mat, uv);
     albedo = mk3(bc.x, bc.y, bc.z);
 }
 
@@ -243,8 +312,9 @@ __device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 r
 
     float ba = (1.0f - h.b1) - h.b2;
     f3 obj_normal = normalize((ba * va.n + h.b1 * vb.n) + h.b2 * vc.n);
+    const f2 uv = {(ba * va.uv.x + h.b1 * vb.uv.x) + h.b2 * vc.uv.x, (ba * va.uv.y + h.b1 * vb.uv.y) + h.b2 * vc.uv.y};
 
-    f3 emission = material_emission(mat);
+    f3 emission = material_emission(s, mat, uv);
     if (maxc(emission) > 0.0f) {
         float4 w0 = ldg4(&di->w2o[0]), w1 = ldg4(&di->w2o[1]), w2 = ldg4(&di->w2o[2]);
         f3 obj_dir = mul3_rows(w0, w1, w2, ray_d);
@@ -271,22 +341,21 @@ __device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 r
     if (pl.final_segment)
         return;
 
-    float4 bc = ldg4(&mat->base_colour);
+    const float4 bc = material_base_colour(s, mat, uv);
     if (bc.w < sample_1d(pl.smp)) {
         pl.next_o = ray_o + ray_d * (h.t + ORIGIN_OFFSET);
         pl.next_d = ray_d;
         return;
     }
-    float4 rmn = ldg4(&mat->rmn);
-    float4 spec = ldg4(&mat->specular);
-    float4 sheen = ldg4(&mat->sheen);
+    const uint32_t bits = map_bits(mat);
     float anisotropy = __ldg(&mat->cc.z);
     BrdfInput bi;
     bi.base_colour = mk3(bc.x, bc.y, bc.z);
-    float roughness = rmn.x;
-    bi.metalness = rmn.y;
-    bi.specular = mk3(spec.x, spec.y, spec.z);
-    bi.sheen = mk3(sheen.x, sheen.y, sheen.z);
+    float roughness;
+    f3 mapped_normal;
+    material_rough_metal_normal(s, mat, uv, roughness, bi.metalness, mapped_normal);
+    bi.specular = material_rgb(s, &mat->specular, (bits & MAP_SPECULAR) != 0, uv);
+    bi.sheen = material_rgb(s, &mat->sheen, (bits & MAP_SHEEN) != 0, uv);
     roughness = fmaxf(0.00001f, roughness * roughness);
     float aspect = sqrtf(1.0f - 0.9f * fabsf(anisotropy));
     bi.alpha = f2{roughness / aspect, roughness * aspect};
@@ -320,8 +389,18 @@ __device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 r
     f3 twn = normalize(mul3_rows(n0, n1, n2, true_obj_normal));
     if (dot(ray_d, twn) > 0.0f)
         twn = -twn;
-    // Normal maps are rejected at upload, so the mapped-normal rotation of
-    // pathtrace.ch.hlsl:322-326 never applies.
+    // mapped normal (pathtrace.ch.hlsl:321-326): rows of the world-to-shading
+    // matrix become float3x3(mx, my, mn) x float3x3(wx, wy, wn)
+    if (mapped_normal.z < 0.999f) {
+        f3 mx, my;
+        onb(mapped_normal, mx, my);
+        const f3 rx = (mx.x * wx + mx.y * wy) + mx.z * wn;
+        const f3 ry = (my.x * wx + my.y * wy) + my.z * wn;
+        const f3 rn = (mapped_normal.x * wx + mapped_normal.y * wy) + mapped_normal.z * wn;
+        wx = rx;
+        wy = ry;
+        wn = rn;
+    }
     f3 nd = -ray_d;
     f3 o = normalize(mk3(dot(wx, nd), dot(wy, nd), dot(wn, nd)));
     if (o.z <= 0.0f) {

@@ -95,6 +95,17 @@ unsigned grid_for(uint32_t n, int threads)
 
 } // namespace
 
+// This unit's copies of the sampler's direction numbers and the sRGB table.
+cudaError_t features_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream)
+{
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_sobol, table128, sizeof(uint32_t) * 128, 0, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyToSymbolAsync(c_srgb, srgb256, sizeof(float) * 256, 0, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess)
+        return e;
+    return cudaStreamSynchronize(stream);
+}
+
 cudaError_t launch_features(const RenderArgs& a, float4* feat_a, float4* feat_n, cudaStream_t st)
 {
     k_features<<<grid_for(a.width * a.height, 128), 128, 0, st>>>(a, feat_a, feat_n);

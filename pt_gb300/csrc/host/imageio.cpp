@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../../include/pt_scene.h"
+#include "png.h"
 
 namespace {
 
@@ -282,3 +283,25 @@ int pt_read_hdr(const char* path, float** rgba, uint32_t* width, uint32_t* heigh
 void pt_host_free(void* p) { std::free(p); }
 
 } // extern "C"
+
+int pt_png_decode(const uint8_t* data, size_t size, uint8_t** texels, uint32_t* width, uint32_t* height,
+                  uint32_t* channels, uint32_t* file_channels)
+{
+    if (!data || !texels || !width || !height || !channels)
+        return PT_ERR_INVALID;
+    pt::host::PngImage img;
+    std::string err;
+    if (!pt::host::png_decode(data, size, img, err))
+        return PT_ERR_IO;
+    uint8_t* out = (uint8_t*)std::malloc(img.texels.size());
+    if (!out)
+        return PT_ERR_OOM;
+    std::memcpy(out, img.texels.data(), img.texels.size());
+    *texels = out;
+    *width = img.width;
+    *height = img.height;
+    *channels = img.channels;
+    if (file_channels)
+        *file_channels = img.file_channels;
+    return PT_OK;
+}

@@ -28,6 +28,7 @@
 
 #include "../../../include/pt_scene.h"
 #include "json.h"
+#include "png.h"
 
 using pth::Json;
 
@@ -186,6 +187,13 @@ std::string directory_of(const std::string& file)
 }
 
 // ---------------------------------------------------------------- loaded model
+// One texture as the reference's TextureData holds it: 8-bit texels with 1, 2
+// or 4 channels (3-channel images widened to 4), srgb only meaningful for 4.
+struct HostTexture {
+    uint32_t width = 0, height = 0, channels = 0, srgb = 0;
+    std::vector<uint8_t> texels;
+};
+
 struct Model {
     std::vector<float> vertices; // PT_VERTEX_FLOATS each
     std::vector<uint32_t> indices;
@@ -194,7 +202,19 @@ struct Model {
     std::vector<std::vector<Mat4>> mesh_instances;
     std::vector<pt_material> materials;
     std::vector<float> point_lights, dir_lights;
+    std::vector<HostTexture> textures;
 };
+
+// TextureData::has_alpha_less_than_one (texturedata.cpp:150-164).
+bool has_alpha_below_one(const HostTexture& t)
+{
+    if (t.channels != 4)
+        return false;
+    for (size_t i = 0; i < (size_t)t.width * t.height; i++)
+        if (t.texels[4 * i + 3] < 255)
+            return true;
+    return false;
+}
 
 std::vector<uint8_t> decode_base64(const std::string& s)
 {
@@ -279,7 +299,8 @@ struct Accessor {
 //    sheen to 0, clearcoat 0 with roughness 0.5, anisotropy 0 (:263-295);
 //  - KHR_materials_emissive_strength gives the emission strength (:140-143);
 //  - KHR_materials_transmission gives opacity = 1 - transmission (:96-108).
-// Textures, cameras and lights inside glTF files are not imported.
+// Textures: PNG images (files, data URIs or buffer views); JPEG is rejected.
+// Cameras and lights inside glTF files are not imported.
 Model load_gltf(const std::string& path)
 {
     std::string text = read_file(path);
@@ -330,40 +351,157 @@ Model load_gltf(const std::string& path)
     };
 
     Model md;
-    // materials
+    // Textures get an index per image in first-use order over the materials
+    // (process_texture, scene.cpp:50-72), keyed by the image path (embedded
+    // images by "*n"); the type of the first use decides sRGB (:42-48).
+    struct TexSource {
+        int64_t image;
+        bool srgb;
+    };
+    std::unordered_map<std::string, uint32_t> tex_index;
+    std::vector<TexSource> tex_src;
+    auto texture = [&](const Json& info, bool srgb) -> int64_t {
+        if (info.kind != Json::OBJ)
+            return -1;
+        const Json& t = doc["textures"][(size_t)info["index"].integer(-1)];
+        if (t.kind != Json::OBJ)
+            throw std::runtime_error("material names a missing texture");
+        const int64_t img = t["source"].integer(-1);
+        const Json& im = doc["images"][(size_t)img];
+        if (im.kind != Json::OBJ)
+            throw std::runtime_error("texture without an image");
+        const bool external = im.has("uri") && im["uri"].str.rfind("data:", 0) != 0;
+        const std::string key = external ? im["uri"].str : "*" + std::to_string(img);
+        auto it = tex_index.find(key);
+        if (it != tex_index.end())
+            return it->second;
+        const uint32_t idx = (uint32_t)tex_src.size();
+        tex_index[key] = idx;
+        tex_src.push_back({img, srgb});
+        return idx;
+    };
+    // materials, in the reference's order of texture lookups (scene.cpp:358-383)
     for (size_t i = 0; i < doc["materials"].size(); i++) {
         const Json& m = doc["materials"][i];
         pt_material pm;
         std::memset(&pm, 0, sizeof(pm));
         uint32_t map_bits = 0;
         const Json& pbr = m["pbrMetallicRoughness"];
-        const Json& bcf = pbr["baseColorFactor"];
-        float base[3] = {(float)bcf[0].number(1.0), (float)bcf[1].number(1.0), (float)bcf[2].number(1.0)};
-        if (pbr.has("baseColorTexture") || pbr.has("metallicRoughnessTexture") || m.has("normalTexture") || m.has("emissiveTexture"))
-            map_bits |= PT_BASE_COLOUR_MAP_BIT; // textures: flagged so the device rejects them
-        float opacity = 1.0f;
         const Json& ext = m["extensions"];
-        if (ext.has("KHR_materials_transmission"))
-            opacity = 1.0f - (float)ext["KHR_materials_transmission"]["transmissionFactor"].number(0.0);
-        for (int k = 0; k < 3; k++)
-            pm.base_colour[k] = from_srgb(base[k]);
-        pm.base_colour[3] = opacity;
-        const Json& ef = m["emissiveFactor"];
-        for (int k = 0; k < 3; k++)
-            pm.emission[k] = from_srgb((float)ef[(size_t)k].number(0.0));
+        // base colour (:74-112): a map stores its index and leaves alpha 0
+        int64_t t = texture(pbr["baseColorTexture"], true);
+        if (t >= 0) {
+            map_bits |= PT_BASE_COLOUR_MAP_BIT;
+            pm.base_colour[0] = bitsf((uint32_t)t);
+        } else {
+            const Json& bcf = pbr["baseColorFactor"];
+            float base[3] = {(float)bcf[0].number(1.0), (float)bcf[1].number(1.0), (float)bcf[2].number(1.0)};
+            float opacity = 1.0f;
+            if (ext.has("KHR_materials_transmission"))
+                opacity = 1.0f - (float)ext["KHR_materials_transmission"]["transmissionFactor"].number(0.0);
+            for (int k = 0; k < 3; k++)
+                pm.base_colour[k] = from_srgb(base[k]);
+            pm.base_colour[3] = opacity;
+        }
+        // emission (:114-147)
+        t = texture(m["emissiveTexture"], true);
+        if (t >= 0) {
+            map_bits |= PT_EMISSION_MAP_BIT;
+            pm.emission[0] = bitsf((uint32_t)t);
+        } else {
+            const Json& ef = m["emissiveFactor"];
+            for (int k = 0; k < 3; k++)
+                pm.emission[k] = from_srgb((float)ef[(size_t)k].number(0.0));
+        }
         pm.emission[3] = ext.has("KHR_materials_emissive_strength")
                              ? (float)ext["KHR_materials_emissive_strength"]["emissiveStrength"].number(1.0)
                              : 1.0f;
-        pm.rough_metal_normal_map_bits[0] = (float)pbr["roughnessFactor"].number(1.0);
-        pm.rough_metal_normal_map_bits[1] = (float)pbr["metallicFactor"].number(1.0);
-        pm.specular[0] = pm.specular[1] = pm.specular[2] = 0.5f;
-        pm.cc_ccrgh_aniso[0] = 0.0f;
+        // roughness / metalness / normal (:149-207): glTF has the combined map
+        t = texture(pbr["metallicRoughnessTexture"], false);
+        if (t >= 0) {
+            map_bits |= PT_ROUGHNESS_METALNESS_MAP_BIT;
+            pm.rough_metal_normal_map_bits[0] = bitsf((uint32_t)t);
+        } else {
+            pm.rough_metal_normal_map_bits[0] = (float)pbr["roughnessFactor"].number(1.0);
+            pm.rough_metal_normal_map_bits[1] = (float)pbr["metallicFactor"].number(1.0);
+        }
+        t = texture(m["normalTexture"], false);
+        if (t >= 0) {
+            map_bits |= PT_NORMAL_MAP_BIT;
+            pm.rough_metal_normal_map_bits[2] = bitsf((uint32_t)t);
+        }
+        // specular, sheen, clearcoat (:209-296) from the KHR extensions' textures
+        t = texture(ext["KHR_materials_specular"]["specularColorTexture"], false);
+        if (t >= 0) {
+            map_bits |= PT_SPECULAR_MAP_BIT;
+            pm.specular[0] = bitsf((uint32_t)t);
+        } else {
+            pm.specular[0] = pm.specular[1] = pm.specular[2] = 0.5f;
+        }
+        t = texture(ext["KHR_materials_sheen"]["sheenColorTexture"], false);
+        if (t >= 0) {
+            map_bits |= PT_SHEEN_MAP_BIT;
+            pm.sheen[0] = bitsf((uint32_t)t);
+        }
+        t = texture(ext["KHR_materials_clearcoat"]["clearcoatTexture"], false);
+        if (t >= 0) {
+            map_bits |= PT_CLEARCOAT_MAP_BIT;
+            pm.cc_ccrgh_aniso[0] = bitsf((uint32_t)t);
+        } else {
+            pm.cc_ccrgh_aniso[0] = 0.0f;
+        }
         pm.cc_ccrgh_aniso[1] = 0.5f;
         pm.cc_ccrgh_aniso[2] = 0.0f;
-        if (pm.base_colour[3] < 1.0f && !(map_bits & PT_BASE_COLOUR_MAP_BIT))
-            map_bits |= PT_MATERIAL_IS_TRANSPARENT_BIT;
         pm.rough_metal_normal_map_bits[3] = bitsf(map_bits);
         md.materials.push_back(pm);
+    }
+    // texture images (load_textures, scene.cpp:318-342; stb_image channel rules)
+    for (const TexSource& src : tex_src) {
+        const Json& im = doc["images"][(size_t)src.image];
+        std::vector<uint8_t> bytes;
+        std::string what;
+        if (im.has("uri")) {
+            const std::string& uri = im["uri"].str;
+            what = uri;
+            if (uri.rfind("data:", 0) == 0) {
+                size_t comma = uri.find(',');
+                bytes = decode_base64(comma == std::string::npos ? "" : uri.substr(comma + 1));
+            } else {
+                std::string f = read_file(dir + uri);
+                bytes.assign(f.begin(), f.end());
+            }
+        } else {
+            const Json& bv = doc["bufferViews"][(size_t)im["bufferView"].integer(-1)];
+            if (bv.kind != Json::OBJ)
+                throw std::runtime_error("image without data");
+            size_t buf = (size_t)bv["buffer"].integer(0);
+            size_t off = (size_t)bv["byteOffset"].integer(0), len = (size_t)bv["byteLength"].integer(0);
+            if (buf >= buffers.size() || off + len > buffers[buf].size())
+                throw std::runtime_error("image buffer view outside its buffer");
+            bytes.assign(buffers[buf].begin() + off, buffers[buf].begin() + off + len);
+            what = "embedded image " + std::to_string(src.image);
+        }
+        if (bytes.size() >= 3 && bytes[0] == 0xFF && bytes[1] == 0xD8 && bytes[2] == 0xFF)
+            throw std::runtime_error("Failed to read texture " + what + " (JPEG textures are not supported)");
+        pt::host::PngImage png;
+        std::string err;
+        if (!pt::host::png_decode(bytes.data(), bytes.size(), png, err))
+            throw std::runtime_error("Failed to read texture " + what + ": " + err);
+        HostTexture ht;
+        ht.width = png.width;
+        ht.height = png.height;
+        ht.channels = png.channels;
+        ht.srgb = (png.channels == 4 && src.srgb) ? 1u : 0u;
+        ht.texels = std::move(png.texels);
+        md.textures.push_back(std::move(ht));
+    }
+    // transparency (has_transparency, scene.cpp:344-355)
+    for (pt_material& pm : md.materials) {
+        uint32_t bits = fbits(pm.rough_metal_normal_map_bits[3]);
+        bool transparent = (bits & PT_BASE_COLOUR_MAP_BIT) ? has_alpha_below_one(md.textures[fbits(pm.base_colour[0])])
+                                                            : pm.base_colour[3] < 1.0f;
+        if (transparent)
+            pm.rough_metal_normal_map_bits[3] = bitsf(bits | PT_MATERIAL_IS_TRANSPARENT_BIT);
     }
     // meshes: one entry per primitive
     std::vector<std::vector<uint32_t>> gltf_mesh_prims(doc["meshes"].size());
@@ -604,6 +742,8 @@ struct pt_host_scene {
     std::vector<float> point_lights, dir_lights;
     float env[3] = {0, 0, 0};
     pt_camera_desc camera{};
+    std::vector<pt_texture> textures;
+    std::vector<uint8_t> texels;
     // packed
     bool packed = false;
     std::vector<pt_instance_data> inst;
@@ -646,7 +786,54 @@ struct pt_host_scene {
                 }
             mesh_instance_offset.push_back((uint32_t)(instance_matrices.size() / 16));
         }
-        materials.insert(materials.end(), md.materials.begin(), md.materials.end());
+        // textures of this object follow the scene's; its materials' map
+        // indices move by the same offset (scenebuild.cpp:315-361, offset_maps_by
+        // in material.cpp:16-42, which offsets the specular and sheen maps in the
+        // .w slots while the shader reads them from .x)
+        const uint32_t toff = (uint32_t)textures.size();
+        for (pt_material pm : md.materials) {
+            const uint32_t bits = fbits(pm.rough_metal_normal_map_bits[3]);
+            auto shift = [&](float& f) { f = bitsf(fbits(f) + toff); };
+            if (bits & PT_BASE_COLOUR_MAP_BIT)
+                shift(pm.base_colour[0]);
+            if (bits & PT_EMISSION_MAP_BIT)
+                shift(pm.emission[0]);
+            if ((bits & PT_ROUGHNESS_MAP_BIT) || (bits & PT_ROUGHNESS_METALNESS_MAP_BIT))
+                shift(pm.rough_metal_normal_map_bits[0]);
+            if (bits & PT_METALNESS_MAP_BIT)
+                shift(pm.rough_metal_normal_map_bits[1]);
+            if (bits & PT_SPECULAR_TINT_MAP_BIT)
+                shift(pm.specular[0]);
+            if (bits & PT_SPECULAR_MAP_BIT)
+                shift(pm.specular[3]);
+            if (bits & PT_SHEEN_TINT_MAP_BIT)
+                shift(pm.sheen[0]);
+            if (bits & PT_SHEEN_MAP_BIT)
+                shift(pm.sheen[3]);
+            if (bits & PT_CLEARCOAT_MAP_BIT)
+                shift(pm.cc_ccrgh_aniso[0]);
+            if (bits & PT_CLEARCOAT_ROUGHNESS_MAP_BIT)
+                shift(pm.cc_ccrgh_aniso[1]);
+            if (bits & PT_ANISOTROPY_MAP_BIT)
+                shift(pm.cc_ccrgh_aniso[2]);
+            if (bits & PT_NORMAL_MAP_BIT)
+                shift(pm.rough_metal_normal_map_bits[2]);
+            materials.push_back(pm);
+        }
+        for (const HostTexture& t : md.textures)
+            add_texture(t.width, t.height, t.channels, t.srgb, t.texels.data());
+    }
+
+    void add_texture(uint32_t w, uint32_t h, uint32_t ch, uint32_t srgb, const uint8_t* data)
+    {
+        pt_texture d;
+        d.offset = texels.size();
+        d.width = w;
+        d.height = h;
+        d.channels = ch;
+        d.srgb = srgb;
+        textures.push_back(d);
+        texels.insert(texels.end(), data, data + (size_t)w * h * ch);
     }
 };
 
@@ -846,6 +1033,13 @@ pt_host_scene* pt_scene_from_raw(const pt_raw_scene* raw, const pt_camera_desc* 
         if (raw->directional_light_count)
             s->dir_lights.assign(raw->directional_lights, raw->directional_lights + 6 * (size_t)raw->directional_light_count);
         std::memcpy(s->env, raw->environment_colour, sizeof(s->env));
+        for (uint32_t i = 0; i < raw->texture_count; i++) {
+            const pt_texture& t = raw->textures[i];
+            if (t.width == 0 || t.height == 0 || !(t.channels == 1 || t.channels == 2 || t.channels == 4) ||
+                t.offset + (uint64_t)t.width * t.height * t.channels > raw->texel_bytes)
+                throw std::runtime_error("texture " + std::to_string(i) + " is malformed");
+            s->add_texture(t.width, t.height, t.channels, t.srgb ? 1u : 0u, raw->texels + t.offset);
+        }
         for (uint32_t m = 0; m < raw->mesh_count; m++) {
             if (s->mesh_material[m] >= raw->material_count)
                 throw std::runtime_error("mesh " + std::to_string(m) + " names a missing material");
@@ -885,6 +1079,10 @@ int pt_scene_raw(const pt_host_scene* s, pt_raw_scene* out)
     out->directional_lights = s->dir_lights.data();
     out->directional_light_count = (uint32_t)(s->dir_lights.size() / 6);
     std::memcpy(out->environment_colour, s->env, sizeof(s->env));
+    out->texels = s->texels.data();
+    out->texel_bytes = s->texels.size();
+    out->textures = s->textures.data();
+    out->texture_count = (uint32_t)s->textures.size();
     return PT_OK;
 }
 
@@ -894,6 +1092,90 @@ int pt_scene_camera(const pt_host_scene* s, pt_camera_desc* out)
         return PT_ERR_INVALID;
     *out = s->camera;
     return PT_OK;
+}
+
+// The reference's generators (src/rng.cpp): xoshiro128++ and splitmix32.
+struct Xshiro128 {
+    uint32_t s[4];
+    static uint32_t rotl(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }
+    uint32_t next()
+    {
+        const uint32_t result = rotl(s[0] + s[3], 7) + s[0];
+        const uint32_t t = s[1] << 9;
+        s[2] ^= s[0];
+        s[3] ^= s[1];
+        s[1] ^= s[2];
+        s[0] ^= s[3];
+        s[2] ^= t;
+        s[3] = rotl(s[3], 11);
+        return result;
+    }
+    // static_cast<float>(next()) / UINT32_MAX: the divisor rounds to 2^32 in float
+    float next_float() { return (float)next() / 4294967296.0f; }
+};
+
+struct Splitmix32 {
+    uint32_t state;
+    uint32_t next()
+    {
+        uint32_t z = (state += 0x9e3779b9u);
+        z = (z ^ (z >> 16)) * 0x85ebca6bu;
+        z = (z ^ (z >> 13)) * 0xc2b2ae35u;
+        return z ^ (z >> 16);
+    }
+};
+
+// Nearest texel of one coordinate: x = min((uint32_t)roundf(frac * size), size - 1)
+// (lightsample.cpp:70-73).  The cast of a negative value is undefined in C++;
+// GCC on x86 wraps it to a large number that the min() clamps, which is what
+// happens here on every platform.
+uint32_t nearest_texel(float f, uint32_t size)
+{
+    const float r = std::roundf(f);
+    if (r < 0.0f || r >= 4294967296.0f)
+        return size - 1;
+    return std::min((uint32_t)r, size - 1);
+}
+
+// calculate_object_intensity (lightsample.cpp:41-87) for an emission map:
+// 20 random points per triangle, nearest texel, raw 8-bit / 255 channels.
+double textured_intensity(const pt_host_scene* s, size_t mesh, const pt_material& mat)
+{
+    Splitmix32 seeder{0xbd7a0d48u};
+    // Xshiro128 rng(seeder.next() x 4): GCC evaluates those arguments right to left
+    const uint32_t a = seeder.next(), b = seeder.next(), c = seeder.next(), d = seeder.next();
+    Xshiro128 rng{{d, c, b, a}};
+    const uint32_t ti = fbits(mat.emission[0]);
+    if (ti >= s->textures.size())
+        throw std::runtime_error("emission map names a missing texture");
+    const pt_texture& tex = s->textures[ti];
+    const uint8_t* texels = s->texels.data() + tex.offset;
+    const pt_mesh_range& r = s->meshes[mesh];
+    double total = 0.0;
+    for (uint32_t t = 0; t < r.tri_count; t++) {
+        const uint32_t* ix = &s->indices[r.index_offset + 3 * t];
+        const float* va = &s->vertices[(size_t)(r.vertex_offset + ix[0]) * PT_VERTEX_FLOATS];
+        const float* vb = &s->vertices[(size_t)(r.vertex_offset + ix[1]) * PT_VERTEX_FLOATS];
+        const float* vc = &s->vertices[(size_t)(r.vertex_offset + ix[2]) * PT_VERTEX_FLOATS];
+        double tri_sum = 0.0;
+        for (int j = 0; j < 20; j++) {
+            const float beta = 1.0f - std::sqrt(rng.next_float());
+            const float gamma = (1.0f - beta) * rng.next_float();
+            const float alpha = (1.0f - beta) - gamma;
+            const float u = (alpha * va[6] + beta * vb[6]) + gamma * vc[6];
+            const float v = (alpha * va[7] + beta * vb[7]) + gamma * vc[7];
+            float integral;
+            const uint32_t x = nearest_texel(std::modf(u, &integral) * (float)tex.width, tex.width);
+            const uint32_t y = nearest_texel(std::modf(v, &integral) * (float)tex.height, tex.height);
+            const uint8_t* p = texels + ((size_t)y * tex.width + x) * tex.channels;
+            const float er = p[0] / 255.0f;
+            const float eg = tex.channels >= 2 ? p[1] / 255.0f : 0.0f;
+            const float eb = tex.channels == 4 ? p[2] / 255.0f : 0.0f;
+            tri_sum += (er + eg) + eb;
+        }
+        total += tri_sum;
+    }
+    return total * (double)mat.emission[3] / (double)((size_t)r.tri_count * 20u);
 }
 
 // SceneBuffer::build (scenebuffer.cpp:65-168) + TableLightSampler
@@ -957,8 +1239,6 @@ int pt_scene_pack(pt_host_scene* s, pt_scene_view* v)
                     const pt_material& mat = s->materials[s->mesh_material[m]];
                     if (!is_emitter(mat))
                         continue;
-                    if (fbits(mat.rough_metal_normal_map_bits[3]) & PT_EMISSION_MAP_BIT)
-                        throw std::runtime_error("textured emitters are not supported");
                     size_t ti;
                     auto it = table_of.find((uint32_t)m);
                     if (it == table_of.end()) {
@@ -983,7 +1263,9 @@ int pt_scene_pack(pt_host_scene* s, pt_scene_view* v)
                     } else {
                         ti = it->second;
                     }
-                    float intensity = (float)(double)(((mat.emission[0] + mat.emission[1]) + mat.emission[2]) * mat.emission[3]);
+                    float intensity = (fbits(mat.rough_metal_normal_map_bits[3]) & PT_EMISSION_MAP_BIT)
+                                          ? (float)textured_intensity(s, m, mat)
+                                          : (float)(double)(((mat.emission[0] + mat.emission[1]) + mat.emission[2]) * mat.emission[3]);
                     weights.push_back(intensity);
                     values.push_back({PT_LIGHT_TYPE_EMITTER, 0u, (uint32_t)tw[ti].size(), s->mesh_instance_offset[m],
                                       s->mesh_instance_offset[m + 1] - s->mesh_instance_offset[m], 0u, 0u});
@@ -1024,6 +1306,10 @@ int pt_scene_pack(pt_host_scene* s, pt_scene_view* v)
         v->light_word_count = (uint32_t)s->light.size();
         v->light_count = s->light_count;
         std::memcpy(v->environment_colour, s->env, sizeof(s->env));
+        v->texels = s->texels.data();
+        v->texel_bytes = s->texels.size();
+        v->textures = s->textures.data();
+        v->texture_count = (uint32_t)s->textures.size();
         return PT_OK;
     } catch (const std::exception& e) {
         g_error = e.what();

@@ -20,7 +20,8 @@ cudaError_t launch_megakernel(const RenderArgs& a, cudaStream_t stream);
 size_t wave_state_bytes(uint32_t n_paths_max);
 cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
                              uint32_t* launches, cudaStream_t stream);
-cudaError_t wave_init_tables(const uint32_t* table128, cudaStream_t stream);
+cudaError_t wave_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
+cudaError_t features_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
 
 // Denoiser features and packing (features.cu).
 cudaError_t launch_features(const RenderArgs& a, float4* feat_a, float4* feat_n, cudaStream_t stream);

@@ -350,6 +350,8 @@ cudaError_t conv3x3_rows(const ConvCall& c, const CUtensorMap* halo_map, int sm_
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(k_conv3x3_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
+        if (e == cudaSuccess) // all of L1 as shared memory, so two CTAs fit on an SM
+            e = cudaFuncSetAttribute(k_conv3x3_rows, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if (e != cudaSuccess)
             return e;
         attr = true;

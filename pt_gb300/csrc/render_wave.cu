@@ -413,9 +413,11 @@ cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_byte
     return cudaGetLastError();
 }
 
-cudaError_t wave_init_tables(const uint32_t* table128, cudaStream_t stream)
+cudaError_t wave_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream)
 {
     cudaError_t e = cudaMemcpyToSymbolAsync(c_sobol, table128, sizeof(uint32_t) * 128, 0, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyToSymbolAsync(c_srgb, srgb256, sizeof(float) * 256, 0, cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess)
         return e;
     return cudaStreamSynchronize(stream);

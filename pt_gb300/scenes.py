@@ -413,3 +413,98 @@ def tiny_raw(kind: str = "two_tris") -> tuple[dict, dict]:
     # eye (0, 1.5, 4) looking at the origin: position -eye, lookdir eye - target
     cam = {"position": (0.0, -1.5, -4.0), "lookdir": (0.0, 1.5, 4.0), "fov_degrees": 50.0}
     return raw, cam
+
+
+def material_row(base, rough=0.5, metal=0.0, emission=0.0, alpha=1.0) -> np.ndarray:
+    """One pt_material row (24 floats).  alpha < 1 sets the transparency bit,
+    as the scene builder does for KHR_materials_transmission (opacity =
+    1 - transmission, scene.cpp:96-108)."""
+    m = np.zeros(24, np.float32)
+    m[0:3] = base
+    m[3] = alpha
+    m[4:7] = 1.0 if emission > 0 else 0.0
+    m[7] = emission if emission > 0 else 1.0
+    m[8] = rough
+    m[9] = metal
+    bits = (1 << 13) if alpha < 1.0 else 0
+    m[11] = np.frombuffer(np.uint32(bits).tobytes(), np.float32)[0]
+    m[12:15] = 0.5
+    m[21] = 0.5
+    return m
+
+
+def assemble_raw(meshes, env) -> dict:
+    """meshes: [((p, n, uv, ix), material row, [4x4 object-to-world matrices])]."""
+    v, idx, ranges, mm, mio, inst, mats = [], [], [], [], [0], [], []
+    voff = ioff = 0
+    for (p, n, uv, ix), mat, insts in meshes:
+        v.append(np.concatenate([p, n, uv], 1))
+        idx.append(ix.reshape(-1))
+        ranges.append((voff, ioff, len(ix), len(p)))
+        voff += len(p)
+        ioff += ix.size
+        mats.append(mat)
+        mm.append(len(mats) - 1)
+        for M in insts:
+            inst.append(np.asarray(M, np.float32).T.reshape(-1))  # column-major
+        mio.append(mio[-1] + len(insts))
+    return {"vertices": np.concatenate(v).astype(np.float32), "indices": np.concatenate(idx).astype(np.uint32),
+            "meshes": np.array(ranges, np.uint32), "mesh_material": np.array(mm, np.uint32),
+            "mesh_instance_offset": np.array(mio, np.uint32), "instance_matrices": np.array(inst, np.float32),
+            "materials": np.array(mats, np.float32), "environment_colour": np.asarray(env, np.float32)}
+
+
+def _displaced_sphere(subdiv: int, rng: np.random.Generator):
+    p, n, uv, ix = icosphere(subdiv)
+    waves = rng.uniform(1, 5, (3, 3))
+    ph = rng.uniform(0, 6.283, 3)
+    d = 1.0 + 0.06 * sum(np.sin(p @ waves[k] * 3.0 + ph[k]) for k in range(3))
+    return (p * d[:, None]).astype(np.float32), n, uv, ix
+
+
+def heavy_scene(seed: int = 3, instances: int = 10000, grids: int = 32, spheres: int = 32, grid_n: int = 144,
+                sphere_subdiv: int = 5, emitters: int = 256):
+    """The heavy benchmark scene as a raw scene: 64 BLASes totalling ~2M unique
+    triangles (32 displaced 144x144 grids of 41,472 triangles, 32 displaced
+    subdivision-5 icospheres of 20,480), 10,000 instances with random rotation
+    (angle U(1e-5, 2 pi)), scale and translation, 10 % of the meshes
+    transmissive (opacity 0.1: the reference maps glTF transmission to
+    opacity), 256 single-triangle emitters with radiance log-uniform in
+    [1, 100].  Returns (raw, camera) for HostScene.from_raw; render at
+    1920x1080 with 12 bounces and Russian roulette from segment 4."""
+    rng = np.random.default_rng(seed)
+    srng = SceneRng(seed)
+    base = [displaced_grid(grid_n, srng, amplitude=0.1) for _ in range(grids)] + \
+           [_displaced_sphere(sphere_subdiv, rng) for _ in range(spheres)]
+    mats = []
+    for k in range(len(base)):
+        transmissive = rng.random() < 0.1
+        mats.append(material_row(rng.uniform(0.1, 0.9, 3), rng.uniform(0.05, 1.0),
+                                 1.0 if rng.random() < 0.3 else 0.0, alpha=0.1 if transmissive else 1.0))
+    per_mesh = [[] for _ in base]
+    for i in range(instances):
+        k = int(rng.integers(len(base)))
+        axis = rng.uniform(-1, 1, 3)
+        axis /= max(np.linalg.norm(axis), 1e-9)
+        ang = rng.uniform(1e-5, 2 * math.pi)
+        x, y, z = axis
+        c, s_, C = math.cos(ang), math.sin(ang), 1 - math.cos(ang)
+        R = np.array([[c + x * x * C, x * y * C - z * s_, x * z * C + y * s_],
+                      [y * x * C + z * s_, c + y * y * C, y * z * C - x * s_],
+                      [z * x * C - y * s_, z * y * C + x * s_, c + z * z * C]])
+        sc = rng.uniform(0.3, 2.5)
+        M = np.eye(4)
+        M[:3, :3] = R * sc
+        M[:3, 3] = (rng.uniform(-120, 120), rng.uniform(0, 25), rng.uniform(-120, 120))
+        per_mesh[k].append(M)
+    meshes = [(m, mat, ms) for m, mat, ms in zip(base, mats, per_mesh) if ms]
+    for e in range(emitters):
+        cx, cy, cz = rng.uniform(-110, 110), rng.uniform(30, 45), rng.uniform(-110, 110)
+        size = rng.uniform(1.0, 4.0)
+        tri = triangle((cx - size, cy, cz - size * 0.5), (cx, cy, cz + size), (cx + size, cy, cz - size * 0.5))
+        strength = float(math.exp(rng.uniform(0.0, math.log(100.0))))
+        meshes.append((tri, material_row((0, 0, 0), 1.0, 0.0, strength), [np.eye(4)]))
+    raw = assemble_raw(meshes, (0.25, 0.3, 0.45))
+    eye, target = np.array([0.0, 60.0, -170.0]), np.array([0.0, 5.0, 0.0])
+    cam = {"position": tuple(-eye), "lookdir": tuple(eye - target), "fov_degrees": 50.0}
+    return raw, cam

@@ -205,3 +205,33 @@ def test_camera_sweep_progressive(ctx, small):
     other.samples = 2
     ctx.render(other)
     assert np.array_equal(a.view(np.uint32), ctx.read_image().view(np.uint32))
+
+
+@pytest.fixture(scope="module")
+def heavy():
+    raw, cam = scenes.heavy_scene()
+    hs = P.HostScene.from_raw(raw, cam)
+    return hs, hs.pack()
+
+
+def test_heavy_scene_bitexact(ctx, heavy, kernel):
+    """The heavy configuration (~2M unique triangles in 64 BLASes, 10k
+    instances, transmissive materials, 256 emitters, 12 bounces, Russian
+    roulette from segment 4) equals the oracle bit for bit at low resolution."""
+    hs, view = heavy
+    params = hs.render_params(96, 54, 2, 12, rr_start=4, kernel=kernel)
+    gpu, ref, st, ost = _render_both(ctx, view, params)
+    _assert_bitexact(gpu, ref)
+    assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
+
+
+def test_heavy_scene_full_hd_throughput(ctx, heavy):
+    hs, view = heavy
+    ctx.upload(view)
+    info = ctx.build_accel()
+    params = hs.render_params(1920, 1080, 4, 12, rr_start=4)
+    ctx.render(params)
+    st = ctx.render(params)
+    assert st.error_word == 0 and st.paths == 1920 * 1080 * 4
+    print(f"heavy scene 1920x1080 4 spp: {st.segments / st.milliseconds / 1e3:.0f} Mpath-segs/s, "
+          f"BVH build {info.build_ms:.1f} ms")
