@@ -75,6 +75,7 @@ def lib():
         L.or_scene_create.restype = C.c_void_p
         L.or_scene_create.argtypes = [C.POINTER(abi.SceneView), C.c_int]
         L.or_scene_destroy.argtypes = [C.c_void_p]
+        L.or_texture_sample.argtypes = [C.c_void_p, C.c_uint32, C.c_float, C.c_float, C.POINTER(C.c_float)]
         L.or_render.restype = C.c_int
         L.or_render.argtypes = [C.c_void_p, C.POINTER(abi.RenderParams), C.c_uint32, C.c_uint32, C.POINTER(C.c_float),
                                 C.POINTER(C.c_double), C.POINTER(OrStats), C.c_int]
@@ -152,6 +153,11 @@ class OracleScene:
         if rc != 0:
             raise RuntimeError("oracle render failed")
         return rgba, st
+
+    def texture_sample(self, index: int, u: float, v: float) -> np.ndarray:
+        out = np.zeros(4, np.float32)
+        lib().or_texture_sample(self._h, index, u, v, fptr(out))
+        return out
 
     def path_signature(self, params, px: int, py: int, sample_index: int, cap: int = 64):
         out = (C.c_uint64 * cap)()

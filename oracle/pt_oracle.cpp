@@ -726,6 +726,9 @@ struct or_scene {
     uint32_t light_count = 0;
     V3 env{0, 0, 0};
     bool brute = false;
+    std::vector<uint8_t> texels;
+    std::vector<pt_texture> textures;
+    float srgb[256]; // sRGB decode of 8-bit values, FP64 curve rounded once
     std::vector<Bvh> blas;
     Bvh tlas;
 
@@ -748,7 +751,86 @@ struct or_scene {
             return {0.0f, 0.0f, 0.0f};
         return position((uint32_t)i);
     }
+    V2 uv_robust(uint64_t i) const
+    {
+        if (i >= vertices.size() / PT_VERTEX_FLOATS)
+            return {0.0f, 0.0f};
+        const float* v = &vertices[(size_t)i * PT_VERTEX_FLOATS];
+        return {v[6], v[7]};
+    }
 };
+
+namespace {
+
+// Texture sampling (material.hlsli SampleLevel(uv, 0) with the sampler of
+// src/graphics/sampler.cpp:8-22: linear, REPEAT, level 0) in the library's
+// stated arithmetic: uv wrapped to [0, 1), texel centres at (i + 0.5) / size,
+// neighbours wrapped, weights (1-a)(1-b), a(1-b), (1-a)b, ab summed in that
+// order.  Texels decode as UNORM (/255) or, for sRGB textures, through the
+// FP64 sRGB curve rounded once; 1- and 2-channel textures read (r, 0, 0, 1)
+// and (r, g, 0, 1).  Out-of-range texture indices read zero.
+struct F4 {
+    float x, y, z, w;
+};
+
+F4 texel(const or_scene& s, const pt_texture& t, uint32_t x, uint32_t y)
+{
+    const uint8_t* p = s.texels.data() + t.offset + ((size_t)y * t.width + x) * t.channels;
+    if (t.channels == 4) {
+        if (t.srgb)
+            return {s.srgb[p[0]], s.srgb[p[1]], s.srgb[p[2]], (float)p[3] / 255.0f};
+        return {(float)p[0] / 255.0f, (float)p[1] / 255.0f, (float)p[2] / 255.0f, (float)p[3] / 255.0f};
+    }
+    if (t.channels == 2)
+        return {(float)p[0] / 255.0f, (float)p[1] / 255.0f, 0.0f, 1.0f};
+    return {(float)p[0] / 255.0f, 0.0f, 0.0f, 1.0f};
+}
+
+F4 sample_texture(const or_scene& s, uint32_t index, V2 uv)
+{
+    if (index >= s.textures.size())
+        return {0.0f, 0.0f, 0.0f, 0.0f};
+    const pt_texture& t = s.textures[index];
+    float u = uv.x - std::floor(uv.x), v = uv.y - std::floor(uv.y);
+    if (!(u >= 0.0f && u < 1.0f))
+        u = 0.0f;
+    if (!(v >= 0.0f && v < 1.0f))
+        v = 0.0f;
+    const float x = u * (float)t.width - 0.5f, y = v * (float)t.height - 0.5f;
+    const float fx = std::floor(x), fy = std::floor(y);
+    const float a = x - fx, b = y - fy;
+    int x0 = (int)fx, y0 = (int)fy;
+    if (x0 < 0)
+        x0 += (int)t.width;
+    if (y0 < 0)
+        y0 += (int)t.height;
+    if (x0 >= (int)t.width)
+        x0 = (int)t.width - 1;
+    if (y0 >= (int)t.height)
+        y0 = (int)t.height - 1;
+    const uint32_t x1 = (uint32_t)x0 + 1 == t.width ? 0u : (uint32_t)x0 + 1;
+    const uint32_t y1 = (uint32_t)y0 + 1 == t.height ? 0u : (uint32_t)y0 + 1;
+    const F4 t00 = texel(s, t, x0, y0), t10 = texel(s, t, x1, y0), t01 = texel(s, t, x0, y1), t11 = texel(s, t, x1, y1);
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    return {((w00 * t00.x + w10 * t10.x) + w01 * t01.x) + w11 * t11.x, ((w00 * t00.y + w10 * t10.y) + w01 * t01.y) + w11 * t11.y,
+            ((w00 * t00.z + w10 * t10.z) + w01 * t01.z) + w11 * t11.z, ((w00 * t00.w + w10 * t10.w) + w01 * t01.w) + w11 * t11.w};
+}
+
+inline uint32_t map_bits_of(const pt_material& m)
+{
+    uint32_t b;
+    std::memcpy(&b, &m.rough_metal_normal_map_bits[3], 4);
+    return b;
+}
+
+inline uint32_t index_of(float f)
+{
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    return b;
+}
+
+} // namespace
 
 namespace {
 
@@ -872,7 +954,22 @@ Hit closest_hit(const or_scene& s, V3 o, V3 d, float tmin, float tmax, Stats& st
     return h;
 }
 
-inline float material_alpha(const or_scene& s, uint32_t inst) { return s.materials[s.instances[inst].data.material_index].base_colour[3]; }
+// shadowray.ah.hlsl:29-34: the base colour's alpha at the hit (a map is
+// sampled at the hit's texture coordinate).
+inline float material_alpha(const or_scene& s, uint32_t inst, uint32_t prim, float b1, float b2)
+{
+    const pt_instance_data& id = s.instances[inst].data;
+    const pt_material& m = s.materials[id.material_index];
+    if (!(map_bits_of(m) & PT_BASE_COLOUR_MAP_BIT))
+        return m.base_colour[3];
+    const uint32_t* ix = &s.indices[(size_t)id.index_index + (size_t)prim * 3];
+    const V2 ua = s.uv_robust((uint64_t)id.vertex_index + ix[0]);
+    const V2 ub = s.uv_robust((uint64_t)id.vertex_index + ix[1]);
+    const V2 uc = s.uv_robust((uint64_t)id.vertex_index + ix[2]);
+    const float ba = (1.0f - b1) - b2;
+    const V2 uv = {(ba * ua.x + b1 * ub.x) + b2 * uc.x, (ba * ua.y + b1 * ub.y) + b2 * uc.y};
+    return sample_texture(s, index_of(m.base_colour[0]), uv).w;
+}
 
 // Shadow ray (shadowray.ah.hlsl / shadowray.ms.hlsl): any opaque hit in
 // [tmin, tmax] occludes; transparent instances attenuate by (1 - alpha).
@@ -897,7 +994,7 @@ float shadow_visibility(const or_scene& s, V3 o, V3 d, float tmin, float tmax, S
                     occluded = true;
                     return true;
                 }
-                throughput *= (1.0f - material_alpha(s, ii));
+                throughput *= (1.0f - material_alpha(s, ii, prim, b1, b2));
                 if (throughput < 1e-5f) {
                     occluded = true;
                     return true;
@@ -996,7 +1093,62 @@ inline float light_pdf(const or_scene& s, uint32_t emitter_index, uint32_t primi
     return p;
 }
 
-inline V3 material_emission(const pt_material& m) { return v3(m.emission[0], m.emission[1], m.emission[2]) * m.emission[3]; }
+// get_emission / get_base_colour / get_roughness_metalness_normal /
+// get_specular / get_sheen (material.hlsli:23-88)
+inline V3 material_emission(const or_scene& s, const pt_material& m, V2 uv)
+{
+    if (map_bits_of(m) & PT_EMISSION_MAP_BIT) {
+        F4 t = sample_texture(s, index_of(m.emission[0]), uv);
+        return v3(t.x, t.y, t.z) * m.emission[3];
+    }
+    return v3(m.emission[0], m.emission[1], m.emission[2]) * m.emission[3];
+}
+
+inline F4 material_base_colour(const or_scene& s, const pt_material& m, V2 uv)
+{
+    if (map_bits_of(m) & PT_BASE_COLOUR_MAP_BIT)
+        return sample_texture(s, index_of(m.base_colour[0]), uv);
+    return {m.base_colour[0], m.base_colour[1], m.base_colour[2], m.base_colour[3]};
+}
+
+void material_rough_metal_normal(const or_scene& s, const pt_material& m, V2 uv, float& roughness, float& metalness, V3& normal)
+{
+    const float* rmn = m.rough_metal_normal_map_bits;
+    const uint32_t bits = map_bits_of(m);
+    if (bits & PT_ROUGHNESS_METALNESS_MAP_BIT) {
+        F4 t = sample_texture(s, index_of(rmn[0]), uv);
+        roughness = t.y;
+        metalness = t.z;
+    } else {
+        roughness = (bits & PT_ROUGHNESS_MAP_BIT) ? sample_texture(s, index_of(rmn[0]), uv).x : rmn[0];
+        metalness = (bits & PT_METALNESS_MAP_BIT) ? sample_texture(s, index_of(rmn[1]), uv).x : rmn[1];
+    }
+    if (bits & PT_NORMAL_MAP_BIT) {
+        F4 t = sample_texture(s, index_of(rmn[2]), uv);
+        normal = normalize(v3(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f));
+    } else {
+        normal = v3(0.0f, 0.0f, 1.0f);
+    }
+}
+
+inline V3 material_rgb(const or_scene& s, const float* field, bool mapped, V2 uv)
+{
+    if (mapped) {
+        F4 t = sample_texture(s, index_of(field[0]), uv);
+        return v3(t.x, t.y, t.z);
+    }
+    return v3(field[0], field[1], field[2]);
+}
+
+// onb (util.hlsli:57-64)
+inline void onb(V3 n, V3& x, V3& y)
+{
+    const float sg = n.z < 0.0f ? -1.0f : 1.0f;
+    const float a = -1.0f / (sg + n.z);
+    const float b = (n.x * n.y) * a;
+    x = v3(1.0f + ((sg * n.x) * n.x) * a, sg * b, -sg * n.x);
+    y = v3(b, sg + (n.y * n.y) * a, -n.y);
+}
 
 V3 sample_light(const or_scene& s, Sampler& smp, V3 pt, V3& light_dir, float& light_dist, float& pdf, bool& is_delta)
 {
@@ -1025,6 +1177,9 @@ V3 sample_light(const or_scene& s, Sampler& smp, V3 pt, V3& light_dir, float& li
         V3 pc = mul_point(id.transform, s.position_robust((uint64_t)id.vertex_index + s.lw(bin_offset + 2)));
         V3 bary = random_barycentric(u12);
         V3 point = (bary.x * pa + bary.y * pb) + bary.z * pc;
+        const uint64_t ia = (uint64_t)id.vertex_index + s.lw(bin_offset + 0);
+        const uint64_t ib = (uint64_t)id.vertex_index + s.lw(bin_offset + 1);
+        const uint64_t ic = (uint64_t)id.vertex_index + s.lw(bin_offset + 2);
         light_dir = point - pt;
         light_dist = 1.0f;
         V3 tn = cross(pb - pa, pc - pa);
@@ -1035,8 +1190,14 @@ V3 sample_light(const or_scene& s, Sampler& smp, V3 pt, V3& light_dir, float& li
         is_delta = false;
         if (!is_finite(pdf))
             return v3(0, 0, 0);
-        // Textured emission is outside this build (emission maps are rejected at upload).
-        return material_emission(s.materials[id.material_index]);
+        // lightsample.hlsli:106-108: emission at the point's texture coordinate
+        const pt_material& lm = s.materials[id.material_index];
+        V2 luv = {0.0f, 0.0f};
+        if (map_bits_of(lm) & PT_EMISSION_MAP_BIT) {
+            const V2 ua = s.uv_robust(ia), ub = s.uv_robust(ib), uc = s.uv_robust(ic);
+            luv = {(bary.x * ua.x + bary.y * ub.x) + bary.z * uc.x, (bary.x * ua.y + bary.y * ub.y) + bary.z * uc.y};
+        }
+        return material_emission(s, lm, luv);
     } else if (light_type == PT_LIGHT_TYPE_POINT) {
         V3 lp = v3(asfloat(s.lw(bin_offset + 1)), asfloat(s.lw(bin_offset + 2)), asfloat(s.lw(bin_offset + 3)));
         light_dir = lp - pt;
@@ -1114,9 +1275,9 @@ void shade(const or_scene& s, Payload& pl, V3 ray_o, V3 ray_d, const Hit& h, Sta
     // get_vertex_attributes (geometry.hlsli:38-47)
     float ba = (1.0f - h.b1) - h.b2;
     V3 obj_normal = normalize((ba * va.normal + h.b1 * vb.normal) + h.b2 * vc.normal);
-    // The interpolated uv only feeds texture lookups, which this build does not have.
+    const V2 uv = {(ba * va.uv.x + h.b1 * vb.uv.x) + h.b2 * vc.uv.x, (ba * va.uv.y + h.b1 * vb.uv.y) + h.b2 * vc.uv.y};
 
-    V3 emission = material_emission(mat);
+    V3 emission = material_emission(s, mat, uv);
     V3 obj_dir = v3((inst.w2o[0][0] * ray_d.x + inst.w2o[0][1] * ray_d.y) + inst.w2o[0][2] * ray_d.z,
                     (inst.w2o[1][0] * ray_d.x + inst.w2o[1][1] * ray_d.y) + inst.w2o[1][2] * ray_d.z,
                     (inst.w2o[2][0] * ray_d.x + inst.w2o[2][1] * ray_d.y) + inst.w2o[2][2] * ray_d.z);
@@ -1141,8 +1302,9 @@ void shade(const or_scene& s, Payload& pl, V3 ray_o, V3 ray_d, const Hit& h, Sta
     if (pl.final_segment)
         return;
 
-    V3 base = v3(mat.base_colour[0], mat.base_colour[1], mat.base_colour[2]);
-    float base_a = mat.base_colour[3];
+    const F4 bc = material_base_colour(s, mat, uv);
+    V3 base = v3(bc.x, bc.y, bc.z);
+    float base_a = bc.w;
     if (base_a < sample_1d(pl.smp)) {
         V3 ip = ray_o + ray_d * (h.t + ORIGIN_OFFSET);
         pl.next_origin = ip;
@@ -1151,11 +1313,13 @@ void shade(const or_scene& s, Payload& pl, V3 ray_o, V3 ray_d, const Hit& h, Sta
     }
     BrdfInput bi;
     bi.base_colour = base;
-    float roughness = mat.rough_metal_normal_map_bits[0];
-    bi.metalness = mat.rough_metal_normal_map_bits[1];
-    bi.specular = v3(mat.specular[0], mat.specular[1], mat.specular[2]);
+    float roughness;
+    V3 mapped_normal;
+    material_rough_metal_normal(s, mat, uv, roughness, bi.metalness, mapped_normal);
+    const uint32_t bits = map_bits_of(mat);
+    bi.specular = material_rgb(s, mat.specular, (bits & PT_SPECULAR_MAP_BIT) != 0, uv);
     float anisotropy = mat.cc_ccrgh_aniso[2];
-    bi.sheen = v3(mat.sheen[0], mat.sheen[1], mat.sheen[2]);
+    bi.sheen = material_rgb(s, mat.sheen, (bits & PT_SHEEN_MAP_BIT) != 0, uv);
     roughness = std::fmax(0.00001f, roughness * roughness);
     float aspect = std::sqrt(1.0f - 0.9f * std::fabs(anisotropy));
     bi.alpha = {roughness / aspect, roughness * aspect};
@@ -1188,8 +1352,18 @@ void shade(const or_scene& s, Payload& pl, V3 ray_o, V3 ray_d, const Hit& h, Sta
     V3 twn = normalize(mul3n(id.normal, true_obj_normal));
     if (dot(ray_d, twn) > 0.0f)
         twn = -twn;
-    // Normal maps are outside this build (rejected at upload), so the
-    // mapped-normal rotation of pathtrace.ch.hlsl:322-326 never applies.
+    // mapped normal (pathtrace.ch.hlsl:321-326): from_world becomes
+    // float3x3(mapped_x, mapped_y, mapped_normal) x float3x3(wx, wy, wn)
+    if (mapped_normal.z < 0.999f) {
+        V3 mx, my;
+        onb(mapped_normal, mx, my);
+        const V3 rx = (mx.x * wx + mx.y * wy) + mx.z * wn;
+        const V3 ry = (my.x * wx + my.y * wy) + my.z * wn;
+        const V3 rn = (mapped_normal.x * wx + mapped_normal.y * wy) + mapped_normal.z * wn;
+        wx = rx;
+        wy = ry;
+        wn = rn;
+    }
     V3 fw[3] = {wx, wy, wn};
     V3 nd = -ray_d;
     V3 o = normalize(v3(dot(fw[0], nd), dot(fw[1], nd), dot(fw[2], nd)));
@@ -1514,6 +1688,8 @@ struct or_packed {
     std::vector<uint32_t> light;
     uint32_t light_count = 0;
     float env[3] = {0, 0, 0};
+    std::vector<uint8_t> texels;
+    std::vector<pt_texture> textures;
 };
 
 namespace {
@@ -1522,6 +1698,83 @@ bool is_emitter(const pt_material& m)
     uint32_t bits = asuint(m.rough_metal_normal_map_bits[3]);
     return ((bits & PT_EMISSION_MAP_BIT) || std::max(std::max(m.emission[0], m.emission[1]), m.emission[2]) > 0.0f) &&
            m.emission[3] > 0.0f;
+}
+
+// Xshiro128 (xoshiro128++) and Splitmix32 of src/rng.cpp.
+struct OrXoshiro {
+    uint32_t s[4];
+    static uint32_t rotl(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }
+    uint32_t next()
+    {
+        uint32_t r = rotl(s[0] + s[3], 7) + s[0];
+        uint32_t t = s[1] << 9;
+        s[2] ^= s[0];
+        s[3] ^= s[1];
+        s[1] ^= s[2];
+        s[0] ^= s[3];
+        s[2] ^= t;
+        s[3] = rotl(s[3], 11);
+        return r;
+    }
+    // float(next()) / float(UINT32_MAX); the float divisor is 2^32
+    float next_float() { return (float)next() / 4294967296.0f; }
+};
+
+uint32_t splitmix32(uint32_t& state)
+{
+    uint32_t z = (state += 0x9e3779b9u);
+    z = (z ^ (z >> 16)) * 0x85ebca6bu;
+    z = (z ^ (z >> 13)) * 0xc2b2ae35u;
+    return z ^ (z >> 16);
+}
+
+// static_cast<uint32_t>(roundf(f)) clamped by min(., size - 1)
+// (lightsample.cpp:70-73): a negative or huge value lands on size - 1.
+uint32_t texel_coordinate(float f, uint32_t size)
+{
+    float r = std::roundf(f);
+    if (!(r >= 0.0f) || r >= 4294967296.0f)
+        return size - 1;
+    uint32_t x = (uint32_t)r;
+    return x < size - 1 ? x : size - 1;
+}
+
+// calculate_object_intensity (lightsample.cpp:41-87) for an emission-mapped
+// material: 20 barycentric samples per triangle from Xshiro128 seeded by four
+// Splitmix32(0xbd7a0d48) draws, nearest texel, channels as UNORM / 255 (no
+// sRGB decode), summed per triangle in double.  The four seed draws reach the
+// constructor in reverse order: GCC evaluates call arguments right to left.
+double emission_map_intensity(const pt_raw_scene* raw, const pt_mesh_range& m, const pt_material& mat)
+{
+    uint32_t st = 0xbd7a0d48u;
+    uint32_t d0 = splitmix32(st), d1 = splitmix32(st), d2 = splitmix32(st), d3 = splitmix32(st);
+    OrXoshiro rng{{d3, d2, d1, d0}};
+    const pt_texture& t = raw->textures[asuint(mat.emission[0])];
+    double total = 0.0;
+    for (uint32_t i = 0; i < m.tri_count; i++) {
+        const uint32_t* ix = raw->indices + m.index_offset + 3 * i;
+        const float* a = raw->vertices + (size_t)(m.vertex_offset + ix[0]) * PT_VERTEX_FLOATS;
+        const float* b = raw->vertices + (size_t)(m.vertex_offset + ix[1]) * PT_VERTEX_FLOATS;
+        const float* c = raw->vertices + (size_t)(m.vertex_offset + ix[2]) * PT_VERTEX_FLOATS;
+        double sum = 0.0;
+        for (int j = 0; j < 20; j++) {
+            float beta = 1.0f - std::sqrt(rng.next_float());
+            float gamma = (1.0f - beta) * rng.next_float();
+            float alpha = (1.0f - beta) - gamma;
+            float u = (alpha * a[6] + beta * b[6]) + gamma * c[6];
+            float v = (alpha * a[7] + beta * b[7]) + gamma * c[7];
+            float ip;
+            uint32_t x = texel_coordinate(std::modf(u, &ip) * (float)t.width, t.width);
+            uint32_t y = texel_coordinate(std::modf(v, &ip) * (float)t.height, t.height);
+            const uint8_t* px = raw->texels + t.offset + ((size_t)y * t.width + x) * t.channels;
+            float r = px[0] / 255.0f;
+            float g = t.channels >= 2 ? px[1] / 255.0f : 0.0f;
+            float bl = t.channels == 4 ? px[2] / 255.0f : 0.0f;
+            sum += (r + g) + bl;
+        }
+        total += sum;
+    }
+    return total * mat.emission[3] / (double)((size_t)m.tri_count * 20);
 }
 
 // AliasTable<T> bins as u32 words: p, q, alias, value words.
@@ -1553,6 +1806,10 @@ or_packed* or_pack(const pt_raw_scene* raw)
     P->materials.assign(raw->materials, raw->materials + raw->material_count);
     for (int k = 0; k < 3; k++)
         P->env[k] = raw->environment_colour[k];
+    if (raw->texture_count) {
+        P->texels.assign(raw->texels, raw->texels + raw->texel_bytes);
+        P->textures.assign(raw->textures, raw->textures + raw->texture_count);
+    }
 
     // scenebuffer.cpp:201-220
     uint32_t emitter_index = 0;
@@ -1625,8 +1882,10 @@ or_packed* or_pack(const pt_raw_scene* raw)
             } else {
                 table_index = it->second;
             }
-            // calculate_object_intensity for a factor-only emitter.
-            float intensity = (float)(double)(((mat.emission[0] + mat.emission[1]) + mat.emission[2]) * mat.emission[3]);
+            // calculate_object_intensity (lightsample.cpp:41-87)
+            float intensity = (asuint(mat.rough_metal_normal_map_bits[3]) & PT_EMISSION_MAP_BIT)
+                                  ? (float)emission_map_intensity(raw, raw->meshes[v], mat)
+                                  : (float)(double)(((mat.emission[0] + mat.emission[1]) + mat.emission[2]) * mat.emission[3]);
             weights.push_back(intensity);
             // table_offset stays 0: the reference accumulates the size of the
             // still-empty light table (lightsample.cpp:126).
@@ -1675,6 +1934,10 @@ void or_packed_view(const or_packed* P, pt_scene_view* v)
     v->light_count = P->light_count;
     for (int k = 0; k < 3; k++)
         v->environment_colour[k] = P->env[k];
+    v->texels = P->texels.data();
+    v->texel_bytes = P->texels.size();
+    v->textures = P->textures.data();
+    v->texture_count = (uint32_t)P->textures.size();
 }
 
 void or_packed_free(or_packed* p) { delete p; }
@@ -1691,6 +1954,14 @@ or_scene* or_scene_create(const pt_scene_view* v, int brute_force)
     s->light_count = v->light_count;
     s->env = v3(v->environment_colour[0], v->environment_colour[1], v->environment_colour[2]);
     s->brute = brute_force != 0;
+    if (v->texture_count) {
+        s->texels.assign(v->texels, v->texels + v->texel_bytes);
+        s->textures.assign(v->textures, v->textures + v->texture_count);
+    }
+    for (int i = 0; i < 256; i++) {
+        const double c = i / 255.0;
+        s->srgb[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+    }
 
     // BLAS per mesh
     s->blas.resize(v->mesh_count);
@@ -1756,6 +2027,15 @@ or_scene* or_scene_create(const pt_scene_view* v, int brute_force)
 }
 
 void or_scene_destroy(or_scene* s) { delete s; }
+
+void or_texture_sample(const or_scene* s, uint32_t index, float u, float v, float out[4])
+{
+    F4 t = sample_texture(*s, index, V2{u, v});
+    out[0] = t.x;
+    out[1] = t.y;
+    out[2] = t.z;
+    out[3] = t.w;
+}
 
 int or_max_threads(void)
 {

@@ -86,6 +86,10 @@ typedef struct or_scene or_scene;
 /* brute_force != 0: test every triangle of every instance (no BVH). */
 or_scene* or_scene_create(const pt_scene_view* view, int brute_force);
 void or_scene_destroy(or_scene* s);
+/* One texture lookup of the scene's texture `index` at (u, v): bilinear,
+ * REPEAT, level 0, sRGB decode for sRGB textures (material.hlsli
+ * SampleLevel with the sampler of src/graphics/sampler.cpp:8-22). */
+void or_texture_sample(const or_scene* s, uint32_t index, float u, float v, float out[4]);
 
 /* Render rows [row_begin, row_end) of params->samples samples starting at
  * params->sample_index.  rgba (width*height*4 floats) holds the running mean

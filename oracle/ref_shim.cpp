@@ -63,6 +63,13 @@ class SceneBuilder {
             const float* L = raw->directional_lights + 6 * i;
             s.directional_lights.push_back(DirectionalLight(Vec3(L[0], L[1], L[2]), Vec3(L[3], L[4], L[5])));
         }
+        for (uint32_t i = 0; i < raw->texture_count; i++) {
+            const pt_texture& t = raw->textures[i];
+            VkFormat f = t.channels == 4   ? (t.srgb ? VK_FORMAT_R8G8B8A8_SRGB : VK_FORMAT_R8G8B8A8_UNORM)
+                         : t.channels == 2 ? (t.srgb ? VK_FORMAT_R8G8_SRGB : VK_FORMAT_R8G8_UNORM)
+                                           : (t.srgb ? VK_FORMAT_R8_SRGB : VK_FORMAT_R8_UNORM);
+            s.textures.emplace_back(raw->texels + t.offset, (size_t)t.width * t.height * t.channels, t.width, t.height, f);
+        }
     }
 };
 

@@ -32,8 +32,16 @@ PT_KERNEL_WAVEFRONT = 2
 
 PT_VERTEX_FLOATS = 8
 PT_NO_EMITTER_INDEX = 0xFFFFFFFF
-PT_MATERIAL_IS_TRANSPARENT_BIT = 1 << 13
+PT_BASE_COLOUR_MAP_BIT = 1 << 0
 PT_EMISSION_MAP_BIT = 1 << 1
+PT_ROUGHNESS_MAP_BIT = 1 << 2
+PT_METALNESS_MAP_BIT = 1 << 3
+PT_ROUGHNESS_METALNESS_MAP_BIT = 1 << 4
+PT_SPECULAR_MAP_BIT = 1 << 5
+PT_SHEEN_MAP_BIT = 1 << 7
+PT_CLEARCOAT_MAP_BIT = 1 << 9
+PT_NORMAL_MAP_BIT = 1 << 12
+PT_MATERIAL_IS_TRANSPARENT_BIT = 1 << 13
 
 
 class MeshRange(C.Structure):

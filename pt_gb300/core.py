@@ -376,4 +376,6 @@ def view_arrays(v: abi.SceneView) -> dict:
         "light": a(v.light_words, v.light_word_count, np.uint32),
         "light_count": v.light_count,
         "env": np.array(list(v.environment_colour), np.float32),
+        "texels": a(v.texels, v.texel_bytes, np.uint8),
+        "textures": a(C.cast(v.textures, C.POINTER(C.c_uint32)), v.texture_count * 6, np.uint32),
     }

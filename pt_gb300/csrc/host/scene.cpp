@@ -1380,9 +1380,10 @@ int pt_scene_details(const pt_host_scene* s, char* buf, size_t len)
     }
     int w = std::snprintf(buf, len,
                           "Scene has:\n    %zu meshes\n    %zu materials\n    %zu point lights\n    %zu directional lights\n"
-                          "    %zu instances with emission\n    0 textures\n    %zu instances\n    %zu unique vertices\n"
+                          "    %zu instances with emission\n    %zu textures\n    %zu instances\n    %zu unique vertices\n"
                           "    %zu unique triangles\n    %zu total triangles\n",
-                          s->meshes.size(), s->materials.size(), s->point_lights.size() / 6, s->dir_lights.size() / 6, emit, inst,
+                          s->meshes.size(), s->materials.size(), s->point_lights.size() / 6, s->dir_lights.size() / 6, emit,
+                          s->textures.size(), inst,
                           uv, ut, tris);
     return w < 0 ? PT_ERR_INVALID : PT_OK;
 }

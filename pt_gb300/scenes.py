@@ -454,6 +454,110 @@ def assemble_raw(meshes, env) -> dict:
             "materials": np.array(mats, np.float32), "environment_colour": np.asarray(env, np.float32)}
 
 
+def _bits(i: int) -> np.float32:
+    return np.frombuffer(np.uint32(i).tobytes(), np.float32)[0]
+
+
+def textured_raw(seed: int = 4) -> tuple[dict, dict]:
+    """A small raw scene that reads every texture path of the shader:
+    a ground quad with an sRGB base-colour map whose alpha dips below one
+    (transparency), a combined roughness-metalness map and a normal map, with
+    texture coordinates running over [-0.7, 1.8) so that REPEAT wraps them;
+    an icosphere with 1-channel roughness, 2-channel metalness, specular and
+    sheen maps; a box with a plain material; an emissive quad whose emission
+    map makes it a textured emitter (light intensity by the reference's
+    20-sample estimate, light samples reading the map at their uv)."""
+    rng = np.random.default_rng(seed)
+    tex = []
+
+    def add(img, srgb):
+        tex.append((np.ascontiguousarray(img, np.uint8), srgb))
+        return len(tex) - 1
+
+    h, w = 48, 64
+    yy, xx = np.mgrid[0:h, 0:w]
+    check = ((xx // 8 + yy // 8) % 2).astype(np.float32)
+    base = np.zeros((h, w, 4), np.uint8)
+    base[..., 0] = 40 + 180 * check
+    base[..., 1] = 60 + 150 * (xx / (w - 1))
+    base[..., 2] = 200 - 150 * (yy / (h - 1))
+    base[..., 3] = np.where((xx // 16 + yy // 16) % 3 == 0, 96, 255)
+    t_base = add(base, True)
+    mr = rng.integers(0, 256, (32, 32, 4), dtype=np.uint8)
+    mr[..., 2] = np.where(mr[..., 2] > 200, 255, 0)
+    t_mr = add(mr, False)
+    nx = 0.35 * np.sin(np.mgrid[0:32, 0:32][1] * 0.6)
+    ny = 0.35 * np.cos(np.mgrid[0:32, 0:32][0] * 0.45)
+    nz = np.sqrt(1 - nx * nx - ny * ny)
+    nrm = np.stack([nx, ny, nz, np.ones_like(nx)], -1)
+    t_normal = add(np.round((nrm * 0.5 + 0.5) * 255), False)
+    t_rough = add(rng.integers(20, 256, (16, 24), dtype=np.uint8), False)
+    t_metal = add(rng.integers(0, 256, (8, 8, 2), dtype=np.uint8), False)
+    t_spec = add(rng.integers(0, 256, (8, 12, 4), dtype=np.uint8), False)
+    t_sheen = add(rng.integers(0, 128, (4, 4, 4), dtype=np.uint8), False)
+    em = np.zeros((16, 16, 4), np.uint8)
+    em[..., 0] = 255
+    em[..., 1] = np.linspace(40, 255, 16)[None, :]
+    em[..., 2] = np.linspace(255, 20, 16)[:, None]
+    em[..., 3] = 255
+    t_emit = add(em, True)
+
+    def mat(**kw):
+        m = material_row(kw.get("base", (0.8, 0.8, 0.8)), kw.get("rough", 0.5), kw.get("metal", 0.0),
+                         kw.get("emission", 0.0))
+        bits = 0
+        for key, bit, slot in (("base_map", 1 << 0, 0), ("emission_map", 1 << 1, 4), ("rough_map", 1 << 2, 8),
+                               ("metal_map", 1 << 3, 9), ("rm_map", 1 << 4, 8), ("spec_map", 1 << 5, 12),
+                               ("sheen_map", 1 << 7, 16), ("normal_map", 1 << 12, 10)):
+            if key in kw:
+                bits |= bit
+                m[slot] = _bits(kw[key])
+        if kw.get("transparent"):
+            bits |= 1 << 13
+        m[11] = _bits(bits)
+        return m
+
+    p, n, uv, ix = quad(6.0, 0.0, False)
+    ground = (p, n, (uv * 2.5 - 0.7).astype(np.float32), ix)
+    sp, sn, suv, six = icosphere(2)
+    boxp, boxn, boxuv, boxix = rounded_box(2, 0.1)
+    lp, ln_, luv, lix = quad(1.5, 3.0, True)
+    eye = np.eye(4, dtype=np.float32)
+    sphere_m = np.diag([0.8, 0.8, 0.8, 1]).astype(np.float32)
+    sphere_m[:3, 3] = (-0.9, 0.8, 0.2)
+    box_m = np.diag([0.6, 0.9, 0.6, 1]).astype(np.float32)
+    box_m[:3, 3] = (1.1, 0.9, -0.6)
+    raw = assemble_raw([
+        (ground, mat(base_map=t_base, rm_map=t_mr, normal_map=t_normal, transparent=True), [eye]),
+        ((sp, sn, suv, six), mat(base=(0.9, 0.5, 0.3), rough_map=t_rough, metal_map=t_metal, spec_map=t_spec,
+                                 sheen_map=t_sheen), [sphere_m]),
+        ((boxp, boxn, boxuv, boxix), mat(base=(0.3, 0.7, 0.4), rough=0.3), [box_m]),
+        ((lp, ln_, luv, lix), mat(base=(0, 0, 0), emission=6.0, emission_map=t_emit), [eye]),
+    ], (0.05, 0.07, 0.12))
+    raw["point_lights"] = np.array([[2.5, 2.0, 2.5, 3.0, 2.5, 2.0]], np.float32)
+    raw["textures"] = tex
+    # eye (0.5, 3.2, 4.5) looking at (0, 0.4, 0)
+    cam = {"position": (-0.5, -3.2, -4.5), "lookdir": (0.5, 2.8, 4.5), "fov_degrees": 55.0}
+    return raw, cam
+
+
+def png_bytes(img: np.ndarray) -> bytes:
+    """Encode an 8-bit image ([h, w] or [h, w, c], c in 1..4) as PNG
+    (filter 0 rows, one zlib stream)."""
+    import zlib
+    img = np.ascontiguousarray(img, np.uint8)
+    h, w = img.shape[:2]
+    c = 1 if img.ndim == 2 else img.shape[2]
+    ctype = {1: 0, 2: 4, 3: 2, 4: 6}[c]
+    rows = b"".join(b"\0" + img[y].tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & U32)
+
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, ctype, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(rows)) + chunk(b"IEND", b""))
+
+
 def _displaced_sphere(subdiv: int, rng: np.random.Generator):
     p, n, uv, ix = icosphere(subdiv)
     waves = rng.uniform(1, 5, (3, 3))

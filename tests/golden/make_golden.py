@@ -149,7 +149,21 @@ def light_scenes():
           "instance_matrices": np.array([M.T.reshape(-1), M2.T.reshape(-1)], np.float32), "materials": mats,
           "environment_colour": np.zeros(3, np.float32)}
     raws.append(("two_emissive_meshes", r3))
+    # an emission-mapped emitter: intensity by the reference's 20-sample estimate
+    r4, _ = scenes.textured_raw()
+    raws.append(("textured_emitter", r4))
     return raws
+
+
+def _fixture_raw(raw):
+    out = {}
+    for k, v in raw.items():
+        if k == "textures":
+            out[k] = [{"shape": list(img.shape), "srgb": bool(srgb), "data": base64.b64encode(img.tobytes()).decode()}
+                      for img, srgb in v]
+        else:
+            out[k] = np.asarray(v).tolist()
+    return out
 
 
 def light_streams(R):
@@ -160,7 +174,7 @@ def light_streams(R):
         count = C.c_uint32()
         n = R.ref_light_stream(C.byref(rs), words, 65536, C.byref(count))
         assert n >= 0
-        out.append({"name": name, "raw": {k: (np.asarray(v).tolist()) for k, v in raw.items()},
+        out.append({"name": name, "raw": _fixture_raw(raw),
                     "light_words": list(words[:n]), "light_count": count.value})
     return out
 

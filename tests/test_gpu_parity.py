@@ -90,6 +90,23 @@ def test_mid_scene_bitexact(ctx, mid, kernel):
     assert st.segments == ost.segments
 
 
+@pytest.fixture(scope="module")
+def textured():
+    raw, cam = scenes.textured_raw()
+    hs = P.HostScene.from_raw(raw, cam)
+    return hs, hs.pack()
+
+
+def test_textured_scene_bitexact(ctx, textured, kernel):
+    """Base-colour, roughness-metalness, normal, 1- and 2-channel, specular and
+    sheen maps, texture alpha in shadow rays and a textured emitter."""
+    hs, view = textured
+    params = hs.render_params(96, 72, 4, 6, kernel=kernel)
+    gpu, ref, st, ost = _render_both(ctx, view, params)
+    _assert_bitexact(gpu, ref)
+    assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
+
+
 def test_progressive_equals_single_call(ctx, small, kernel):
     """Rendering spp in several calls gives the same running mean as one call
     (the reference dispatches one sample per submission, ptdispatch.cpp:101)."""

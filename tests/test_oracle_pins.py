@@ -160,6 +160,9 @@ def test_scn_transforms_match_reference_parser():
 def _raw_from_fixture(r):
     raw = {}
     for k, v in r.items():
+        if k == "textures":
+            raw[k] = [(np.frombuffer(base64.b64decode(t["data"]), np.uint8).reshape(t["shape"]), t["srgb"]) for t in v]
+            continue
         dt = np.uint32 if k in ("indices", "meshes", "mesh_material", "mesh_instance_offset") else np.float32
         raw[k] = np.array(v, dt)
     return raw

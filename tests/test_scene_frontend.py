@@ -172,3 +172,109 @@ def test_cli_argument_errors(args, message):
 def test_cli_help():
     r = run_cli("--help")
     assert r.returncode == 0 and r.stdout.startswith("Usage: ") and "--samples, -s" in r.stdout
+
+
+def _textured_gltf(d: Path, name: str, images, textures, materials, prim_material=0):
+    """A quad glTF whose document carries the given images / textures / materials."""
+    scenes.write_gltf(d / f"{name}.gltf", scenes.quad(2.0, 0.0, False), {"base": (1, 1, 1)})
+    doc = json.loads((d / f"{name}.gltf").read_text())
+    doc["images"] = images
+    doc["textures"] = textures
+    doc["materials"] = materials
+    doc["meshes"][0]["primitives"][0]["material"] = prim_material
+    (d / f"{name}.gltf").write_text(json.dumps(doc))
+
+
+def _u32(f):
+    return int(np.float32(f).view(np.uint32))
+
+
+def test_gltf_texture_order_srgb_channels_and_transparency(tmp_path):
+    """Texture indices follow first use over the materials, in the order
+    base colour, emission, metallic-roughness, normal (process_texture,
+    scene.cpp:50-72); the first use decides sRGB; 3-channel images are stored
+    as 4; a base-colour map with alpha below one makes the material
+    transparent (scene.cpp:344-355)."""
+    rng = np.random.default_rng(3)
+    rgb = rng.integers(0, 256, (5, 7, 3), dtype=np.uint8)
+    gray = rng.integers(0, 256, (4, 4), dtype=np.uint8)
+    ga = rng.integers(0, 256, (3, 6, 2), dtype=np.uint8)
+    rgba = rng.integers(0, 256, (6, 5, 4), dtype=np.uint8)
+    rgba[..., 3] = 255
+    rgba[2, 3, 3] = 254
+    for n, img in (("rgb", rgb), ("gray", gray), ("ga", ga), ("rgba", rgba)):
+        (tmp_path / f"{n}.png").write_bytes(scenes.png_bytes(img))
+    images = [{"uri": "rgba.png"}, {"uri": "rgb.png"}, {"uri": "gray.png"}, {"uri": "ga.png"}, {"uri": "rgb.png"}]
+    textures = [{"source": i} for i in range(5)]
+    materials = [
+        {"pbrMetallicRoughness": {"baseColorTexture": {"index": 1}, "metallicRoughnessTexture": {"index": 2}},
+         "normalTexture": {"index": 4}},
+        {"pbrMetallicRoughness": {"baseColorTexture": {"index": 3}}, "emissiveTexture": {"index": 0}},
+        {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}}},
+    ]
+    _textured_gltf(tmp_path, "tq", images, textures, materials)
+    hs = P.HostScene.load(scn(tmp_path, "camera:\n\nobjects:\ntq tq.gltf\ntq\n"))
+    raw = hs.raw()
+    tex = raw["textures"]
+    # rgb.png (base of material 0) -> 0, gray.png -> 1, rgb.png again (normal, same uri) -> 0,
+    # ga.png (base of material 1) -> 2, rgba.png (emission) -> 3
+    assert len(tex) == 4
+    assert tex[0][0].shape == (5, 7, 4) and tex[0][1] is True
+    assert np.array_equal(tex[0][0][..., :3], rgb) and np.all(tex[0][0][..., 3] == 255)
+    assert tex[1][0].shape == (4, 4) and tex[1][1] is False and np.array_equal(tex[1][0], gray)
+    assert tex[2][0].shape == (3, 6, 2) and tex[2][1] is False  # sRGB only exists for 4 channels
+    assert np.array_equal(tex[3][0], rgba) and tex[3][1] is True
+    m = raw["materials"]
+    bits = [_u32(r[11]) for r in m]
+    assert bits[0] == abi.PT_BASE_COLOUR_MAP_BIT | abi.PT_ROUGHNESS_METALNESS_MAP_BIT | abi.PT_NORMAL_MAP_BIT
+    assert (_u32(m[0][0]), _u32(m[0][8]), _u32(m[0][10])) == (0, 1, 0)
+    assert bits[1] == abi.PT_BASE_COLOUR_MAP_BIT | abi.PT_EMISSION_MAP_BIT  # 2-channel map: no transparency
+    assert (_u32(m[1][0]), _u32(m[1][4])) == (2, 3)
+    assert bits[2] == abi.PT_BASE_COLOUR_MAP_BIT | abi.PT_MATERIAL_IS_TRANSPARENT_BIT and _u32(m[2][0]) == 3
+    assert "4 textures" in hs.details()
+
+
+def test_gltf_texture_offsets_across_objects(tmp_path):
+    """A second object's textures follow the first's and its map indices move
+    by the same offset, except the specular and sheen maps, whose offset lands
+    in the unused .w slot (offset_maps_by, material.cpp:16-42)."""
+    rng = np.random.default_rng(4)
+    for n in ("a", "b", "c"):
+        (tmp_path / f"{n}.png").write_bytes(scenes.png_bytes(rng.integers(0, 256, (2, 3, 4), dtype=np.uint8)))
+    _textured_gltf(tmp_path, "one", [{"uri": "a.png"}], [{"source": 0}],
+                   [{"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}}}])
+    mat = {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}},
+           "extensions": {"KHR_materials_specular": {"specularColorTexture": {"index": 1}},
+                          "KHR_materials_sheen": {"sheenColorTexture": {"index": 0}}}}
+    _textured_gltf(tmp_path, "two", [{"uri": "b.png"}, {"uri": "c.png"}], [{"source": 0}, {"source": 1}], [mat])
+    hs = P.HostScene.load(scn(tmp_path, "camera:\n\nobjects:\none one.gltf\ntwo two.gltf\none\ntwo\n"))
+    raw = hs.raw()
+    assert len(raw["textures"]) == 3
+    m = raw["materials"]
+    assert _u32(m[0][0]) == 0
+    assert _u32(m[1][0]) == 1  # base colour: local 0 + offset 1
+    assert _u32(m[1][12]) == 1 and _u32(m[1][15]) == 1  # specular: .x keeps local 1, .w gets the offset
+    assert _u32(m[1][16]) == 0 and _u32(m[1][19]) == 1  # sheen: .x keeps local 0
+
+
+def test_jpeg_textures_are_rejected(tmp_path):
+    (tmp_path / "j.jpg").write_bytes(b"\xff\xd8\xff\xe0" + bytes(64))
+    _textured_gltf(tmp_path, "j", [{"uri": "j.jpg"}], [{"source": 0}],
+                   [{"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}}}])
+    msg = load_error(scn(tmp_path, "camera:\n\nobjects:\njq j.gltf\njq\n"))
+    assert "JPEG" in msg
+
+
+def test_textured_pack_matches_oracle():
+    raw, cam = scenes.textured_raw()
+    hs = P.HostScene.from_raw(raw, cam)
+    a = P.view_arrays(hs.pack())
+    rs, keep = core.raw_to_struct(raw)
+    packed = oracle.OraclePacked(rs)
+    b = P.view_arrays(packed.view)
+    for k in a:
+        if isinstance(a[k], np.ndarray):
+            assert np.array_equal(a[k], b[k]), k
+        else:
+            assert a[k] == b[k], k
+    assert a["textures"].size == 6 * len(raw["textures"]) and a["texels"].size == sum(t.size for t, _ in raw["textures"])
