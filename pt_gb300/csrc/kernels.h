@@ -13,6 +13,9 @@ struct DevInstance;
 struct DevInstanceData;
 
 cudaError_t launch_megakernel(const RenderArgs& a, cudaStream_t stream);
+// The megakernel with a tile of tile_w x (128 / tile_w) pixels per block
+// (tile_w 8, 16 or 32).
+cudaError_t launch_megakernel_tiled(const RenderArgs& a, uint32_t tile_w, cudaStream_t stream);
 
 // Wavefront path tracer (render_wave.cu).  `state` holds wave_state_bytes(n)
 // bytes of path state for up to n_paths_max paths (a multiple of the pixel
@@ -21,6 +24,26 @@ size_t wave_state_bytes(uint32_t n_paths_max);
 cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
                              uint32_t* launches, cudaStream_t stream);
 cudaError_t wave_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
+
+// Batched wavefront: waves hold shares of several jobs (RenderArgs in device
+// memory, one per job).  A share is `samples` consecutive samples from
+// `first_sample` of all `pixels` pixels of job `job`: path ids [path_base,
+// path_base + samples * pixels) in sample-major order and accumulation
+// threads [pixel_base, pixel_base + pixels).  Shares of a wave are sorted by
+// path_base and pixel_base.
+struct WaveShare {
+    uint32_t job, path_base, pixel_base, first_sample, samples, pixels;
+};
+struct BatchWave {
+    uint32_t share_offset, share_count; // into the device share array
+    uint32_t n_paths, n_pixels;         // totals of the wave's shares
+    uint32_t max_bounces;               // largest of the wave's jobs
+};
+// `path_share` holds n_paths_max u32; `waves` is host memory (the launch
+// sequence is fixed by it, so the whole call can be captured in a graph).
+cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shares, const BatchWave* waves, uint32_t wave_count,
+                                   uint32_t* path_share, unsigned long long* counters, void* state, size_t state_bytes,
+                                   uint32_t n_paths_max, int sm_count, uint32_t* launches, cudaStream_t stream);
 cudaError_t features_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
 
 // Denoiser features and packing (features.cu).

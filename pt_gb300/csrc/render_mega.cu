@@ -22,10 +22,12 @@ __device__ __forceinline__ void shade_segment(const DevScene& s, PathState& pl, 
     finish_nee(pl.radiance, nee, vis);
 }
 
+// One block = a TW x (128 / TW) pixel tile.
+template <int TW>
 __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
 {
-    const uint32_t px = blockIdx.x * 16 + (threadIdx.x & 15);
-    const uint32_t py = blockIdx.y * 8 + (threadIdx.x >> 4);
+    const uint32_t px = blockIdx.x * TW + (threadIdx.x % TW);
+    const uint32_t py = blockIdx.y * (128 / TW) + (threadIdx.x / TW);
     uint32_t segments = 0, shadow_rays = 0, paths = 0;
     TraceCounters tc{0u, 0u};
     if (px < a.width && py < a.height) {
@@ -120,12 +122,27 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
     }
 }
 
-cudaError_t launch_megakernel(const RenderArgs& a, cudaStream_t stream)
+cudaError_t launch_megakernel_tiled(const RenderArgs& a, uint32_t tile_w, cudaStream_t stream)
 {
-    dim3 grid((a.width + 15) / 16, (a.height + 7) / 8);
-    k_megakernel<<<grid, 128, 0, stream>>>(a);
+    const uint32_t th = 128 / tile_w;
+    dim3 grid((a.width + tile_w - 1) / tile_w, (a.height + th - 1) / th);
+    switch (tile_w) {
+    case 8:
+        k_megakernel<8><<<grid, 128, 0, stream>>>(a);
+        break;
+    case 16:
+        k_megakernel<16><<<grid, 128, 0, stream>>>(a);
+        break;
+    case 32:
+        k_megakernel<32><<<grid, 128, 0, stream>>>(a);
+        break;
+    default:
+        return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
+
+cudaError_t launch_megakernel(const RenderArgs& a, cudaStream_t stream) { return launch_megakernel_tiled(a, 16, stream); }
 
 } // namespace pt
 

@@ -20,10 +20,93 @@
 // shadow stage of segment s runs before the shade stage of segment s + 1.
 // Queue lengths stay on the device; every kernel reads its own count, so the
 // host issues a fixed sequence of launches per wave (CUDA-graph friendly).
+//
+// The stages are templates over the source of a wave's paths: one render
+// (`OneJob`: path id -> sample and pixel of the call's camera) or a batch
+// (`ManyJobs`: a wave holds shares of several jobs, each with its own scene,
+// camera, size and sample range; raygen records each path's share).
 #include "device/render.cuh"
 #include "kernels.h"
 
 namespace pt {
+
+// Pixel and sample of a path, and the job it belongs to.
+struct PathLoc {
+    uint32_t job, pix, si;
+};
+
+struct OneJob {
+    RenderArgs r;
+    uint32_t first_sample; // sample index of path ids [0, W*H)
+    uint32_t samples;      // k
+    uint32_t pixels;       // W * H
+    uint32_t n_paths;      // k * W * H
+    __device__ __forceinline__ PathLoc assign(uint32_t p) const
+    {
+        uint32_t j = p / pixels;
+        return PathLoc{0u, p - j * pixels, first_sample + j};
+    }
+    __device__ __forceinline__ PathLoc locate(uint32_t p) const { return assign(p); }
+    __device__ __forceinline__ uint32_t job_of(uint32_t) const { return 0u; }
+    __device__ __forceinline__ const RenderArgs& args(uint32_t) const { return r; }
+    __device__ __forceinline__ unsigned long long* counters() const { return r.counters; }
+    __device__ __forceinline__ uint32_t accum_threads() const { return pixels; }
+    // one job's share: its args, pixel, first path id, pixels, first sample, samples
+    __device__ __forceinline__ const WaveShare share_of_pixel(uint32_t t, uint32_t& pix) const
+    {
+        pix = t;
+        return WaveShare{0u, 0u, 0u, first_sample, samples, pixels};
+    }
+};
+
+struct ManyJobs {
+    const RenderArgs* jobs;    // device table, one per job
+    const WaveShare* shares;   // this wave's shares, ascending path_base / pixel_base
+    uint32_t* path_share;      // per path: index of its share (written by raygen)
+    uint32_t share_count;
+    uint32_t n_paths;          // sum of the shares' samples * pixels
+    uint32_t n_pixels;         // sum of the shares' pixels
+    unsigned long long* ctr;   // batch counters
+    __device__ __forceinline__ PathLoc from_share(uint32_t e, uint32_t p) const
+    {
+        const WaveShare& E = shares[e];
+        uint32_t lp = p - E.path_base;
+        uint32_t j = lp / E.pixels;
+        return PathLoc{E.job, lp - j * E.pixels, E.first_sample + j};
+    }
+    __device__ __forceinline__ PathLoc assign(uint32_t p) const
+    {
+        uint32_t lo = 0, hi = share_count; // last share with path_base <= p
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (shares[mid].path_base <= p)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        path_share[p] = lo;
+        return from_share(lo, p);
+    }
+    __device__ __forceinline__ PathLoc locate(uint32_t p) const { return from_share(path_share[p], p); }
+    __device__ __forceinline__ uint32_t job_of(uint32_t p) const { return shares[path_share[p]].job; }
+    __device__ __forceinline__ const RenderArgs& args(uint32_t job) const { return jobs[job]; }
+    __device__ __forceinline__ unsigned long long* counters() const { return ctr; }
+    __device__ __forceinline__ uint32_t accum_threads() const { return n_pixels; }
+    __device__ __forceinline__ const WaveShare share_of_pixel(uint32_t t, uint32_t& pix) const
+    {
+        uint32_t lo = 0, hi = share_count;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (shares[mid].pixel_base <= t)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        const WaveShare E = shares[lo];
+        pix = t - E.pixel_base;
+        return E;
+    }
+};
 
 struct WaveState {
     // per path
@@ -48,13 +131,10 @@ struct WaveState {
     uint32_t* counts;   // [0],[1] path queues, [2] shadow queue, [3] work fetch, [4] shadow fetch
 };
 
+template <class Src>
 struct WaveArgs {
-    RenderArgs r;
+    Src src;
     WaveState w;
-    uint32_t wave_first_sample; // sample index of path ids [0, W*H)
-    uint32_t wave_samples;      // k
-    uint32_t pixels;            // W * H
-    uint32_t n_paths;           // k * W * H
 };
 
 __device__ __forceinline__ void push_warp(uint32_t* queue, uint32_t* count, bool pred, uint32_t value)
@@ -72,13 +152,14 @@ __device__ __forceinline__ void push_warp(uint32_t* queue, uint32_t* count, bool
         queue[base + __popc(mask & ((1u << lane) - 1u))] = value;
 }
 
-__global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs a)
+template <class Src>
+__global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs<Src> a)
 {
-    const RenderArgs& R = a.r;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n_paths; p += gridDim.x * blockDim.x) {
-        uint32_t j = p / a.pixels, pix = p - j * a.pixels;
-        uint32_t px = pix % R.width, py = pix / R.width;
-        uint32_t si = a.wave_first_sample + j;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.src.n_paths; p += gridDim.x * blockDim.x) {
+        const PathLoc L = a.src.assign(p);
+        const RenderArgs& R = a.src.args(L.job);
+        uint32_t px = L.pix % R.width, py = L.pix / R.width;
+        uint32_t si = L.si;
         Sampler smp;
         sampler_start(smp, px, py, si, 0);
         f2 u_pixel = sample_2d(smp);
@@ -93,7 +174,7 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs a)
         a.w.queue[0][p] = p;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.w.counts[0] = a.n_paths;
+        a.w.counts[0] = a.src.n_paths;
         a.w.counts[1] = 0;
         a.w.counts[2] = 0;
         a.w.counts[3] = 0;
@@ -102,9 +183,9 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs a)
 }
 
 // Persistent traversal: warps fetch 32 queue entries at a time.
-__global__ void __launch_bounds__(128) k_wf_extend(WaveArgs a, uint32_t qi)
+template <class Src>
+__global__ void __launch_bounds__(128) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
 {
-    const DevScene& s = a.r.s;
     const uint32_t* queue = a.w.queue[qi];
     const uint32_t count = *(volatile uint32_t*)&a.w.counts[qi];
     unsigned lane = threadIdx.x & 31;
@@ -119,6 +200,7 @@ __global__ void __launch_bounds__(128) k_wf_extend(WaveArgs a, uint32_t qi)
         uint32_t i = base + lane;
         if (i < count) {
             uint32_t p = queue[i];
+            const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
             Hit h;
             bool hit = trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
@@ -129,15 +211,14 @@ __global__ void __launch_bounds__(128) k_wf_extend(WaveArgs a, uint32_t qi)
     uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
     uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
     if (lane == 0) {
-        atomicAdd(a.r.counters + 3, (unsigned long long)nodes);
-        atomicAdd(a.r.counters + 4, (unsigned long long)tris);
+        atomicAdd(a.src.counters() + 3, (unsigned long long)nodes);
+        atomicAdd(a.src.counters() + 4, (unsigned long long)tris);
     }
 }
 
-__global__ void __launch_bounds__(128) k_wf_shade(WaveArgs a, uint32_t qi)
+template <class Src>
+__global__ void __launch_bounds__(128) k_wf_shade(WaveArgs<Src> a, uint32_t qi)
 {
-    const RenderArgs& R = a.r;
-    const DevScene& s = R.s;
     const uint32_t* qin = a.w.queue[qi];
     uint32_t* qout = a.w.queue[qi ^ 1];
     const uint32_t count = a.w.counts[qi];
@@ -151,9 +232,11 @@ __global__ void __launch_bounds__(128) k_wf_shade(WaveArgs a, uint32_t qi)
         if (active) {
             segments++;
             uint32_t sg = a.w.seg[p];
-            uint32_t j = p / a.pixels, pix = p - j * a.pixels;
-            uint32_t px = pix % R.width, py = pix / R.width;
-            uint32_t si = a.wave_first_sample + j;
+            const PathLoc L = a.src.locate(p);
+            const RenderArgs& R = a.src.args(L.job);
+            const DevScene& s = R.s;
+            uint32_t px = L.pix % R.width, py = L.pix / R.width;
+            uint32_t si = L.si;
             PathState pl;
             float4 t4 = a.w.tp[p], r4 = a.w.rad[p];
             pl.throughput = mk3(t4.x, t4.y, t4.z);
@@ -221,14 +304,14 @@ __global__ void __launch_bounds__(128) k_wf_shade(WaveArgs a, uint32_t qi)
     segments = __reduce_add_sync(0xffffffffu, segments);
     shadow_rays = __reduce_add_sync(0xffffffffu, shadow_rays);
     if ((threadIdx.x & 31) == 0 && (segments | shadow_rays)) {
-        atomicAdd(R.counters + 0, (unsigned long long)segments);
-        atomicAdd(R.counters + 1, (unsigned long long)shadow_rays);
+        atomicAdd(a.src.counters() + 0, (unsigned long long)segments);
+        atomicAdd(a.src.counters() + 1, (unsigned long long)shadow_rays);
     }
 }
 
-__global__ void __launch_bounds__(128) k_wf_shadow(WaveArgs a)
+template <class Src>
+__global__ void __launch_bounds__(128) k_wf_shadow(WaveArgs<Src> a)
 {
-    const DevScene& s = a.r.s;
     const uint32_t count = a.w.counts[2];
     unsigned lane = threadIdx.x & 31;
     TraceCounters tc{0u, 0u};
@@ -242,6 +325,7 @@ __global__ void __launch_bounds__(128) k_wf_shadow(WaveArgs a)
         uint32_t i = base + lane;
         if (i < count) {
             uint32_t p = a.w.shadow_queue[i];
+            const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.nee_o[p], d = a.w.nee_d[p];
             float vis = trace_shadow_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, o.w, tc);
             NeeRequest nee;
@@ -263,24 +347,27 @@ __global__ void __launch_bounds__(128) k_wf_shadow(WaveArgs a)
     uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
     uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
     if (lane == 0) {
-        atomicAdd(a.r.counters + 3, (unsigned long long)nodes);
-        atomicAdd(a.r.counters + 4, (unsigned long long)tris);
+        atomicAdd(a.src.counters() + 3, (unsigned long long)nodes);
+        atomicAdd(a.src.counters() + 4, (unsigned long long)tris);
     }
 }
 
 // Clears the consumed queue count and the fetch counters between stages.
-__global__ void k_wf_reset(WaveArgs a, uint32_t qi)
+__global__ void k_wf_reset(uint32_t* counts, uint32_t qi)
 {
-    a.w.counts[qi] = 0;  // the queue just consumed by shade
-    a.w.counts[2] = 0;   // shadow queue consumed
-    a.w.counts[3] = 0;
-    a.w.counts[4] = 0;
+    counts[qi] = 0; // the queue just consumed by shade
+    counts[2] = 0;  // shadow queue consumed
+    counts[3] = 0;
+    counts[4] = 0;
 }
 
-__global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs a)
+template <class Src>
+__global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs<Src> a)
 {
-    const RenderArgs& R = a.r;
-    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < a.pixels; pix += gridDim.x * blockDim.x) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < a.src.accum_threads(); t += gridDim.x * blockDim.x) {
+        uint32_t pix;
+        const WaveShare E = a.src.share_of_pixel(t, pix);
+        const RenderArgs& R = a.src.args(E.job);
         float4 acc = R.image[pix];
         double s64[3] = {0.0, 0.0, 0.0};
         if (R.sum64) {
@@ -292,18 +379,19 @@ __global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs a)
         if (R.feat_a) {
             fa = R.feat_a[pix];
             fn = R.feat_n[pix];
-            for (uint32_t j = 0; j < a.wave_samples; j++) {
-                feature_mean(fa, a.w.f_a[(size_t)j * a.pixels + pix], a.wave_first_sample + j);
-                feature_mean(fn, a.w.f_n[(size_t)j * a.pixels + pix], a.wave_first_sample + j);
+            for (uint32_t j = 0; j < E.samples; j++) {
+                const size_t q = E.path_base + (size_t)j * E.pixels + pix;
+                feature_mean(fa, a.w.f_a[q], E.first_sample + j);
+                feature_mean(fn, a.w.f_n[q], E.first_sample + j);
             }
             R.feat_a[pix] = fa;
             R.feat_n[pix] = fn;
         }
-        for (uint32_t j = 0; j < a.wave_samples; j++) {
-            float4 r4 = a.w.rad[(size_t)j * a.pixels + pix];
+        for (uint32_t j = 0; j < E.samples; j++) {
+            float4 r4 = a.w.rad[E.path_base + (size_t)j * E.pixels + pix];
             f3 r = correct_radiance(mk3(r4.x, r4.y, r4.z) * R.exposure);
-            accumulate(acc, r, a.wave_first_sample + j);
-            if (R.snapshot && a.wave_first_sample + j + 1 == R.snapshot_after)
+            accumulate(acc, r, E.first_sample + j);
+            if (R.snapshot && E.first_sample + j + 1 == R.snapshot_after)
                 R.snapshot[pix] = acc;
             s64[0] += (double)r.x;
             s64[1] += (double)r.y;
@@ -315,11 +403,11 @@ __global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs a)
             d[0] = s64[0];
             d[1] = s64[1];
             d[2] = s64[2];
-            d[3] += (double)a.wave_samples;
+            d[3] += (double)E.samples;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
-        atomicAdd(R.counters + 2, (unsigned long long)a.n_paths);
+        atomicAdd(a.src.counters() + 2, (unsigned long long)a.src.n_paths);
 }
 
 size_t wave_state_bytes(uint32_t n_paths)
@@ -334,44 +422,49 @@ static inline char* bump(char*& p, size_t bytes)
     return (char*)a;
 }
 
-cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
-                             uint32_t* launches, cudaStream_t st)
+// Carves the SoA path state for n paths out of `state`.
+static bool carve_state(WaveState& w, void* state, size_t state_bytes, size_t n)
 {
-    if (state_bytes < wave_state_bytes(n_paths_max))
-        return cudaErrorInvalidValue;
-    WaveArgs a;
-    a.r = r;
+    if (state_bytes < wave_state_bytes((uint32_t)n))
+        return false;
     char* p = (char*)state;
-    size_t n = n_paths_max;
-    a.w.ray_o = (float4*)bump(p, 16 * n);
-    a.w.ray_d = (float4*)bump(p, 16 * n);
-    a.w.tp = (float4*)bump(p, 16 * n);
-    a.w.rad = (float4*)bump(p, 16 * n);
-    a.w.seg = (uint32_t*)bump(p, 4 * n);
-    a.w.hit = (float4*)bump(p, 16 * n);
-    a.w.hit_prim = (uint32_t*)bump(p, 4 * n);
-    a.w.nee_o = (float4*)bump(p, 16 * n);
-    a.w.nee_d = (float4*)bump(p, 16 * n);
-    a.w.nee_e = (float4*)bump(p, 16 * n);
-    a.w.nee_b = (float4*)bump(p, 16 * n);
-    a.w.nee_tp = (float4*)bump(p, 16 * n);
-    a.w.f_a = (float4*)bump(p, 16 * n);
-    a.w.f_n = (float4*)bump(p, 16 * n);
-    a.w.queue[0] = (uint32_t*)bump(p, 4 * n);
-    a.w.queue[1] = (uint32_t*)bump(p, 4 * n);
-    a.w.shadow_queue = (uint32_t*)bump(p, 4 * n);
-    a.w.counts = (uint32_t*)bump(p, 64);
-    if ((size_t)(p - (char*)state) > state_bytes)
-        return cudaErrorInvalidValue;
-    a.pixels = r.width * r.height;
-    uint32_t k_max = n_paths_max / a.pixels;
-    if (k_max == 0)
-        return cudaErrorInvalidValue;
+    w.ray_o = (float4*)bump(p, 16 * n);
+    w.ray_d = (float4*)bump(p, 16 * n);
+    w.tp = (float4*)bump(p, 16 * n);
+    w.rad = (float4*)bump(p, 16 * n);
+    w.seg = (uint32_t*)bump(p, 4 * n);
+    w.hit = (float4*)bump(p, 16 * n);
+    w.hit_prim = (uint32_t*)bump(p, 4 * n);
+    w.nee_o = (float4*)bump(p, 16 * n);
+    w.nee_d = (float4*)bump(p, 16 * n);
+    w.nee_e = (float4*)bump(p, 16 * n);
+    w.nee_b = (float4*)bump(p, 16 * n);
+    w.nee_tp = (float4*)bump(p, 16 * n);
+    w.f_a = (float4*)bump(p, 16 * n);
+    w.f_n = (float4*)bump(p, 16 * n);
+    w.queue[0] = (uint32_t*)bump(p, 4 * n);
+    w.queue[1] = (uint32_t*)bump(p, 4 * n);
+    w.shadow_queue = (uint32_t*)bump(p, 4 * n);
+    w.counts = (uint32_t*)bump(p, 64);
+    return (size_t)(p - (char*)state) <= state_bytes;
+}
+
+static inline uint32_t capped_grid(uint64_t threads, uint32_t block, int sm_count)
+{
+    uint64_t g = (threads + block - 1) / block;
+    uint64_t cap = (uint64_t)sm_count * 16;
+    return (uint32_t)(g < cap ? (g == 0 ? 1 : g) : cap);
+}
+
+// One wave: raygen, (extend, shade, shadow, reset) per segment, accumulate.
+template <class Src>
+static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32_t accum_threads, int sm_count, cudaStream_t st)
+{
     // persistent traversal grids: exactly the resident blocks of every SM
     static int ext_per_sm = 0, sh_per_sm = 0;
     if (ext_per_sm == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_wf_extend, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh_per_sm, k_wf_shadow, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_wf_extend<Src>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh_per_sm, k_wf_shadow<Src>, 128, 0);
         if (ext_per_sm < 1)
             ext_per_sm = 1;
         if (sh_per_sm < 1)
@@ -380,33 +473,67 @@ cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_byte
     const int trace_blocks = sm_count * ext_per_sm;
     const int shadow_blocks = sm_count * sh_per_sm;
     uint32_t nl = 0;
+    k_wf_raygen<Src><<<capped_grid(a.src.n_paths, 256, sm_count), 256, 0, st>>>(a);
+    nl++;
+    uint32_t qi = 0;
+    const uint32_t sgrid = capped_grid(a.src.n_paths, 128, sm_count);
+    for (uint32_t sg = 0; sg <= max_bounces; sg++) {
+        k_wf_extend<Src><<<trace_blocks, 128, 0, st>>>(a, qi);
+        k_wf_shade<Src><<<sgrid, 128, 0, st>>>(a, qi);
+        k_wf_shadow<Src><<<shadow_blocks, 128, 0, st>>>(a);
+        k_wf_reset<<<1, 1, 0, st>>>(a.w.counts, qi);
+        nl += 4;
+        qi ^= 1;
+    }
+    k_wf_accumulate<Src><<<capped_grid(accum_threads, 256, sm_count), 256, 0, st>>>(a);
+    nl++;
+    return nl;
+}
+
+cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
+                             uint32_t* launches, cudaStream_t st)
+{
+    WaveArgs<OneJob> a;
+    a.src.r = r;
+    if (!carve_state(a.w, state, state_bytes, n_paths_max))
+        return cudaErrorInvalidValue;
+    a.src.pixels = r.width * r.height;
+    uint32_t k_max = n_paths_max / a.src.pixels;
+    if (k_max == 0)
+        return cudaErrorInvalidValue;
+    uint32_t nl = 0;
     for (uint32_t done = 0; done < r.samples;) {
-        a.wave_samples = r.samples - done < k_max ? r.samples - done : k_max;
-        a.wave_first_sample = r.sample_index + done;
-        a.n_paths = a.wave_samples * a.pixels;
-        uint32_t grid = (a.n_paths + 255) / 256;
-        if (grid > (uint32_t)sm_count * 16)
-            grid = sm_count * 16;
-        k_wf_raygen<<<grid, 256, 0, st>>>(a);
-        nl++;
-        uint32_t qi = 0;
-        for (uint32_t sg = 0; sg <= r.max_bounces; sg++) {
-            k_wf_extend<<<trace_blocks, 128, 0, st>>>(a, qi);
-            uint32_t sgrid = (a.n_paths + 127) / 128;
-            if (sgrid > (uint32_t)sm_count * 16)
-                sgrid = sm_count * 16;
-            k_wf_shade<<<sgrid, 128, 0, st>>>(a, qi);
-            k_wf_shadow<<<shadow_blocks, 128, 0, st>>>(a);
-            k_wf_reset<<<1, 1, 0, st>>>(a, qi);
-            nl += 4;
-            qi ^= 1;
-        }
-        uint32_t agrid = (a.pixels + 255) / 256;
-        if (agrid > (uint32_t)sm_count * 16)
-            agrid = sm_count * 16;
-        k_wf_accumulate<<<agrid, 256, 0, st>>>(a);
-        nl++;
-        done += a.wave_samples;
+        a.src.samples = r.samples - done < k_max ? r.samples - done : k_max;
+        a.src.first_sample = r.sample_index + done;
+        a.src.n_paths = a.src.samples * a.src.pixels;
+        nl += launch_wave(a, r.max_bounces, a.src.pixels, sm_count, st);
+        done += a.src.samples;
+    }
+    if (launches)
+        *launches = nl;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shares, const BatchWave* waves, uint32_t wave_count,
+                                   uint32_t* path_share, unsigned long long* counters, void* state, size_t state_bytes,
+                                   uint32_t n_paths_max, int sm_count, uint32_t* launches, cudaStream_t st)
+{
+    WaveArgs<ManyJobs> a;
+    if (!carve_state(a.w, state, state_bytes, n_paths_max))
+        return cudaErrorInvalidValue;
+    a.src.jobs = jobs;
+    a.src.path_share = path_share;
+    a.src.ctr = counters;
+    uint32_t nl = 0;
+    for (uint32_t i = 0; i < wave_count; i++) {
+        const BatchWave& bw = waves[i];
+        if (bw.n_paths > n_paths_max || bw.share_count == 0)
+            return cudaErrorInvalidValue;
+        a.src.shares = shares + bw.share_offset;
+        a.src.share_count = bw.share_count;
+        a.src.n_paths = bw.n_paths;
+        a.src.n_pixels = bw.n_pixels;
+        nl += launch_wave(a, bw.max_bounces, bw.n_pixels, sm_count, st);
     }
     if (launches)
         *launches = nl;
