@@ -289,6 +289,55 @@ int pt_mse_host(pt_ctx* ctx, const float* reference_rgba, double* mse_out);
 int pt_mse_noalloc(const float* image_rgba, const float* reference_rgba, uint32_t width, uint32_t height, double* mse_out,
                    void* stream);
 
+/* ---- Batched rendering ----------------------------------------------------
+ * Many render jobs, each with its own scene, camera, image size, sample count
+ * and bounce limit, rendered by one call.  The jobs' paths share the waves of
+ * one wavefront launch sequence (a wave holds consecutive samples of several
+ * jobs, so small jobs fill the GPU together), the sequence is captured into a
+ * CUDA graph and launched as one unit, and small jobs may instead run as
+ * megakernel launches on a parallel branch of the same graph.  An autotuner
+ * times short trial batches (every job at 1/32 of its samples, at least one)
+ * and picks the wave capacity (paths in flight), the megakernel tile and the
+ * work size below which a job runs on the megakernel; its choice is cached
+ * per batch.  Every job's image equals, bit for bit, rendering that job alone
+ * with pt_render.  The reference renders one scene per process and has no
+ * counterpart; the call exists to keep the GPU full with many small jobs. */
+typedef struct pt_batch_job {
+    const pt_ctx* scene;     /* context holding the job's scene (uploaded, acceleration structure built);
+                                same device; may be the batch context itself */
+    pt_render_params params; /* sample_index 0, flags 0; kernel PT_KERNEL_AUTO lets the tuner decide,
+                                PT_KERNEL_MEGA / PT_KERNEL_WAVEFRONT force one */
+} pt_batch_job;
+
+#define PT_BATCH_NO_TUNE 1u  /* skip the tuner: every AUTO job on the wavefront, 2^23 paths per wave */
+#define PT_BATCH_NO_GRAPH 2u /* issue the launch sequence directly instead of through a CUDA graph */
+#define PT_BATCH_RETUNE 4u   /* ignore the tuning cache */
+/* Fixes the wave capacity at 2^n paths (10 <= n <= 23) instead of tuning it. */
+#define PT_BATCH_CAPACITY_LOG2(n) ((uint32_t)(n) << 8)
+
+typedef struct pt_batch_stats {
+    uint64_t segments, shadow_rays, paths; /* over all jobs */
+    float milliseconds;       /* device time of the batch render (CUDA events around the graph launch) */
+    float tune_milliseconds;  /* host time of the tuner's trial batches (0 on a cache hit or NO_TUNE) */
+    float build_milliseconds; /* host time of planning, graph capture and instantiation (0 when reused) */
+    uint32_t waves;           /* wavefront waves */
+    uint32_t kernel_launches; /* kernels in the launch sequence */
+    uint32_t mega_jobs;       /* jobs rendered by the megakernel */
+    uint32_t wave_capacity;   /* paths per wave */
+    uint32_t tile_w;          /* megakernel tile: tile_w x (128 / tile_w) pixels */
+    uint32_t graph_reused;    /* 1: the graph of an identical earlier batch was launched again */
+    uint64_t mega_threshold;  /* AUTO jobs whose trial work, pixels x max(1, samples / 32) x (bounces + 1),
+                                 is below this ran on the megakernel */
+    uint32_t error_word;      /* device error word (0 = none) */
+    uint32_t reserved;
+} pt_batch_stats;
+
+/* Render `count` jobs; synchronous (returns when every image is final). */
+int pt_render_batch(pt_ctx* ctx, const pt_batch_job* jobs, uint32_t count, uint32_t flags, pt_batch_stats* stats_out);
+/* Copy job `job`'s image of the last pt_render_batch to host memory, as
+ * pt_read_image does (fp64 = 1 needs PT_ACCUM_FP32_FP64 for that job). */
+int pt_read_batch_image(pt_ctx* ctx, uint32_t job, void* rgba, size_t pitch_bytes, int fp64);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,6 +94,27 @@ class RenderStats(C.Structure):
                 ("error_word", C.c_uint32)]
 
 
+class BatchJob(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("params", RenderParams)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("segments", C.c_uint64), ("shadow_rays", C.c_uint64), ("paths", C.c_uint64),
+                ("milliseconds", C.c_float), ("tune_milliseconds", C.c_float), ("build_milliseconds", C.c_float),
+                ("waves", C.c_uint32), ("kernel_launches", C.c_uint32), ("mega_jobs", C.c_uint32),
+                ("wave_capacity", C.c_uint32), ("tile_w", C.c_uint32), ("graph_reused", C.c_uint32),
+                ("mega_threshold", C.c_uint64), ("error_word", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+PT_BATCH_NO_TUNE = 1
+PT_BATCH_NO_GRAPH = 2
+PT_BATCH_RETUNE = 4
+
+
+def PT_BATCH_CAPACITY_LOG2(n: int) -> int:
+    return n << 8
+
+
 class AccelInfo(C.Structure):
     _fields_ = [("blas_count", C.c_uint32), ("tlas_nodes", C.c_uint32), ("blas_nodes", C.c_uint64),
                 ("triangles", C.c_uint64), ("device_bytes", C.c_uint64), ("build_ms", C.c_float)]
@@ -135,6 +156,8 @@ SIGNATURES = [
     ("pt_tonemap", C.c_int, [C.c_void_p]),
     ("pt_mse_host", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     ("pt_mse_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("pt_render_batch", C.c_int, [C.c_void_p, C.POINTER(BatchJob), C.c_uint32, C.c_uint32, C.POINTER(BatchStats)]),
+    ("pt_read_batch_image", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t, C.c_int]),
     ("pt_scene_last_error", C.c_char_p, []),
     ("pt_scene_load", C.c_void_p, [C.c_char_p]),
     ("pt_scene_from_raw", C.c_void_p, [C.POINTER(RawScene), C.POINTER(CameraDesc)]),

@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-f
               "--expt-relaxed-constexpr"] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["api.cu", "render_mega.cu", "render_wave.cu", "bvh_build.cu", "post.cu", "noalloc.cu", "features.cu",
+CU_SOURCES = ["api.cu", "batch.cu", "render_mega.cu", "render_wave.cu", "bvh_build.cu", "post.cu", "noalloc.cu", "features.cu",
               "nn/conv.cu", "nn/conv_rows.cu", "nn/ops.cu", "nn/unet.cu", "nn/api_nn.cu"]
 # The denoiser is not on the bit-exact path: let it contract multiply-adds.
 NN_FLAGS = [f for f in NVCC_FLAGS if f != "-fmad=false"]

@@ -214,6 +214,23 @@ class Context:
         _check(lib().pt_mse_host(self._h, _ptr(ref, C.c_float), C.byref(v)), self._h)
         return v.value
 
+    def render_batch(self, jobs, flags: int = 0) -> abi.BatchStats:
+        """Render [(scene Context, RenderParams), ...] as one batch (pt_render_batch)."""
+        arr = (abi.BatchJob * len(jobs))()
+        for i, (ctx, params) in enumerate(jobs):
+            arr[i].scene = ctx._h.value
+            arr[i].params = params
+        st = abi.BatchStats()
+        _check(lib().pt_render_batch(self._h, arr, len(jobs), flags, C.byref(st)), self._h)
+        self._batch_sizes = [(p.height, p.width) for _, p in jobs]
+        return st
+
+    def read_batch_image(self, job: int, fp64: bool = False) -> np.ndarray:
+        h, w = self._batch_sizes[job]
+        out = np.empty((h, w, 4), dtype=np.float64 if fp64 else np.float32)
+        _check(lib().pt_read_batch_image(self._h, job, out.ctypes.data, out.strides[0], 1 if fp64 else 0), self._h)
+        return out
+
 
 @dataclass
 class PathTraceParameters:

@@ -17,6 +17,7 @@
 
 #include "../../include/pt_denoise.h"
 #include "../../include/pt_gpu.h"
+#include "ctx.h"
 #include "device/render.cuh"
 #include "kernels.h"
 
@@ -28,31 +29,6 @@ using namespace pt;
 
 namespace {
 
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    cudaError_t alloc(size_t count)
-    {
-        release();
-        if (count == 0)
-            count = 1;
-        cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
-        if (e != cudaSuccess) {
-            p = nullptr;
-            return e;
-        }
-        n = count;
-        return cudaSuccess;
-    }
-    void release()
-    {
-        if (p)
-            cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-};
 
 // Sobol' direction numbers for 4 dimensions: van der Corput, then the
 // primitive polynomials / initial numbers (s, a, m) = (1, 0, {1}),
@@ -109,70 +85,6 @@ void inverse4(const double m[16], double out[16])
 
 } // namespace
 
-struct pt_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    bool tables = false;
-    // scene
-    bool scene_ok = false;
-    DevBuf<float4> vertices;
-    DevBuf<uint32_t> indices;
-    DevBuf<DevInstanceData> inst_data;
-    DevBuf<DevMaterial> materials;
-    DevBuf<uint8_t> texels;
-    DevBuf<DevTexture> textures;
-    uint32_t texture_count = 0;
-    DevBuf<uint32_t> light;
-    DevBuf<uint32_t> mesh_vertex_offset, mesh_index_offset, mesh_tri_base, inst_mesh;
-    DevBuf<DevInstance> dinst;
-    uint32_t vertex_count = 0, index_count = 0, mesh_count = 0, tri_count = 0, instance_count = 0, material_count = 0;
-    uint32_t light_words = 0, light_count = 0;
-    float env[3] = {0, 0, 0};
-    std::vector<DevInstance> h_dinst;
-    // acceleration structure
-    bool accel_ok = false;
-    DevBuf<BvhNode> nodes;
-    DevBuf<TriRec> tris;
-    DevBuf<int> mesh_root;
-    int tlas_root = REF_EMPTY;
-    pt_accel_info accel{};
-    // image
-    DevBuf<float4> image;
-    DevBuf<double> sum64;
-    uint32_t width = 0, height = 0;
-    uint32_t samples_done = 0;
-    bool have_fp64 = false;
-    DevBuf<unsigned long long> counters;
-    DevBuf<uint32_t> error_word;
-    DevBuf<char> wave_state;    // wavefront path state
-    uint32_t wave_paths = 0;    // paths the wave state holds
-    int sm_count = 0;
-    pt_render_params camera{};  // pt_set_camera state
-    bool camera_set = false;
-    uint32_t next_sample = 0;
-    DevBuf<float4> feat_a, feat_n; // denoiser features: albedo + depth, normal
-    uint32_t feat_w = 0, feat_h = 0;
-    DevBuf<float4> denoised;    // last pt_denoise result
-    DevBuf<float4> half;        // pt_denoise_snapshot: mean image of the first samples
-    uint32_t half_w = 0, half_h = 0, half_spp = 0, half_epoch = 0;
-    uint32_t snapshot_armed = 0; // pt_denoise_snapshot_at: take it at this many samples (0 = off)
-    uint32_t image_epoch = 0;   // counts fresh renders (sample_index 0)
-    DevBuf<float4> mse_ref;     // reference image for pt_mse_host
-    DevBuf<double> mse_partial; // [0] result, [1..] per-block partial sums
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-
-    int fail(int code, const std::string& msg)
-    {
-        err = msg;
-        return code;
-    }
-    int cuda_fail(cudaError_t e, const char* what)
-    {
-        err = std::string(what) + ": " + cudaGetErrorString(e);
-        return e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA;
-    }
-};
 
 static thread_local std::string g_create_error;
 
@@ -346,6 +258,14 @@ void pt_destroy(pt_ctx* c)
     c->mse_ref.release();
     c->mse_partial.release();
     c->wave_state.release();
+    c->texels.release();
+    c->textures.release();
+    c->feat_a.release();
+    c->feat_n.release();
+    c->denoised.release();
+    c->half.release();
+    pt::batch_free(c->batch);
+    c->batch = nullptr;
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -379,6 +299,7 @@ int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
     cudaSetDevice(c->device);
     c->scene_ok = false;
     c->accel_ok = false;
+    c->scene_generation++;
     if ((v->vertex_count && !v->vertices) || (v->index_count && !v->indices) || (v->mesh_count && !v->meshes) ||
         (v->instance_count && (!v->instances || !v->instance_mesh)) || (v->material_count && !v->materials) ||
         (v->light_word_count && !v->light_words))
@@ -535,6 +456,7 @@ int pt_build_accel(pt_ctx* c, pt_accel_info* info)
             return c->fail(PT_ERR_DEVICE, "BVH validation: " + problem);
     }
     c->accel_ok = true;
+    c->scene_generation++;
     c->accel.blas_count = c->mesh_count;
     c->accel.tlas_nodes = c->instance_count > 1 ? c->instance_count - 1 : 0;
     c->accel.blas_nodes = c->tri_count > 1 ? c->tri_count - 1 : 0;
@@ -572,8 +494,10 @@ static int ensure_image(pt_ctx* c, uint32_t w, uint32_t h, bool fp64, bool reset
     return PT_OK;
 }
 
+} // extern "C"
+
 // Device view of the context's scene and the camera/image of `p`.
-static RenderArgs render_args(pt_ctx* c, const pt_render_params* p, bool fp64)
+RenderArgs render_args(const pt_ctx* c, const pt_render_params* p, bool fp64)
 {
     RenderArgs a{};
     a.s.vertices = c->vertices.p;
@@ -613,6 +537,8 @@ static RenderArgs render_args(pt_ctx* c, const pt_render_params* p, bool fp64)
     a.counters = c->counters.p;
     return a;
 }
+
+extern "C" {
 
 int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
 {

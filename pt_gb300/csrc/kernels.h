@@ -41,6 +41,8 @@ struct BatchWave {
 };
 // `path_share` holds n_paths_max u32; `waves` is host memory (the launch
 // sequence is fixed by it, so the whole call can be captured in a graph).
+// Occupancy queries of the batched kernels; call before capturing a batch.
+cudaError_t wave_batch_prepare();
 cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shares, const BatchWave* waves, uint32_t wave_count,
                                    uint32_t* path_share, unsigned long long* counters, void* state, size_t state_bytes,
                                    uint32_t n_paths_max, int sm_count, uint32_t* launches, cudaStream_t stream);

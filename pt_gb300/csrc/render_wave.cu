@@ -456,22 +456,34 @@ static inline uint32_t capped_grid(uint64_t threads, uint32_t block, int sm_coun
     return (uint32_t)(g < cap ? (g == 0 ? 1 : g) : cap);
 }
 
+// Resident 128-thread blocks per SM of the persistent traversal kernels
+// (queried once per source type; thread-safe initialisation).
+template <class Src>
+static int2 traversal_blocks_per_sm()
+{
+    static const int2 v = [] {
+        int e = 0, s = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e, k_wf_extend<Src>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s, k_wf_shadow<Src>, 128, 0);
+        return make_int2(e < 1 ? 1 : e, s < 1 ? 1 : s);
+    }();
+    return v;
+}
+
+cudaError_t wave_batch_prepare()
+{
+    traversal_blocks_per_sm<ManyJobs>();
+    return cudaGetLastError();
+}
+
 // One wave: raygen, (extend, shade, shadow, reset) per segment, accumulate.
 template <class Src>
 static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32_t accum_threads, int sm_count, cudaStream_t st)
 {
     // persistent traversal grids: exactly the resident blocks of every SM
-    static int ext_per_sm = 0, sh_per_sm = 0;
-    if (ext_per_sm == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, k_wf_extend<Src>, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh_per_sm, k_wf_shadow<Src>, 128, 0);
-        if (ext_per_sm < 1)
-            ext_per_sm = 1;
-        if (sh_per_sm < 1)
-            sh_per_sm = 1;
-    }
-    const int trace_blocks = sm_count * ext_per_sm;
-    const int shadow_blocks = sm_count * sh_per_sm;
+    const int2 per_sm = traversal_blocks_per_sm<Src>();
+    const int trace_blocks = sm_count * per_sm.x;
+    const int shadow_blocks = sm_count * per_sm.y;
     uint32_t nl = 0;
     k_wf_raygen<Src><<<capped_grid(a.src.n_paths, 256, sm_count), 256, 0, st>>>(a);
     nl++;

@@ -145,13 +145,15 @@ def displaced_grid(n: int, rng: SceneRng, amplitude: float = 0.08):
     nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
     p = np.stack([X, Y, Z], -1).reshape(-1, 3).astype(np.float32)
     uv = np.stack([(X + 1) / 2, (Z + 1) / 2], -1).reshape(-1, 2).astype(np.float32)
-    idx = []
-    for j in range(n):
-        for i in range(n):
-            a = j * (n + 1) + i
-            b, c, d = a + 1, a + n + 1, a + n + 2
-            idx += [(a, c, b), (b, c, d)]
-    return p, nrm.reshape(-1, 3).astype(np.float32), uv, np.array(idx, np.uint32)
+    return p, nrm.reshape(-1, 3).astype(np.float32), uv, grid_indices(n)
+
+
+def grid_indices(n: int) -> np.ndarray:
+    """Triangles of an (n+1)^2-vertex grid: per cell (row-major) (a, c, b), (b, c, d)."""
+    j, i = np.meshgrid(np.arange(n, dtype=np.uint32), np.arange(n, dtype=np.uint32), indexing="ij")
+    a = (j * (n + 1) + i).reshape(-1)
+    b, c, d = a + 1, a + n + 1, a + n + 2
+    return np.stack([np.stack([a, c, b], 1), np.stack([b, c, d], 1)], 1).reshape(-1, 3).astype(np.uint32)
 
 
 def rounded_box(k: int, radius: float):
@@ -539,6 +541,73 @@ def textured_raw(seed: int = 4) -> tuple[dict, dict]:
     # eye (0.5, 3.2, 4.5) looking at (0, 0.4, 0)
     cam = {"position": (-0.5, -3.2, -4.5), "lookdir": (0.5, 2.8, 4.5), "fov_degrees": 55.0}
     return raw, cam
+
+
+_ICOSPHERES: dict = {}
+
+
+def _icosphere_cached(subdiv: int):
+    if subdiv not in _ICOSPHERES:
+        _ICOSPHERES[subdiv] = icosphere(subdiv)
+    return _ICOSPHERES[subdiv]
+
+
+def batch_scene(seed: int, tris: int) -> tuple[dict, dict]:
+    """One job scene of the batch workload with about `tris` unique triangles:
+    a 12x12 ground quad, a displaced grid holding ~70 % of the triangles
+    (scaled 3x, at the centre), an icosphere of subdivision s (20 * 4^s
+    triangles, ~30 %) instanced 3-8 times, 1-3 emissive quads (strength
+    log-uniform [2, 40]), roughness U[0.05, 1], metallic Bernoulli(0.3), base
+    colour U[0.1, 0.9]^3, eye on a circle of radius U[5, 9] at height
+    U[1.5, 4] looking at the origin, fov U[35, 65]."""
+    rng = np.random.default_rng(seed)
+    srng = SceneRng(seed)
+
+    def mat(**kw):
+        return material_row(rng.uniform(0.1, 0.9, 3), float(rng.uniform(0.05, 1.0)), float(rng.random() < 0.3), **kw)
+
+    n = max(2, int(round(math.sqrt(0.35 * tris))))
+    sub = int(min(6, max(0, round(math.log(max(0.3 * tris, 20) / 20, 4)))))
+    grid = displaced_grid(n, srng, amplitude=0.12)
+    gm = np.diag([3.0, 3.0, 3.0, 1.0]).astype(np.float32)
+    meshes = [(quad(12.0, -0.4, False), mat(), [np.eye(4, dtype=np.float32)]),
+              (grid, mat(), [gm])]
+    sphere_insts = []
+    for _ in range(int(rng.integers(3, 9))):
+        m = np.diag([rng.uniform(0.3, 0.8)] * 3 + [1.0]).astype(np.float32)
+        m[:3, 3] = (rng.uniform(-4, 4), rng.uniform(0.2, 1.5), rng.uniform(-4, 4))
+        sphere_insts.append(m)
+    meshes.append((_icosphere_cached(sub), mat(), sphere_insts))
+    for _ in range(int(rng.integers(1, 4))):
+        m = np.eye(4, dtype=np.float32)
+        m[:3, 3] = (rng.uniform(-3, 3), rng.uniform(3.5, 5.5), rng.uniform(-3, 3))
+        meshes.append((quad(float(rng.uniform(0.8, 2.0)), 0.0, True),
+                       material_row((0, 0, 0), emission=float(math.exp(rng.uniform(math.log(2), math.log(40))))), [m]))
+    raw = assemble_raw(meshes, rng.uniform(0.05, 0.4, 3).astype(np.float32))
+    ang = rng.uniform(0, 2 * math.pi)
+    r = rng.uniform(5, 9)
+    eye = np.array([r * math.cos(ang), rng.uniform(1.5, 4.0), r * math.sin(ang)], np.float32)
+    cam = {"position": tuple(-eye), "lookdir": tuple(eye), "fov_degrees": float(rng.uniform(35, 65))}
+    return raw, cam
+
+
+def batch_workload(seed: int = 7, jobs: int = 64, side=(128, 1024), spp=(4, 256), tris=(1000, 500000),
+                   max_bounces: int = 8) -> list[dict]:
+    """The batch workload: `jobs` render jobs with image side log-uniform in
+    `side` (square images, side rounded to a multiple of 8), samples
+    log-uniform in `spp` (integer) and unique triangles log-uniform in `tris`,
+    each with its own scene (batch_scene).  Returns dicts with keys seed,
+    side, spp, tris, max_bounces."""
+    rng = np.random.default_rng(seed)
+
+    def logu(lo, hi):
+        return math.exp(rng.uniform(math.log(lo), math.log(hi)))
+
+    out = []
+    for j in range(jobs):
+        out.append({"seed": seed * 1000 + j, "side": int(round(logu(*side) / 8)) * 8, "spp": int(round(logu(*spp))),
+                    "tris": int(round(logu(*tris))), "max_bounces": max_bounces})
+    return out
 
 
 def png_bytes(img: np.ndarray) -> bytes:

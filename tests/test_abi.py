@@ -48,7 +48,7 @@ def test_struct_layouts_match_c():
     structs = {"pt_mesh_range": abi.MeshRange, "pt_instance_data": abi.InstanceData, "pt_material": abi.Material,
                "pt_scene_view": abi.SceneView, "pt_render_params": abi.RenderParams, "pt_render_stats": abi.RenderStats,
                "pt_accel_info": abi.AccelInfo, "pt_raw_scene": abi.RawScene, "pt_camera_desc": abi.CameraDesc,
-               "pt_texture": abi.Texture}
+               "pt_texture": abi.Texture, "pt_batch_job": abi.BatchJob, "pt_batch_stats": abi.BatchStats}
     src = '#include <stdio.h>\n#include <stddef.h>\n#include "pt_scene.h"\nint main(void){\n'
     for name in structs:
         src += f'printf("{name} %zu\\n", sizeof({name}));\n'
