@@ -73,6 +73,14 @@ def bseg_bytes(m: dict) -> float | None:
     return 128 + 332 + p * (40 + 24 + 128 + 96 + 96) + (m["n_node"] * 64 + m["n_tri"] * 36) * (1 + p)
 
 
+def extend_bytes(m: dict) -> float:
+    """Algorithmic bytes of one closest-hit ray in k_wf_extend (the dominant
+    kernel): the traversal term of B_seg for one ray, N_node * 64 + N_tri * 36,
+    plus the ray it reads (origin + direction, 32 B), the queue entry (4 B)
+    and the hit it writes (t, barycentrics, instance 16 B + primitive 4 B)."""
+    return m["n_node"] * 64 + m["n_tri"] * 36 + 32 + 4 + 20
+
+
 class ClockSampler:
     """Samples nvidia-smi clocks every 200 ms while running."""
 
@@ -324,6 +332,49 @@ def time_to_mse(ctx, hs, kernel: int, ref_spp: int) -> dict:
     return out
 
 
+def batch_bench(device_index: int, jobs: int = 64, side=(128, 1024), spp=(4, 256), tris=(1000, 500000)) -> dict:
+    """The batch workload (scenes.batch_workload: `jobs` jobs, own scene each,
+    square side, samples and unique triangles log-uniform in the given
+    ranges, 8 bounces) rendered by pt_render_batch (tuned, CUDA graph) and,
+    for comparison, job after job with pt_render (wavefront).  The tuner's
+    trials and the graph capture run in a first, untimed call; the timed
+    batch is the graph launch of a second call (device time)."""
+    import pt_gb300 as P
+    from pt_gb300 import scenes
+
+    spec = scenes.batch_workload(jobs=jobs, side=side, spp=spp, tris=tris)
+    ctx = P.Context(device_index)
+    keep, js = [], []
+    for j in spec:
+        raw, cam = scenes.batch_scene(j["seed"], j["tris"])
+        hs = P.HostScene.from_raw(raw, cam)
+        v = hs.pack()
+        c = P.Context(device_index)
+        c.upload(v)
+        c.build_accel()
+        keep.append((hs, v))
+        js.append((c, hs.render_params(j["side"], j["side"], j["spp"], j["max_bounces"])))
+    first = ctx.render_batch(js)
+    st = ctx.render_batch(js)
+    seq_ms, seq_segs = 0.0, 0
+    for c, p in js:
+        s1 = c.render(p)
+        seq_ms += s1.milliseconds
+        seq_segs += s1.segments
+    out = {"jobs": jobs, "side": list(side), "spp": list(spp), "tris": list(tris),
+           "paths": int(st.paths), "segments": int(st.segments),
+           "batch_ms": st.milliseconds, "batch_mseg_s": st.segments / st.milliseconds / 1e3,
+           "sequential_ms": seq_ms, "sequential_mseg_s": seq_segs / seq_ms / 1e3,
+           "speedup_vs_sequential": seq_ms / st.milliseconds,
+           "tune_ms": first.tune_milliseconds, "capture_ms": first.build_milliseconds, "graph_reused": int(st.graph_reused),
+           "waves": st.waves, "graph_launches": st.kernel_launches, "wave_capacity": st.wave_capacity,
+           "mega_jobs": st.mega_jobs, "mega_threshold": int(st.mega_threshold), "tile_w": st.tile_w}
+    for c, _ in js:
+        c.close()
+    ctx.close()
+    return out
+
+
 def run_denoise_profile(args) -> None:
     """The denoised pipeline alone (mid scene, --denoise-profile spp), three
     times after a warm-up: the command profiled for the denoiser's launch list."""
@@ -395,8 +446,10 @@ def run_ours(args) -> None:
     info = ctx.build_accel()
     first = rank * SPP
 
-    def params(n=SPP, start=first):
-        return hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=start, kernel=args.kernel)
+    def params(n=SPP, start=first, flags=0):
+        p = hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=start, kernel=args.kernel)
+        p.flags = flags
+        return p
 
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device_index}")
 
@@ -413,6 +466,8 @@ def run_ours(args) -> None:
 
     # ---- device-resident timing
     dev_ms = []
+    stage_ms = [0.0] * 6
+    stage_launches = 0
     if dist:
         tdist.barrier()
     torch.cuda.synchronize()
@@ -420,10 +475,12 @@ def run_ours(args) -> None:
     with ClockSampler(device_index) as clocks:
         for _ in range(args.steps):
             l2_flush()
-            s = ctx.render(params())
+            s = ctx.render(params(flags=abi.PT_RENDER_TIME_STAGES))
             if s.segments != segs_per_step:
                 raise RuntimeError("segment count changed between identical renders")
             dev_ms.append(s.milliseconds)
+            stage_ms = [a + b for a, b in zip(stage_ms, s.stage_ms)]
+            stage_launches += s.stage_launches
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     t_dev = sum(dev_ms) / 1000.0
@@ -463,25 +520,43 @@ def run_ours(args) -> None:
 
     if rank == 0:
         peaks = measured_peaks()
+        peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks["source"] == "measured" else "fallback"
         b = bseg_bytes(BSEG["mid"])
-        achieved = (b * segs_per_step / (t_dev / args.steps) / 1e9) if b else None
-        # DRAM bytes of a render step: ncu's dram__bytes (read + write) of every
-        # render kernel of a smaller capture of the same scene, per path segment,
-        # times this step's segments (profiles/traffic.json says which capture)
+        step_achieved = b * segs_per_step / (t_dev / args.steps) / 1e9
+        # The dominant kernel is k_wf_extend (closest-hit traversal): its
+        # launches are timed by CUDA events recorded between the wavefront's
+        # launches on the render stream (PT_RENDER_TIME_STAGES) over the timed
+        # steps.  One launch traces the queued rays of one segment of a wave.
+        ext_b = extend_bytes(BSEG["mid"])
+        ext_s = stage_ms[1] / 1000.0
+        ext_launches = max(1, stage_launches)
+        rays_per_launch = segs_per_step * args.steps / ext_launches
+        ext_achieved = ext_b * segs_per_step * args.steps / ext_s / 1e9 if ext_s > 0 else None
+        # DRAM bytes per extend launch: ncu's dram__bytes_read.sum +
+        # dram__bytes_write.sum of k_wf_extend per traced ray on a smaller
+        # capture of the same scene (profiles/traffic.json), times the rays of
+        # an average launch here.
         traffic = None
         tfile = ROOT / "profiles" / "traffic.json"
         if tfile.exists():
-            per_seg = json.loads(tfile.read_text()).get("mid_wavefront", {}).get("dram_bytes_per_segment")
-            if per_seg:
-                traffic = per_seg * segs_per_step
-        roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": traffic,
-                "traffic_unit": "bytes per step (all render kernels)", "algorithmic_bytes": b * segs_per_step if b else None,
-                "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)" if peaks["source"] == "measured" else "fallback",
-                "bytes_per_segment": b}
+            per_ray = json.loads(tfile.read_text()).get("mid_wavefront", {}).get("extend_dram_bytes_per_ray")
+            if per_ray:
+                traffic = per_ray * rays_per_launch
+        roof = {"bound": "hbm", "kernel": "k_wf_extend", "achieved": ext_achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": (ext_achieved / peaks["hbm_gbs"]) if ext_achieved else None, "traffic": traffic,
+                "algorithmic_bytes": ext_b * rays_per_launch, "bytes_per_ray": ext_b,
+                "launches": stage_launches, "avg_launch_ms": stage_ms[1] / ext_launches, "rays_per_launch": rays_per_launch,
+                "peak_source": peak_src,
+                "stage_ms_per_step": {k: v / args.steps for k, v in zip(abi.STAGES, stage_ms)},
+                "step": {"achieved": step_achieved, "frac": step_achieved / peaks["hbm_gbs"], "bytes_per_segment": b,
+                         "note": "whole render step: B_seg x segments / step time"}}
         base = cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES), seconds_target=float(args.cpu_seconds)) \
             if not args.no_cpu else None
         ttm = time_to_mse(ctx, hs, args.kernel, args.ref_spp) if not args.no_mse else None
+        batches = None
+        if not args.no_batch:
+            batches = {"uneven_64": batch_bench(device_index),
+                       "small_64": batch_bench(device_index, side=(128, 256), spp=(4, 16), tris=(1000, 50000))}
         line = {"metric": METRIC, "value": value, "unit": "Mpath-segs/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -497,7 +572,7 @@ def run_ours(args) -> None:
                         "d2h_bytes_per_step": int(HEIGHT * WIDTH * 16), "ms_per_step": 1000.0 * t_e2e / args.steps,
                         "includes": "scene upload + BVH build + render + image read-back"},
                 "gpu_launches": int(launches_per_step * args.steps),
-                "roofline": roof, "cpu_baseline": base, "clocks": clocks.summary(), "time_to_mse": ttm,
+                "roofline": roof, "cpu_baseline": base, "clocks": clocks.summary(), "time_to_mse": ttm, "batch": batches,
                 "wall_s_timed_region": wall}
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -517,6 +592,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mse", action="store_true", help="skip the time-to-MSE measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering measurement")
     ap.add_argument("--ref-spp", type=int, default=REF_SPP)
     ap.add_argument("--denoise-profile", type=int, default=0, help="only run the denoised pipeline at this spp (profiling)")
     ap.add_argument("--width", type=int, default=1024, help="smaller images only for profiling captures")

@@ -182,6 +182,9 @@ typedef struct pt_render_params {
  * the camera, hit distance; zero where the camera ray escapes), as running
  * means like the image.  The rendered image is unchanged. */
 #define PT_RENDER_FEATURES 1u
+/* pt_render_params.flags: time the wavefront's stages with CUDA events
+ * recorded between its launches (pt_render_stats.stage_ms). */
+#define PT_RENDER_TIME_STAGES 2u
 
 /* Counters of the last pt_render call. */
 typedef struct pt_render_stats {
@@ -194,6 +197,12 @@ typedef struct pt_render_stats {
     uint32_t kernel_launches; /* kernels launched by the call              */
     uint32_t kernel_used;     /* PT_KERNEL_MEGA or PT_KERNEL_WAVEFRONT     */
     uint32_t error_word;      /* device error word (0 = none)              */
+    /* With PT_RENDER_TIME_STAGES (wavefront): device time of the raygen,
+     * extend (closest hit), shade, shadow (any hit), queue-reset and
+     * accumulate launches, in ms, summed over the call; `stage_launches`
+     * counts the extend launches.  Zero otherwise. */
+    float stage_ms[6];
+    uint32_t stage_launches;
 } pt_render_stats;
 
 /* Accelerating-structure summary. */

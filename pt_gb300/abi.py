@@ -90,8 +90,12 @@ class RenderParams(C.Structure):
 
 class RenderStats(C.Structure):
     _fields_ = [("segments", C.c_uint64), ("shadow_rays", C.c_uint64), ("paths", C.c_uint64),
-                ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64), ("milliseconds", C.c_float), ("kernel_launches", C.c_uint32), ("kernel_used", C.c_uint32),
-                ("error_word", C.c_uint32)]
+                ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64), ("milliseconds", C.c_float),
+                ("kernel_launches", C.c_uint32), ("kernel_used", C.c_uint32), ("error_word", C.c_uint32),
+                ("stage_ms", C.c_float * 6), ("stage_launches", C.c_uint32)]
+
+
+STAGES = ("raygen", "extend", "shade", "shadow", "reset", "accumulate")
 
 
 class BatchJob(C.Structure):
@@ -207,6 +211,7 @@ SIGNATURES = [
 
 PT_IMAGE_DENOISED = 2
 PT_RENDER_FEATURES = 1
+PT_RENDER_TIME_STAGES = 2
 PT_UNET_IN_CHANNELS = 16
 PT_UNET_OUT_CHANNELS = 16
 

@@ -266,6 +266,9 @@ void pt_destroy(pt_ctx* c)
     c->half.release();
     pt::batch_free(c->batch);
     c->batch = nullptr;
+    for (cudaEvent_t ev : c->stage_events)
+        cudaEventDestroy(ev);
+    c->stage_events.clear();
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -562,7 +565,7 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     if (p->sample_index == 0)
         c->image_epoch++;
     RenderArgs a = render_args(c, p, fp64);
-    if (p->flags & ~PT_RENDER_FEATURES)
+    if (p->flags & ~(PT_RENDER_FEATURES | PT_RENDER_TIME_STAGES))
         return c->fail(PT_ERR_INVALID, "unknown render flags");
     const bool features = (p->flags & PT_RENDER_FEATURES) != 0;
     if (features) {
@@ -590,6 +593,8 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
         a.snapshot_after = c->snapshot_armed;
     }
     cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
+    const bool timing = (p->flags & PT_RENDER_TIME_STAGES) != 0;
+    uint32_t stage_marks = 0;
     uint64_t pixels = (uint64_t)p->width * p->height;
     uint32_t kernel = p->kernel == PT_KERNEL_MEGA ? PT_KERNEL_MEGA : PT_KERNEL_WAVEFRONT;
     uint32_t launches = 0;
@@ -621,9 +626,30 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
         a.sample_index = p->sample_index;
         a.samples = p->samples;
         uint32_t n_paths = (uint32_t)(std::min<uint64_t>(c->wave_paths / pixels, p->samples) * pixels);
-        cudaError_t e = launch_wavefront(a, c->wave_state.p, c->wave_state.n, n_paths, c->sm_count, &launches, c->stream);
+        StageTimer timer;
+        if (timing) {
+            // waves x ((bounces + 1) x 4 + 2) launches, one event before each and one at the end
+            const uint64_t waves = (p->samples + n_paths / pixels - 1) / (n_paths / pixels);
+            const uint64_t need = waves * ((uint64_t)(p->max_bounces + 1) * 4 + 3);
+            if (need > (1u << 20))
+                return c->fail(PT_ERR_UNSUPPORTED, "too many launches to time by stage");
+            while (c->stage_events.size() < need) {
+                cudaEvent_t ev;
+                cudaError_t ee = cudaEventCreate(&ev);
+                if (ee != cudaSuccess)
+                    return c->cuda_fail(ee, "stage timing events");
+                c->stage_events.push_back(ev);
+            }
+            c->stage_of.resize(c->stage_events.size());
+            timer.events = c->stage_events.data();
+            timer.stage = c->stage_of.data();
+            timer.capacity = (uint32_t)c->stage_events.size();
+        }
+        cudaError_t e = launch_wavefront(a, c->wave_state.p, c->wave_state.n, n_paths, c->sm_count, &launches, c->stream,
+                                         timing ? &timer : nullptr);
         if (e != cudaSuccess)
             return c->cuda_fail(e, "wavefront launch");
+        stage_marks = timer.count;
     }
     cudaEventRecord(c->ev1, c->stream);
     c->samples_done = p->sample_index + p->samples;
@@ -658,6 +684,18 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
         stats->kernel_launches = launches;
         stats->kernel_used = kernel;
         stats->error_word = ew;
+        for (int k = 0; k < STAGE_COUNT; k++)
+            stats->stage_ms[k] = 0.0f;
+        stats->stage_launches = 0;
+        for (uint32_t i = 0; i + 1 < stage_marks; i++) {
+            const uint8_t sg = c->stage_of[i];
+            if (sg >= STAGE_COUNT)
+                continue;
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, c->stage_events[i], c->stage_events[i + 1]);
+            stats->stage_ms[sg] += t;
+            stats->stage_launches += sg == 1 ? 1u : 0u;
+        }
         if (ew != 0)
             return c->fail(PT_ERR_DEVICE, "device error word " + std::to_string(ew));
     }

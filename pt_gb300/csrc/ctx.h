@@ -104,6 +104,8 @@ struct pt_ctx {
     DevBuf<float4> mse_ref;     // reference image for pt_mse_host
     DevBuf<double> mse_partial; // [0] result, [1..] per-block partial sums
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> stage_events; // PT_RENDER_TIME_STAGES event pool
+    std::vector<uint8_t> stage_of;
     uint64_t scene_generation = 0;   // bumped by every scene upload and acceleration build
     pt::BatchState* batch = nullptr; // pt_render_batch state (images, job tables, graph, tuning cache)
 

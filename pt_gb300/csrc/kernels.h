@@ -17,12 +17,32 @@ cudaError_t launch_megakernel(const RenderArgs& a, cudaStream_t stream);
 // (tile_w 8, 16 or 32).
 cudaError_t launch_megakernel_tiled(const RenderArgs& a, uint32_t tile_w, cudaStream_t stream);
 
+// Per-stage device time of the wavefront: an event is recorded before every
+// launch and after the last one; the interval after event i belongs to
+// stage[i].  Stages: 0 raygen, 1 extend, 2 shade, 3 shadow, 4 reset,
+// 5 accumulate, 6 end marker.
+struct StageTimer {
+    cudaEvent_t* events = nullptr;
+    uint8_t* stage = nullptr;
+    uint32_t capacity = 0;
+    uint32_t count = 0;
+    void mark(cudaStream_t st, uint8_t s)
+    {
+        if (count < capacity) {
+            cudaEventRecord(events[count], st);
+            stage[count] = s;
+            count++;
+        }
+    }
+};
+constexpr int STAGE_COUNT = 6;
+
 // Wavefront path tracer (render_wave.cu).  `state` holds wave_state_bytes(n)
 // bytes of path state for up to n_paths_max paths (a multiple of the pixel
 // count); r.samples samples are rendered in waves of n_paths_max / pixels.
 size_t wave_state_bytes(uint32_t n_paths_max);
 cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
-                             uint32_t* launches, cudaStream_t stream);
+                             uint32_t* launches, cudaStream_t stream, StageTimer* timer = nullptr);
 cudaError_t wave_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
 
 // Batched wavefront: waves hold shares of several jobs (RenderArgs in device

@@ -478,32 +478,44 @@ cudaError_t wave_batch_prepare()
 
 // One wave: raygen, (extend, shade, shadow, reset) per segment, accumulate.
 template <class Src>
-static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32_t accum_threads, int sm_count, cudaStream_t st)
+static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32_t accum_threads, int sm_count, cudaStream_t st,
+                            StageTimer* tm = nullptr)
 {
+    auto mark = [&](uint8_t s) {
+        if (tm)
+            tm->mark(st, s);
+    };
     // persistent traversal grids: exactly the resident blocks of every SM
     const int2 per_sm = traversal_blocks_per_sm<Src>();
     const int trace_blocks = sm_count * per_sm.x;
     const int shadow_blocks = sm_count * per_sm.y;
     uint32_t nl = 0;
+    mark(0);
     k_wf_raygen<Src><<<capped_grid(a.src.n_paths, 256, sm_count), 256, 0, st>>>(a);
     nl++;
     uint32_t qi = 0;
     const uint32_t sgrid = capped_grid(a.src.n_paths, 128, sm_count);
     for (uint32_t sg = 0; sg <= max_bounces; sg++) {
+        mark(1);
         k_wf_extend<Src><<<trace_blocks, 128, 0, st>>>(a, qi);
+        mark(2);
         k_wf_shade<Src><<<sgrid, 128, 0, st>>>(a, qi);
+        mark(3);
         k_wf_shadow<Src><<<shadow_blocks, 128, 0, st>>>(a);
+        mark(4);
         k_wf_reset<<<1, 1, 0, st>>>(a.w.counts, qi);
         nl += 4;
         qi ^= 1;
     }
+    mark(5);
     k_wf_accumulate<Src><<<capped_grid(accum_threads, 256, sm_count), 256, 0, st>>>(a);
     nl++;
+    mark(6);
     return nl;
 }
 
 cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
-                             uint32_t* launches, cudaStream_t st)
+                             uint32_t* launches, cudaStream_t st, StageTimer* timer)
 {
     WaveArgs<OneJob> a;
     a.src.r = r;
@@ -518,7 +530,7 @@ cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_byte
         a.src.samples = r.samples - done < k_max ? r.samples - done : k_max;
         a.src.first_sample = r.sample_index + done;
         a.src.n_paths = a.src.samples * a.src.pixels;
-        nl += launch_wave(a, r.max_bounces, a.src.pixels, sm_count, st);
+        nl += launch_wave(a, r.max_bounces, a.src.pixels, sm_count, st, timer);
         done += a.src.samples;
     }
     if (launches)

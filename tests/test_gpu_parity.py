@@ -135,6 +135,22 @@ def test_fp64_accumulation_matches_oracle(ctx, small, kernel):
     assert np.array_equal(g64[..., :3], mean)
 
 
+def test_stage_timing(ctx, small):
+    """PT_RENDER_TIME_STAGES times every wavefront launch and leaves the image unchanged."""
+    hs, view = small
+    ctx.upload(view)
+    ctx.build_accel()
+    p = hs.render_params(64, 64, 4, 5, kernel=abi.PT_KERNEL_WAVEFRONT)
+    ctx.render(p)
+    a = ctx.read_image().copy()
+    p.flags = abi.PT_RENDER_TIME_STAGES
+    st = ctx.render(p)
+    assert np.array_equal(a.view(np.uint32), ctx.read_image().view(np.uint32))
+    assert st.stage_launches == 6  # one wave, segments 0..5
+    assert all(t >= 0 for t in st.stage_ms) and st.stage_ms[1] > 0
+    assert sum(st.stage_ms) <= st.milliseconds * 1.05 + 0.05
+
+
 def test_deterministic(ctx, small):
     hs, view = small
     params = hs.render_params(64, 48, 3, 8)
