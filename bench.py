@@ -157,29 +157,21 @@ def make_scene(workdir: Path):
 
 
 def cpu_baseline(view, params_fn, seconds_target: float = 15.0) -> dict:
-    """Oracle port on all host threads over a bounded sample (rows of the first spp)."""
+    """Oracle port on all host threads over a bounded sample of the workload:
+    whole frames of consecutive samples (0, 1, 2, ...) until about
+    seconds_target of wall time has been spent.  params_fn(samples, first)."""
     import oracle
     threads = os.cpu_count() or 1
     osc = oracle.OracleScene(view)
-    p = params_fn(1)
-    # bands of 32 rows taken alternately below and above the image centre
-    # until about seconds_target of CPU time has been spent
-    segs, dt, rows_done = 0, 0.0, 0
-    lo = hi = HEIGHT // 2
-    while dt < seconds_target and rows_done < HEIGHT:
-        if (rows_done // 32) % 2 == 0 and hi < HEIGHT:
-            band = (hi, min(HEIGHT, hi + 32))
-            hi = band[1]
-        else:
-            band = (max(0, lo - 32), lo)
-            lo = band[0]
+    segs, dt, n = 0, 0.0, 0
+    while dt < seconds_target:
         t0 = time.perf_counter()
-        _, st = osc.render(p, rows=band, threads=threads)
+        _, st = osc.render(params_fn(1, n), threads=threads)
         dt += time.perf_counter() - t0
         segs += st.segments
-        rows_done += band[1] - band[0]
+        n += 1
     return {"value": segs / dt / 1e6, "unit": "Mpath-segs/s", "cores": threads, "kind": "port",
-            "sample": f"mid scene, sample 0 of rows {lo}-{hi - 1} of 1024x1024 ({segs} segments, {dt:.1f} s)",
+            "sample": f"mid scene 1024x1024, samples 0-{n - 1} of 128 ({segs} segments, {dt:.1f} s)",
             "segments": int(segs), "seconds": dt}
 
 
@@ -190,12 +182,12 @@ def run_reference(args) -> None:
     with tempfile.TemporaryDirectory() as td:
         hs = make_scene(Path(td))
         view = hs.pack()
-        base = cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES), seconds_target=float(args.cpu_seconds))
+        base = cpu_baseline(view, lambda n, f: hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=f), seconds_target=float(args.cpu_seconds))
         values = []
         for _ in range(args.warmup):
-            cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES), seconds_target=2.0)
+            cpu_baseline(view, lambda n, f: hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=f), seconds_target=2.0)
         for _ in range(args.steps):
-            values.append(cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES),
+            values.append(cpu_baseline(view, lambda n, f: hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=f),
                                        seconds_target=float(args.cpu_seconds))["value"])
         v = statistics.median(values)
         line = {"metric": METRIC, "value": v, "unit": "Mpath-segs/s", "n_gpus": args.gpus, "steps": args.steps,
@@ -550,7 +542,7 @@ def run_ours(args) -> None:
                 "stage_ms_per_step": {k: v / args.steps for k, v in zip(abi.STAGES, stage_ms)},
                 "step": {"achieved": step_achieved, "frac": step_achieved / peaks["hbm_gbs"], "bytes_per_segment": b,
                          "note": "whole render step: B_seg x segments / step time"}}
-        base = cpu_baseline(view, lambda n: hs.render_params(WIDTH, HEIGHT, n, BOUNCES), seconds_target=float(args.cpu_seconds)) \
+        base = cpu_baseline(view, lambda n, f: hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=f), seconds_target=float(args.cpu_seconds)) \
             if not args.no_cpu else None
         ttm = time_to_mse(ctx, hs, args.kernel, args.ref_spp) if not args.no_mse else None
         batches = None
