@@ -185,6 +185,12 @@ typedef struct pt_render_params {
 /* pt_render_params.flags: time the wavefront's stages with CUDA events
  * recorded between its launches (pt_render_stats.stage_ms). */
 #define PT_RENDER_TIME_STAGES 2u
+/* pt_render_params.flags (with PT_RENDER_FEATURES or an armed snapshot, and
+ * for pt_render_features): store the denoiser's feature buffers and the
+ * half-sample snapshot as 4 x FP16 per pixel instead of 4 x FP32 (running
+ * means are updated in FP32 and rounded to nearest on every store).  The
+ * image itself stays FP32. */
+#define PT_RENDER_FEATURES_FP16 4u
 
 /* Counters of the last pt_render call. */
 typedef struct pt_render_stats {

@@ -4,6 +4,7 @@
 // Replaces the reference's PathTraceDispatcher / PathTracer host code
 // (src/pathtrace/ptdispatch.cpp:18-204, pathtrace.cpp:81-516) with one CUDA
 // stream per context and explicit device buffers.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -565,9 +566,10 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     if (p->sample_index == 0)
         c->image_epoch++;
     RenderArgs a = render_args(c, p, fp64);
-    if (p->flags & ~(PT_RENDER_FEATURES | PT_RENDER_TIME_STAGES))
+    if (p->flags & ~(PT_RENDER_FEATURES | PT_RENDER_TIME_STAGES | PT_RENDER_FEATURES_FP16))
         return c->fail(PT_ERR_INVALID, "unknown render flags");
     const bool features = (p->flags & PT_RENDER_FEATURES) != 0;
+    a.fp16_features = (p->flags & PT_RENDER_FEATURES_FP16) ? 1u : 0u;
     if (features) {
         const size_t px = (size_t)p->width * p->height;
         if (c->feat_a.n < px) {
@@ -657,8 +659,10 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     if (features) {
         c->feat_w = p->width;
         c->feat_h = p->height;
+        c->feat_fp16 = a.fp16_features != 0;
     }
     if (snap) {
+        c->half_fp16 = a.fp16_features != 0;
         c->half_w = p->width;
         c->half_h = p->height;
         c->half_spp = c->snapshot_armed;
@@ -803,9 +807,12 @@ int pt_render_features(pt_ctx* c, const pt_render_params* p)
         if (e != cudaSuccess)
             return c->cuda_fail(e, "feature buffers");
     }
+    if (p->flags & ~PT_RENDER_FEATURES_FP16)
+        return c->fail(PT_ERR_INVALID, "unknown flags for the feature pass");
     RenderArgs a = render_args(c, p, false);
     a.sample_index = p->sample_index;
     a.samples = p->samples;
+    a.fp16_features = (p->flags & PT_RENDER_FEATURES_FP16) ? 1u : 0u;
     cudaError_t e = launch_features(a, c->feat_a.p, c->feat_n.p, c->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
@@ -813,6 +820,7 @@ int pt_render_features(pt_ctx* c, const pt_render_params* p)
         return c->cuda_fail(e, "feature pass");
     c->feat_w = p->width;
     c->feat_h = p->height;
+    c->feat_fp16 = a.fp16_features != 0;
     return PT_OK;
 }
 
@@ -832,6 +840,7 @@ int pt_denoise_snapshot(pt_ctx* c)
     cudaError_t e = cudaMemcpyAsync(c->half.p, c->image.p, pixels * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream);
     if (e != cudaSuccess)
         return c->cuda_fail(e, "snapshot");
+    c->half_fp16 = false;
     c->half_w = c->width;
     c->half_h = c->height;
     c->half_spp = c->samples_done;
@@ -846,14 +855,30 @@ int pt_read_features(pt_ctx* c, float* albedo_depth, float* normal)
     if (!c->feat_a.p || c->feat_w == 0)
         return c->fail(PT_ERR_STATE, "no features rendered");
     cudaSetDevice(c->device);
-    const size_t bytes = (size_t)c->feat_w * c->feat_h * sizeof(float4);
+    const size_t n = (size_t)c->feat_w * c->feat_h;
     cudaError_t e = cudaSuccess;
-    if (albedo_depth)
-        e = cudaMemcpyAsync(albedo_depth, c->feat_a.p, bytes, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess && normal)
-        e = cudaMemcpyAsync(normal, c->feat_n.p, bytes, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess)
-        e = cudaStreamSynchronize(c->stream);
+    if (!c->feat_fp16) {
+        if (albedo_depth)
+            e = cudaMemcpyAsync(albedo_depth, c->feat_a.p, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess && normal)
+            e = cudaMemcpyAsync(normal, c->feat_n.p, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        return e == cudaSuccess ? PT_OK : c->cuda_fail(e, "feature read-back");
+    }
+    // FP16 storage: 4 halves per pixel, widened here
+    std::vector<__half> h(4 * n);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+        float* dst = k == 0 ? albedo_depth : normal;
+        if (!dst)
+            continue;
+        e = cudaMemcpyAsync(h.data(), k == 0 ? (const void*)c->feat_a.p : (const void*)c->feat_n.p, 4 * n * sizeof(__half),
+                            cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        for (size_t i = 0; e == cudaSuccess && i < 4 * n; i++)
+            dst[i] = __half2float(h[i]);
+    }
     return e == cudaSuccess ? PT_OK : c->cuda_fail(e, "feature read-back");
 }
 
@@ -876,7 +901,8 @@ static int denoise_input(pt_ctx* c, uint32_t spp, uint16_t* input, float* base)
     const bool have_half = c->half.p && c->half_w == c->width && c->half_h == c->height && c->half_epoch == c->image_epoch &&
                            c->half_spp < c->samples_done;
     cudaError_t e = launch_denoise_input(c->image.p, have_half ? c->half.p : nullptr, c->feat_a.p, c->feat_n.p,
-                                         c->width * c->height, spp_feature, input, base, c->stream);
+                                         c->width * c->height, spp_feature, input, base, c->feat_fp16 ? 1u : 0u,
+                                         c->half_fp16 ? 1u : 0u, c->stream);
     if (e != cudaSuccess)
         return c->cuda_fail(e, "denoiser input");
     return PT_OK;

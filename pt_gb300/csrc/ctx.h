@@ -96,6 +96,7 @@ struct pt_ctx {
     uint32_t next_sample = 0;
     DevBuf<float4> feat_a, feat_n; // denoiser features: albedo + depth, normal
     uint32_t feat_w = 0, feat_h = 0;
+    bool feat_fp16 = false, half_fp16 = false; // storage of feat_a/feat_n and of the snapshot
     DevBuf<float4> denoised;    // last pt_denoise result
     DevBuf<float4> half;        // pt_denoise_snapshot: mean image of the first samples
     uint32_t half_w = 0, half_h = 0, half_spp = 0, half_epoch = 0;

@@ -1,5 +1,7 @@
 // render.cuh — camera rays, path loop and accumulation (pathtrace.rg.hlsl:9-68).
 #pragma once
+#include <cuda_fp16.h>
+
 #include "shade.cuh"
 
 namespace pt {
@@ -16,6 +18,7 @@ struct RenderArgs {
     uint32_t snapshot_after;
     float4* feat_a;         // optional first-hit feature means: base colour + hit distance
     float4* feat_n;         //   and shading normal (PT_RENDER_FEATURES)
+    uint32_t fp16_features; // feat_a, feat_n and snapshot hold 4 x FP16 per pixel (PT_RENDER_FEATURES_FP16)
     unsigned long long* counters; // [0] segments, [1] shadow rays, [2] paths, [3] node visits, [4] triangle tests
 };
 
@@ -43,6 +46,29 @@ __device__ __forceinline__ void camera_ray(const RenderArgs& a, uint32_t px, uin
     dir = normalize(mk3(((iv[0] * rd.x + iv[1] * rd.y) + iv[2] * rd.z) + iv[3] * 0.0f,
                         ((iv[4] * rd.x + iv[5] * rd.y) + iv[6] * rd.z) + iv[7] * 0.0f,
                         ((iv[8] * rd.x + iv[9] * rd.y) + iv[10] * rd.z) + iv[11] * 0.0f));
+}
+
+// Feature and snapshot buffers: float4 per pixel, or 4 x FP16 (8 bytes) per
+// pixel when `h` is set (values rounded to nearest on store).
+__device__ __forceinline__ float4 feat_load(const float4* p, size_t i, uint32_t h)
+{
+    if (h) {
+        const __half2* q = reinterpret_cast<const __half2*>(p) + 2 * i;
+        const float2 a = __half22float2(q[0]), b = __half22float2(q[1]);
+        return make_float4(a.x, a.y, b.x, b.y);
+    }
+    return p[i];
+}
+
+__device__ __forceinline__ void feat_store(float4* p, size_t i, float4 v, uint32_t h)
+{
+    if (h) {
+        __half2* q = reinterpret_cast<__half2*>(p) + 2 * i;
+        q[0] = __floats2half2_rn(v.x, v.y);
+        q[1] = __floats2half2_rn(v.z, v.w);
+        return;
+    }
+    p[i] = v;
 }
 
 // Running mean of pathtrace.rg.hlsl:62-67 with one sample per update (the

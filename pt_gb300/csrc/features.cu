@@ -16,6 +16,7 @@ namespace {
 
 __global__ void __launch_bounds__(128) k_features(RenderArgs a, float4* feat_a, float4* feat_n)
 {
+    const uint32_t h = a.fp16_features;
     const uint32_t pixels = a.width * a.height;
     TraceCounters tc{0u, 0u};
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < pixels; pix += gridDim.x * blockDim.x) {
@@ -39,8 +40,8 @@ __global__ void __launch_bounds__(128) k_features(RenderArgs a, float4* feat_a, 
             depth += h.t;
         }
         const float inv = 1.0f / (float)a.samples;
-        feat_a[pix] = make_float4(alb.x * inv, alb.y * inv, alb.z * inv, depth * inv);
-        feat_n[pix] = make_float4(nrm.x * inv, nrm.y * inv, nrm.z * inv, 0.0f);
+        feat_store(feat_a, pix, make_float4(alb.x * inv, alb.y * inv, alb.z * inv, depth * inv), h);
+        feat_store(feat_n, pix, make_float4(nrm.x * inv, nrm.y * inv, nrm.z * inv, 0.0f), h);
     }
 }
 
@@ -58,14 +59,14 @@ __device__ __forceinline__ float slog(float x)
 }
 
 __global__ void k_denoise_input(const float4* img, const float4* half, const float4* fa, const float4* fn, uint32_t pixels,
-                                float spp_feature, uint16_t* out, float4* base)
+                                float spp_feature, uint16_t* out, float4* base, uint32_t feat_h, uint32_t half_h)
 {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < pixels; p += gridDim.x * blockDim.x) {
-        const float4 c = img[p], a = fa[p], n = fn[p];
+        const float4 c = img[p], a = feat_load(fa, p, feat_h), n = feat_load(fn, p, feat_h);
         const float r = log1pf(fmaxf(c.x, 0.0f)), g = log1pf(fmaxf(c.y, 0.0f)), b = log1pf(fmaxf(c.z, 0.0f));
         float dr = 0.0f, dg = 0.0f, db = 0.0f, have = 0.0f;
         if (half) {
-            const float4 h = half[p];
+            const float4 h = feat_load(half, p, half_h);
             dr = slog(h.x - c.x);
             dg = slog(h.y - c.y);
             db = slog(h.z - c.z);
@@ -113,10 +114,11 @@ cudaError_t launch_features(const RenderArgs& a, float4* feat_a, float4* feat_n,
 }
 
 cudaError_t launch_denoise_input(const float4* img, const float4* half, const float4* fa, const float4* fn, uint32_t pixels,
-                                 float spp_feature, uint16_t* out, float* base, cudaStream_t st)
+                                 float spp_feature, uint16_t* out, float* base, uint32_t feat_fp16, uint32_t half_fp16,
+                                 cudaStream_t st)
 {
     k_denoise_input<<<grid_for(pixels, 256), 256, 0, st>>>(img, half, fa, fn, pixels, spp_feature, out,
-                                                           reinterpret_cast<float4*>(base));
+                                                           reinterpret_cast<float4*>(base), feat_fp16, half_fp16);
     return cudaGetLastError();
 }
 

@@ -70,8 +70,10 @@ cudaError_t features_init_tables(const uint32_t* table128, const float* srgb256,
 
 // Denoiser features and packing (features.cu).
 cudaError_t launch_features(const RenderArgs& a, float4* feat_a, float4* feat_n, cudaStream_t stream);
+// fa/fn (and half) hold 4 x FP16 per pixel when feat_fp16 (half_fp16) is set.
 cudaError_t launch_denoise_input(const float4* img, const float4* half, const float4* fa, const float4* fn, uint32_t pixels,
-                                 float spp_feature, uint16_t* out, float* base, cudaStream_t stream);
+                                 float spp_feature, uint16_t* out, float* base, uint32_t feat_fp16, uint32_t half_fp16,
+                                 cudaStream_t stream);
 cudaError_t launch_denoise_output(const float* out32, uint32_t pixels, float4* img, cudaStream_t stream);
 
 // Output stage (post.cu).

@@ -43,8 +43,8 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
         const DevScene& s = a.s;
         float4 fa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), fn = fa;
         if (a.feat_a) {
-            fa = a.feat_a[pix];
-            fn = a.feat_n[pix];
+            fa = feat_load(a.feat_a, pix, a.fp16_features);
+            fn = feat_load(a.feat_n, pix, a.fp16_features);
         }
         for (uint32_t si = a.sample_index; si < a.sample_index + a.samples; si++) {
             PathState pl;
@@ -88,15 +88,15 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderArgs a)
             f3 r = correct_radiance(pl.radiance * a.exposure);
             accumulate(acc, r, si);
             if (a.snapshot && si + 1 == a.snapshot_after)
-                a.snapshot[pix] = acc;
+                feat_store(a.snapshot, pix, acc, a.fp16_features);
             s64[0] += (double)r.x;
             s64[1] += (double)r.y;
             s64[2] += (double)r.z;
         }
         a.image[pix] = acc;
         if (a.feat_a) {
-            a.feat_a[pix] = fa;
-            a.feat_n[pix] = fn;
+            feat_store(a.feat_a, pix, fa, a.fp16_features);
+            feat_store(a.feat_n, pix, fn, a.fp16_features);
         }
         if (a.sum64) {
             double* d = a.sum64 + 4 * pix;

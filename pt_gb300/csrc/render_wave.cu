@@ -377,22 +377,22 @@ __global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs<Src> a)
         }
         float4 fa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), fn = fa;
         if (R.feat_a) {
-            fa = R.feat_a[pix];
-            fn = R.feat_n[pix];
+            fa = feat_load(R.feat_a, pix, R.fp16_features);
+            fn = feat_load(R.feat_n, pix, R.fp16_features);
             for (uint32_t j = 0; j < E.samples; j++) {
                 const size_t q = E.path_base + (size_t)j * E.pixels + pix;
                 feature_mean(fa, a.w.f_a[q], E.first_sample + j);
                 feature_mean(fn, a.w.f_n[q], E.first_sample + j);
             }
-            R.feat_a[pix] = fa;
-            R.feat_n[pix] = fn;
+            feat_store(R.feat_a, pix, fa, R.fp16_features);
+            feat_store(R.feat_n, pix, fn, R.fp16_features);
         }
         for (uint32_t j = 0; j < E.samples; j++) {
             float4 r4 = a.w.rad[E.path_base + (size_t)j * E.pixels + pix];
             f3 r = correct_radiance(mk3(r4.x, r4.y, r4.z) * R.exposure);
             accumulate(acc, r, E.first_sample + j);
             if (R.snapshot && E.first_sample + j + 1 == R.snapshot_after)
-                R.snapshot[pix] = acc;
+                feat_store(R.snapshot, pix, acc, R.fp16_features);
             s64[0] += (double)r.x;
             s64[1] += (double)r.y;
             s64[2] += (double)r.z;

@@ -148,3 +148,27 @@ def test_features_accumulated_in_render(ctx, tmp_path):
     fa, fn = out["wave"]
     assert np.allclose(fa, sa, rtol=1e-5, atol=1e-6) and np.allclose(fn, sn, rtol=1e-5, atol=1e-6)
     assert fa[..., 3].max() > 0 and np.abs(fn[..., :3]).max() > 0.5
+
+
+def test_fp16_feature_storage(ctx, trained, tmp_path):
+    """PT_RENDER_FEATURES_FP16: features and the armed snapshot stored as FP16
+    are the FP32 ones rounded to nearest, the image is unchanged, and the
+    denoised result moves by far less than its error against the reference."""
+    hs = P.HostScene.load(scenes.mid_scene(tmp_path / "h", seed=1))
+    ctx.upload(hs.pack())
+    ctx.build_accel()
+    ctx.render(hs.render_params(W, H, 1024, 8, accum_mode=abi.PT_ACCUM_FP32_FP64), stats=False)
+    ref = ctx.read_image(fp64=True)
+    out = {}
+    for name, flags in (("fp32", 0), ("fp16", abi.PT_RENDER_FEATURES_FP16)):
+        p = hs.render_params(W, H, 6, 8)
+        p.flags = flags
+        ctx.render_denoised(trained, p)
+        out[name] = (ctx.read_image().copy(), ctx.read_features(), ctx.read_denoised().copy())
+    (i32, (a32, n32), d32), (i16, (a16, n16), d16) = out["fp32"], out["fp16"]
+    assert np.array_equal(i32.view(np.uint32), i16.view(np.uint32))
+    for x32, x16 in ((a32, a16), (n32, n16)):
+        assert np.array_equal(x32.astype(np.float16).astype(np.float32), x16)
+    e32, e16, shift = meansq(d32, ref), meansq(d16, ref), meansq(d16, d32.astype(np.float64))
+    print(f"fp16 features: denoised MSE {e16:.5g} vs fp32 {e32:.5g}; between them {shift:.3g}")
+    assert shift < 0.05 * e32 and abs(e16 - e32) < 0.05 * e32
