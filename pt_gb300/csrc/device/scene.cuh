@@ -438,6 +438,131 @@ static __device__ __forceinline__ bool trace_closest_inl(const DevScene& s, f3 o
     return found;
 }
 
+// Closest hit as trace_closest_inl, traversed "while-while" with speculative
+// leaves (Aila & Laine 2009): a lane that reaches a BLAS leaf parks it and
+// keeps descending interior nodes until every converged lane of the warp holds
+// a parked leaf (or has none left), then the warp tests triangles together.
+// Instance entry and exit happen in the node phase, but only with no leaf
+// parked (a parked leaf belongs to the current instance's object-space ray).
+// The hit is the same (t, instance, primitive) minimum: triangles are only
+// tested later, never skipped, and culling compares against the best t so far.
+static __device__ __forceinline__ bool trace_closest_ww(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h,
+                                                        TraceCounters& tc)
+{
+    uint32_t n_nodes = 0, n_tris = 0;
+    h.t = tmax;
+    h.inst = 0xFFFFFFFFu;
+    h.prim = 0xFFFFFFFFu;
+    h.b1 = h.b2 = 0.0f;
+    bool found = false;
+    ObjRay world;
+    world.o = o;
+    world.d = d;
+    setup_slab(world);
+    ObjRay r = world;
+    int stack[STACK_SIZE];
+    int sp = 0;
+    stack[sp++] = REF_DONE;
+    int ref = s.tlas_root;
+    bool in_blas = false;
+    uint32_t cur_inst = 0;
+    if (ref == REF_EMPTY)
+        return false;
+    int leaf = REF_EMPTY; // parked BLAS leaf (REF_EMPTY: none)
+    uint32_t iter = 0;
+    for (;;) {
+        // node phase
+        while (ref != REF_DONE) {
+            if (++iter >= s.max_iterations)
+                break;
+            if (ref >= 0) {
+                float e0, e1;
+                int c0, c1;
+                n_nodes++;
+                int m = node_children(s.nodes + ref, r, tmin, h.t, e0, e1, c0, c1);
+                if (m == 3) {
+                    int near = c0, far = c1;
+                    if (e1 < e0) {
+                        near = c1;
+                        far = c0;
+                    }
+                    if (sp < STACK_SIZE)
+                        stack[sp++] = far;
+                    else
+                        atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+                    ref = near;
+                } else if (m == 1) {
+                    ref = c0;
+                } else if (m == 2) {
+                    ref = c1;
+                } else {
+                    ref = stack[--sp];
+                }
+            } else if (ref == REF_EXIT_BLAS) {
+                if (leaf != REF_EMPTY)
+                    break;
+                r = world;
+                in_blas = false;
+                ref = stack[--sp];
+            } else if (!in_blas) {
+                // TLAS leaf: instances [first, first + count); one per leaf here.
+                const uint32_t first = leaf_first(ref), count = leaf_count(ref);
+                const DevInstance* di = s.dinst + first;
+                const int root = __ldg(&di->blas_root);
+                if (root == REF_EMPTY || count != 1 || sp >= STACK_SIZE) {
+                    if (sp >= STACK_SIZE)
+                        atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+                    ref = stack[--sp];
+                } else {
+                    cur_inst = first;
+                    to_object(di, o, d, r);
+                    stack[sp++] = REF_EXIT_BLAS;
+                    in_blas = true;
+                    ref = root;
+                }
+            } else {
+                if (leaf != REF_EMPTY)
+                    break;
+                leaf = ref;
+                ref = stack[--sp];
+            }
+            if (!__any_sync(__activemask(), leaf == REF_EMPTY))
+                break;
+        }
+        if (iter >= s.max_iterations) {
+            // A well-formed BVH never gets here; a malformed one must not hang the GPU.
+            atomicOr(s.error_word, ERR_WATCHDOG);
+            break;
+        }
+        // leaf phase
+        if (leaf != REF_EMPTY) {
+            const uint32_t first = leaf_first(leaf), count = leaf_count(leaf);
+            n_tris += count;
+            for (uint32_t k = 0; k < count; k++) {
+                const TriRec* tr = s.tris + first + k;
+                float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
+                float t, b1, b2;
+                uint32_t prim = __float_as_uint(a.w);
+                if (watertight(r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), t, b1, b2) && t >= tmin && t <= h.t &&
+                    better(t, cur_inst, prim, h)) {
+                    h.t = t;
+                    h.b1 = b1;
+                    h.b2 = b2;
+                    h.inst = cur_inst;
+                    h.prim = prim;
+                    found = true;
+                }
+            }
+            leaf = REF_EMPTY;
+        } else if (ref == REF_DONE) {
+            break;
+        }
+    }
+    tc.nodes += n_nodes;
+    tc.tris += n_tris;
+    return found;
+}
+
 // Shadow ray of shadowray.ah.hlsl / shadowray.ms.hlsl: the first opaque hit in
 // [tmin, tmax] occludes; transparent instances attenuate by (1 - alpha).
 // Returns the visibility throughput (0 = occluded).

@@ -25,6 +25,9 @@
 // (`OneJob`: path id -> sample and pixel of the call's camera) or a batch
 // (`ManyJobs`: a wave holds shares of several jobs, each with its own scene,
 // camera, size and sample range; raygen records each path's share).
+#include <cstdlib>
+#include <cstring>
+
 #include "device/render.cuh"
 #include "kernels.h"
 
@@ -183,7 +186,8 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs<Src> a)
 }
 
 // Persistent traversal: warps fetch 32 queue entries at a time.
-template <class Src>
+// WW selects the while-while traversal with speculative leaves.
+template <class Src, bool WW = true>
 __global__ void __launch_bounds__(128) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
 {
     const uint32_t* queue = a.w.queue[qi];
@@ -203,7 +207,8 @@ __global__ void __launch_bounds__(128) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
             const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
             Hit h;
-            bool hit = trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
+            bool hit = WW ? trace_closest_ww(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc)
+                          : trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
             a.w.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
             a.w.hit_prim[p] = hit ? h.prim : 0xFFFFFFFFu;
         }
@@ -456,6 +461,18 @@ static inline uint32_t capped_grid(uint64_t threads, uint32_t block, int sm_coun
     return (uint32_t)(g < cap ? (g == 0 ? 1 : g) : cap);
 }
 
+// Closest-hit traversal of k_wf_extend: while-while with speculative leaves
+// (default), or one node-or-leaf step per iteration with PT_TRAVERSAL=single
+// (kept for A/B measurements).
+static bool traversal_ww()
+{
+    static const bool ww = [] {
+        const char* v = std::getenv("PT_TRAVERSAL");
+        return !(v && std::strcmp(v, "single") == 0);
+    }();
+    return ww;
+}
+
 // Resident 128-thread blocks per SM of the persistent traversal kernels
 // (queried once per source type; thread-safe initialisation).
 template <class Src>
@@ -497,7 +514,10 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32
     const uint32_t sgrid = capped_grid(a.src.n_paths, 128, sm_count);
     for (uint32_t sg = 0; sg <= max_bounces; sg++) {
         mark(1);
-        k_wf_extend<Src><<<trace_blocks, 128, 0, st>>>(a, qi);
+        if (traversal_ww())
+            k_wf_extend<Src, true><<<trace_blocks, 128, 0, st>>>(a, qi);
+        else
+            k_wf_extend<Src, false><<<trace_blocks, 128, 0, st>>>(a, qi);
         mark(2);
         k_wf_shade<Src><<<sgrid, 128, 0, st>>>(a, qi);
         mark(3);
