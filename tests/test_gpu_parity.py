@@ -212,12 +212,9 @@ def test_kernels_agree_on_counts(ctx, mid):
     a = ctx.render(hs.render_params(128, 96, 3, 8, kernel=abi.PT_KERNEL_MEGA))
     b = ctx.render(hs.render_params(128, 96, 3, 8, kernel=abi.PT_KERNEL_WAVEFRONT))
     assert (a.segments, a.shadow_rays, a.paths) == (b.segments, b.shadow_rays, b.paths)
-    # The wavefront's closest-hit traversal is while-while with speculative
-    # leaves: lanes keep descending while others in the warp look for a leaf,
-    # so it visits a few percent more nodes and tests a few more triangles
-    # than the megakernel's one-step loop; the hits (and images) are the same.
-    assert a.node_visits <= b.node_visits <= 1.10 * a.node_visits
-    assert a.tri_tests <= b.tri_tests <= 1.25 * a.tri_tests  # measured +11 % on this view
+    # Both kernels run the same one-step traversal loop per ray (the
+    # while-while variant behind PT_TRAVERSAL=ww visits more nodes).
+    assert a.node_visits == b.node_visits and a.tri_tests == b.tri_tests
     assert b.kernel_used == abi.PT_KERNEL_WAVEFRONT and a.kernel_used == abi.PT_KERNEL_MEGA
 
 
