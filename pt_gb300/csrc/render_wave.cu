@@ -25,6 +25,7 @@
 // (`OneJob`: path id -> sample and pixel of the call's camera) or a batch
 // (`ManyJobs`: a wave holds shares of several jobs, each with its own scene,
 // camera, size and sample range; raygen records each path's share).
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 
@@ -186,9 +187,10 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs<Src> a)
 }
 
 // Persistent traversal: warps fetch 32 queue entries at a time.
-// WW selects the while-while traversal with speculative leaves.
-template <class Src, bool WW = false>
-__global__ void __launch_bounds__(128) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
+// WW selects the while-while traversal with speculative leaves; MINB is the
+// resident-block target of the launch bounds (the register budget).
+template <class Src, bool WW, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
 {
     const uint32_t* queue = a.w.queue[qi];
     const uint32_t count = *(volatile uint32_t*)&a.w.counts[qi];
@@ -221,8 +223,8 @@ __global__ void __launch_bounds__(128) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
     }
 }
 
-template <class Src>
-__global__ void __launch_bounds__(128) k_wf_shade(WaveArgs<Src> a, uint32_t qi)
+template <class Src, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_t qi)
 {
     const uint32_t* qin = a.w.queue[qi];
     uint32_t* qout = a.w.queue[qi ^ 1];
@@ -314,8 +316,8 @@ __global__ void __launch_bounds__(128) k_wf_shade(WaveArgs<Src> a, uint32_t qi)
     }
 }
 
-template <class Src>
-__global__ void __launch_bounds__(128) k_wf_shadow(WaveArgs<Src> a)
+template <class Src, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_wf_shadow(WaveArgs<Src> a)
 {
     const uint32_t count = a.w.counts[2];
     unsigned lane = threadIdx.x & 31;
@@ -461,29 +463,62 @@ static inline uint32_t capped_grid(uint64_t threads, uint32_t block, int sm_coun
     return (uint32_t)(g < cap ? (g == 0 ? 1 : g) : cap);
 }
 
-// Closest-hit traversal of k_wf_extend: one node-or-leaf step per iteration
-// (default), or while-while with speculative leaves with PT_TRAVERSAL=ww
-// (kept for A/B measurements: on the mid scene it ran 24 % slower, its extra
-// node visits and triangle tests costing more than the coherence gained).
-static bool traversal_ww()
+// Launch variants of the stage kernels, fixed per process: the closest-hit
+// traversal (one node-or-leaf step per iteration, or while-while with
+// speculative leaves with PT_TRAVERSAL=ww: on the mid scene the latter ran
+// 24 % slower, its extra node visits and triangle tests costing more than the
+// coherence gained) and the resident-block targets of extend, shadow and
+// shade (PT_MINB="extend,shadow,shade", e.g. "8,8,5"; default none, the
+// occupancy their natural register counts give: 7, 7 and 4 blocks).  The alternatives stay for
+// A/B measurements.
+struct StageVariant {
+    bool ww = false;
+    int ext = 0, sh = 0, shade = 0; // 0: no resident-block target
+};
+
+static StageVariant stage_variant()
 {
-    static const bool ww = [] {
-        const char* v = std::getenv("PT_TRAVERSAL");
-        return v && std::strcmp(v, "ww") == 0;
+    static const StageVariant v = [] {
+        StageVariant r;
+        const char* t = std::getenv("PT_TRAVERSAL");
+        r.ww = t && std::strcmp(t, "ww") == 0;
+        const char* m = std::getenv("PT_MINB");
+        int e = 0, s = 0, h = 0;
+        if (m && std::sscanf(m, "%d,%d,%d", &e, &s, &h) == 3) {
+            r.ext = (e == 8 || e == 10) ? e : 0;
+            r.sh = (s == 8 || s == 10) ? s : 0;
+            r.shade = (h == 5 || h == 6) ? h : 0;
+        }
+        if (r.ww)
+            r.ext = 0;
+        return r;
     }();
-    return ww;
+    return v;
 }
 
-// Resident 128-thread blocks per SM of the persistent traversal kernels
-// (queried once per source type; thread-safe initialisation).
+template <typename K>
+static int resident_blocks(K kernel)
+{
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 128, 0);
+    return b < 1 ? 1 : b;
+}
+
+// Resident 128-thread blocks per SM of the persistent traversal kernels of the
+// process's variant (queried once; thread-safe initialisation).
 template <class Src>
 static int2 traversal_blocks_per_sm()
 {
     static const int2 v = [] {
-        int e = 0, s = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e, k_wf_extend<Src>, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s, k_wf_shadow<Src>, 128, 0);
-        return make_int2(e < 1 ? 1 : e, s < 1 ? 1 : s);
+        const StageVariant sv = stage_variant();
+        int e = sv.ww ? resident_blocks(k_wf_extend<Src, true, 0>)
+                      : sv.ext == 8 ? resident_blocks(k_wf_extend<Src, false, 8>)
+                      : sv.ext == 10 ? resident_blocks(k_wf_extend<Src, false, 10>)
+                                     : resident_blocks(k_wf_extend<Src, false, 0>);
+        int s = sv.sh == 8 ? resident_blocks(k_wf_shadow<Src, 8>)
+              : sv.sh == 10 ? resident_blocks(k_wf_shadow<Src, 10>)
+                            : resident_blocks(k_wf_shadow<Src, 0>);
+        return make_int2(e, s);
     }();
     return v;
 }
@@ -504,6 +539,7 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32
             tm->mark(st, s);
     };
     // persistent traversal grids: exactly the resident blocks of every SM
+    const StageVariant sv = stage_variant();
     const int2 per_sm = traversal_blocks_per_sm<Src>();
     const int trace_blocks = sm_count * per_sm.x;
     const int shadow_blocks = sm_count * per_sm.y;
@@ -515,14 +551,28 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32
     const uint32_t sgrid = capped_grid(a.src.n_paths, 128, sm_count);
     for (uint32_t sg = 0; sg <= max_bounces; sg++) {
         mark(1);
-        if (traversal_ww())
-            k_wf_extend<Src, true><<<trace_blocks, 128, 0, st>>>(a, qi);
+        if (sv.ww)
+            k_wf_extend<Src, true, 0><<<trace_blocks, 128, 0, st>>>(a, qi);
+        else if (sv.ext == 8)
+            k_wf_extend<Src, false, 8><<<trace_blocks, 128, 0, st>>>(a, qi);
+        else if (sv.ext == 10)
+            k_wf_extend<Src, false, 10><<<trace_blocks, 128, 0, st>>>(a, qi);
         else
-            k_wf_extend<Src, false><<<trace_blocks, 128, 0, st>>>(a, qi);
+            k_wf_extend<Src, false, 0><<<trace_blocks, 128, 0, st>>>(a, qi);
         mark(2);
-        k_wf_shade<Src><<<sgrid, 128, 0, st>>>(a, qi);
+        if (sv.shade == 5)
+            k_wf_shade<Src, 5><<<sgrid, 128, 0, st>>>(a, qi);
+        else if (sv.shade == 6)
+            k_wf_shade<Src, 6><<<sgrid, 128, 0, st>>>(a, qi);
+        else
+            k_wf_shade<Src, 0><<<sgrid, 128, 0, st>>>(a, qi);
         mark(3);
-        k_wf_shadow<Src><<<shadow_blocks, 128, 0, st>>>(a);
+        if (sv.sh == 8)
+            k_wf_shadow<Src, 8><<<shadow_blocks, 128, 0, st>>>(a);
+        else if (sv.sh == 10)
+            k_wf_shadow<Src, 10><<<shadow_blocks, 128, 0, st>>>(a);
+        else
+            k_wf_shadow<Src, 0><<<shadow_blocks, 128, 0, st>>>(a);
         mark(4);
         k_wf_reset<<<1, 1, 0, st>>>(a.w.counts, qi);
         nl += 4;
