@@ -16,7 +16,20 @@
 // 1e-5 of the largest coordinate) so the traversal's box tests stay
 // conservative.  The TLAS is the same construction over instance world boxes
 // with one segment.
+//
+// Default topology: PLOC (Meister & Bittner 2018, "Parallel locally-ordered
+// clustering for bounding volume hierarchy construction") on the same sorted
+// keys: every primitive starts as a cluster; each round, every cluster finds
+// the neighbour within PLOC_RADIUS positions (same segment) whose merged box
+// has the smallest surface area (ties broken by the lower index pair, so the
+// globally closest pair in each segment is always mutual), mutual nearest
+// neighbours merge into a new node, and the survivors are compacted in
+// order, until each segment is one cluster.  Nodes are numbered in merge
+// order by prefix sums (deterministic).  PT_BVH=lbvh selects the radix tree
+// instead (kept for A/B).
 #include <cub/cub.cuh>
+#include <cstdlib>
+#include <cstring>
 
 #include "device/scene.cuh"
 #include "kernels.h"
@@ -81,6 +94,19 @@ struct Scratch {
     int* seg_root;
     void* cub_temp;
     size_t cub_bytes;
+    // PLOC clusters (double-buffered) and per-round flags / prefix sums
+    int* c_ref[2];
+    float4* c_lo[2];
+    float4* c_hi[2];
+    uint32_t* c_seg[2];
+    int* nn;
+    uint32_t* m_flag;
+    uint32_t* a_flag;
+    uint32_t* m_scan;
+    uint32_t* a_scan;
+    uint32_t* counters; // [0] nodes emitted, [1] clusters after the round, [2] merges in the round
+    void* scan_temp;
+    size_t scan_bytes;
 };
 
 template <typename T>
@@ -97,6 +123,13 @@ size_t cub_sort_bytes(uint32_t n)
     size_t bytes = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, bytes, (uint64_t*)nullptr, (uint64_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
                                     (int)n, 0, 64);
+    return bytes;
+}
+
+size_t cub_scan_bytes(uint32_t n)
+{
+    size_t bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n);
     return bytes;
 }
 
@@ -123,6 +156,20 @@ Scratch carve_scratch(void* base, uint32_t n, uint32_t nseg)
     s.seg_box = carve<int>(p, 6 * (size_t)(nseg + 1));
     s.seg_base = carve<uint32_t>(p, nseg + 2);
     s.seg_root = carve<int>(p, nseg + 1);
+    for (int b = 0; b < 2; b++) {
+        s.c_ref[b] = carve<int>(p, nn);
+        s.c_lo[b] = carve<float4>(p, nn);
+        s.c_hi[b] = carve<float4>(p, nn);
+        s.c_seg[b] = carve<uint32_t>(p, nn);
+    }
+    s.nn = carve<int>(p, nn);
+    s.m_flag = carve<uint32_t>(p, nn);
+    s.a_flag = carve<uint32_t>(p, nn);
+    s.m_scan = carve<uint32_t>(p, nn);
+    s.a_scan = carve<uint32_t>(p, nn);
+    s.counters = carve<uint32_t>(p, 4);
+    s.scan_bytes = cub_scan_bytes(nn);
+    s.scan_temp = carve<char>(p, s.scan_bytes);
     s.cub_bytes = cub_sort_bytes(nn);
     s.cub_temp = carve<char>(p, s.cub_bytes);
     return s;
@@ -393,6 +440,119 @@ __global__ void k_emit_nodes(Scratch s, int n, BvhNode* nodes, int node_base, in
     nodes[node_base + i] = nd;
 }
 
+// ---- PLOC
+constexpr int PLOC_RADIUS = 16;
+
+__device__ __forceinline__ float half_area(float4 lo, float4 hi)
+{
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ __forceinline__ float4 box_min(float4 a, float4 b) { return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f); }
+__device__ __forceinline__ float4 box_max(float4 a, float4 b) { return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), 0.0f); }
+
+// Initial clusters: one per primitive, in sorted order.
+__global__ void k_ploc_init(Scratch s, uint32_t n, int mode_tlas)
+{
+    uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= n)
+        return;
+    const uint32_t p = s.vals_out[pos];
+    s.c_ref[0][pos] = mode_tlas ? make_leaf(p, 1) : make_leaf(pos, 1);
+    s.c_lo[0][pos] = s.lo[p];
+    s.c_hi[0][pos] = s.hi[p];
+    s.c_seg[0][pos] = (uint32_t)(s.keys_out[pos] >> KEY_SEG_SHIFT);
+}
+
+// (min, max) index pair order for ties between equal distances
+__device__ __forceinline__ bool pair_before(int i, int j, int k)
+{
+    const int a0 = min(i, j), a1 = max(i, j), b0 = min(i, k), b1 = max(i, k);
+    return a0 < b0 || (a0 == b0 && a1 < b1);
+}
+
+__global__ void k_ploc_nn(const float4* lo, const float4* hi, const uint32_t* seg, int n, int* nn)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const float4 li = lo[i], hi_i = hi[i];
+    const uint32_t si = seg[i];
+    float best = 0.0f;
+    int bj = -1;
+    const int j0 = max(0, i - PLOC_RADIUS), j1 = min(n - 1, i + PLOC_RADIUS);
+    for (int j = j0; j <= j1; j++) {
+        if (j == i || seg[j] != si)
+            continue;
+        const float d = half_area(box_min(li, lo[j]), box_max(hi_i, hi[j]));
+        if (bj < 0 || d < best || (d == best && pair_before(i, j, bj))) {
+            best = d;
+            bj = j;
+        }
+    }
+    nn[i] = bj;
+}
+
+// Mutual nearest neighbours merge; the lower index of a pair keeps the merged cluster.
+__global__ void k_ploc_flags(const int* nn, int n, uint32_t* m_flag, uint32_t* a_flag)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const int j = nn[i];
+    const bool mutual = j >= 0 && nn[j] == i;
+    m_flag[i] = (mutual && i < j) ? 1u : 0u;
+    a_flag[i] = (mutual && i > j) ? 0u : 1u;
+}
+
+__global__ void k_ploc_merge(Scratch s, int cur, int n, BvhNode* nodes, int node_base)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !s.a_flag[i])
+        return;
+    const int nxt = cur ^ 1;
+    const uint32_t o = s.a_scan[i];
+    const float4 lo = s.c_lo[cur][i], hi = s.c_hi[cur][i];
+    if (s.m_flag[i]) {
+        const int j = s.nn[i];
+        const float4 lo_j = s.c_lo[cur][j], hi_j = s.c_hi[cur][j];
+        const int node = (int)(s.counters[0] + s.m_scan[i]);
+        float4 blo[2], bhi[2];
+        padded(lo, hi, blo[0], bhi[0]);
+        padded(lo_j, hi_j, blo[1], bhi[1]);
+        BvhNode nd;
+        nd.c0xy = make_float4(blo[0].x, bhi[0].x, blo[0].y, bhi[0].y);
+        nd.c1xy = make_float4(blo[1].x, bhi[1].x, blo[1].y, bhi[1].y);
+        nd.c01z = make_float4(blo[0].z, bhi[0].z, blo[1].z, bhi[1].z);
+        nd.link = make_int4(s.c_ref[cur][i], s.c_ref[cur][j], 0, 0);
+        nodes[node_base + node] = nd;
+        s.c_ref[nxt][o] = node_base + node;
+        s.c_lo[nxt][o] = box_min(lo, lo_j);
+        s.c_hi[nxt][o] = box_max(hi, hi_j);
+    } else {
+        s.c_ref[nxt][o] = s.c_ref[cur][i];
+        s.c_lo[nxt][o] = lo;
+        s.c_hi[nxt][o] = hi;
+    }
+    s.c_seg[nxt][o] = s.c_seg[cur][i];
+}
+
+__global__ void k_ploc_count(Scratch s, int n)
+{
+    const uint32_t merges = s.m_scan[n - 1] + s.m_flag[n - 1];
+    s.counters[0] += merges;
+    s.counters[1] = s.a_scan[n - 1] + s.a_flag[n - 1];
+    s.counters[2] = merges;
+}
+
+__global__ void k_ploc_roots(Scratch s, int cur, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        s.seg_root[s.c_seg[cur][i]] = s.c_ref[cur][i];
+}
+
 __global__ void k_write_tris(BvhBuildInput in, Scratch s, TriRec* tris)
 {
     uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
@@ -433,7 +593,52 @@ int bits_for(uint32_t v)
     return b;
 }
 
-// Sort + radix tree + boxes + node emission for one key set.
+bool use_ploc()
+{
+    static const bool v = [] {
+        const char* e = std::getenv("PT_BVH");
+        return !(e && std::strcmp(e, "lbvh") == 0);
+    }();
+    return v;
+}
+
+// PLOC rounds over the sorted primitives; ends when a round merges nothing
+// (then every non-empty segment is one cluster).
+cudaError_t build_ploc(Scratch& s, uint32_t n, BvhNode* nodes, int node_base, int mode_tlas, cudaStream_t st)
+{
+    k_ploc_init<<<blocks(n, 256), 256, 0, st>>>(s, n, mode_tlas);
+    cudaMemsetAsync(s.counters, 0, 4 * sizeof(uint32_t), st);
+    int cur = 0;
+    uint32_t live = n;
+    for (uint32_t round = 0; live > 1; round++) {
+        if (round > n)
+            return cudaErrorUnknown; // every round merges at least one pair while a segment has two clusters
+        k_ploc_nn<<<blocks(live, 128), 128, 0, st>>>(s.c_lo[cur], s.c_hi[cur], s.c_seg[cur], (int)live, s.nn);
+        k_ploc_flags<<<blocks(live, 256), 256, 0, st>>>(s.nn, (int)live, s.m_flag, s.a_flag);
+        size_t bytes = s.scan_bytes;
+        cudaError_t e = cub::DeviceScan::ExclusiveSum(s.scan_temp, bytes, s.m_flag, s.m_scan, (int)live, st);
+        if (e == cudaSuccess)
+            e = cub::DeviceScan::ExclusiveSum(s.scan_temp, bytes, s.a_flag, s.a_scan, (int)live, st);
+        if (e != cudaSuccess)
+            return e;
+        k_ploc_merge<<<blocks(live, 128), 128, 0, st>>>(s, cur, (int)live, nodes, node_base);
+        k_ploc_count<<<1, 1, 0, st>>>(s, (int)live);
+        uint32_t c[3];
+        e = cudaMemcpyAsync(c, s.counters, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess)
+            return e;
+        cur ^= 1;
+        live = c[1];
+        if (c[2] == 0)
+            break;
+    }
+    k_ploc_roots<<<blocks(live, 128), 128, 0, st>>>(s, cur, (int)live);
+    return cudaGetLastError();
+}
+
+// Sort + tree topology + node emission for one key set.
 cudaError_t build_tree(Scratch& s, uint32_t n, uint32_t nseg, BvhNode* nodes, int node_base, int mode_tlas, cudaStream_t st)
 {
     if (n == 0) {
@@ -448,6 +653,10 @@ cudaError_t build_tree(Scratch& s, uint32_t n, uint32_t nseg, BvhNode* nodes, in
     cudaError_t e = cub::DeviceRadixSort::SortPairs(s.cub_temp, bytes, s.keys_in, s.keys_out, s.vals_in, s.vals_out, (int)n, 0, end_bit, st);
     if (e != cudaSuccess)
         return e;
+    if (use_ploc()) {
+        k_small_roots<<<blocks(nseg, 128), 128, 0, st>>>(s, nseg, mode_tlas);
+        return build_ploc(s, n, nodes, node_base, mode_tlas, st);
+    }
     cudaMemsetAsync(s.parent, 0xFF, sizeof(int) * n, st);
     if (n > 1)
         k_karras<<<blocks(n - 1, 256), 256, 0, st>>>(s, (int)n, node_base, mode_tlas);
