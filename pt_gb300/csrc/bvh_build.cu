@@ -20,7 +20,7 @@
 // Default topology: PLOC (Meister & Bittner 2018, "Parallel locally-ordered
 // clustering for bounding volume hierarchy construction") on the same sorted
 // keys: every primitive starts as a cluster; each round, every cluster finds
-// the neighbour within PLOC_RADIUS positions (same segment) whose merged box
+// the neighbour within a window of positions (same segment) whose merged box
 // has the smallest surface area (ties broken by the lower index pair, so the
 // globally closest pair in each segment is always mutual), mutual nearest
 // neighbours merge into a new node, and the survivors are compacted in
@@ -441,7 +441,22 @@ __global__ void k_emit_nodes(Scratch s, int n, BvhNode* nodes, int node_base, in
 }
 
 // ---- PLOC
-constexpr int PLOC_RADIUS = 16;
+// Neighbour windows of the BLAS and TLAS passes: PT_PLOC_RADIUS and
+// PT_PLOC_RADIUS_TLAS (1..256), default 64 for both (measured on the mid and
+// heavy scenes against 8..256; wider windows did not lower node visits).
+int env_radius(const char* name, int dflt)
+{
+    const char* e = std::getenv(name);
+    const int r = e ? std::atoi(e) : dflt;
+    return r < 1 ? 1 : (r > 256 ? 256 : r);
+}
+
+int ploc_radius(int mode_tlas)
+{
+    static const int blas = env_radius("PT_PLOC_RADIUS", 64);
+    static const int tlas = env_radius("PT_PLOC_RADIUS_TLAS", 64);
+    return mode_tlas ? tlas : blas;
+}
 
 __device__ __forceinline__ float half_area(float4 lo, float4 hi)
 {
@@ -472,7 +487,7 @@ __device__ __forceinline__ bool pair_before(int i, int j, int k)
     return a0 < b0 || (a0 == b0 && a1 < b1);
 }
 
-__global__ void k_ploc_nn(const float4* lo, const float4* hi, const uint32_t* seg, int n, int* nn)
+__global__ void k_ploc_nn(const float4* lo, const float4* hi, const uint32_t* seg, int n, int radius, int* nn)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -481,7 +496,7 @@ __global__ void k_ploc_nn(const float4* lo, const float4* hi, const uint32_t* se
     const uint32_t si = seg[i];
     float best = 0.0f;
     int bj = -1;
-    const int j0 = max(0, i - PLOC_RADIUS), j1 = min(n - 1, i + PLOC_RADIUS);
+    const int j0 = max(0, i - radius), j1 = min(n - 1, i + radius);
     for (int j = j0; j <= j1; j++) {
         if (j == i || seg[j] != si)
             continue;
@@ -613,7 +628,7 @@ cudaError_t build_ploc(Scratch& s, uint32_t n, BvhNode* nodes, int node_base, in
     for (uint32_t round = 0; live > 1; round++) {
         if (round > n)
             return cudaErrorUnknown; // every round merges at least one pair while a segment has two clusters
-        k_ploc_nn<<<blocks(live, 128), 128, 0, st>>>(s.c_lo[cur], s.c_hi[cur], s.c_seg[cur], (int)live, s.nn);
+        k_ploc_nn<<<blocks(live, 128), 128, 0, st>>>(s.c_lo[cur], s.c_hi[cur], s.c_seg[cur], (int)live, ploc_radius(mode_tlas), s.nn);
         k_ploc_flags<<<blocks(live, 256), 256, 0, st>>>(s.nn, (int)live, s.m_flag, s.a_flag);
         size_t bytes = s.scan_bytes;
         cudaError_t e = cub::DeviceScan::ExclusiveSum(s.scan_temp, bytes, s.m_flag, s.m_scan, (int)live, st);
