@@ -191,6 +191,12 @@ typedef struct pt_render_params {
  * means are updated in FP32 and rounded to nearest on every store).  The
  * image itself stays FP32. */
 #define PT_RENDER_FEATURES_FP16 4u
+/* pt_render_params.flags: clear the image and the FP64 sums before this call
+ * even when sample_index > 0.  For replicas rendering a sample range
+ * [sample_index, sample_index + samples) of a larger render on another GPU:
+ * their FP64 sums (PT_IMAGE_SUMS64) are that range's contribution; the FP32
+ * image of such a call is not a mean of anything and is not meant to be read. */
+#define PT_RENDER_RESTART 8u
 
 /* Counters of the last pt_render call. */
 typedef struct pt_render_stats {
@@ -266,7 +272,12 @@ int pt_render_next(pt_ctx* ctx, uint32_t samples, pt_render_stats* stats_out);
 
 /* Copy the accumulated image to host memory as RGBA rows of `pitch_bytes`
  * bytes (float when fp64 == 0, double when fp64 == 1).  Replaces the copy
- * into the host-visible image and vkMapMemory of ptdispatch.cpp:77-94. */
+ * into the host-visible image and vkMapMemory of ptdispatch.cpp:77-94.
+ * fp64 == PT_IMAGE_SUMS64 copies the raw FP64 sums instead (rgb radiance
+ * sums and the sample count per pixel, 4 doubles): the form in which
+ * replicas rendering disjoint sample ranges on several GPUs are merged (an
+ * element-wise sum). */
+#define PT_IMAGE_SUMS64 3
 int pt_read_image(pt_ctx* ctx, void* rgba, size_t pitch_bytes, int fp64);
 
 /* Wait for all work of the context. */

@@ -213,6 +213,8 @@ PT_IMAGE_DENOISED = 2
 PT_RENDER_FEATURES = 1
 PT_RENDER_TIME_STAGES = 2
 PT_RENDER_FEATURES_FP16 = 4
+PT_RENDER_RESTART = 8
+PT_IMAGE_SUMS64 = 3
 PT_UNET_IN_CHANNELS = 16
 PT_UNET_OUT_CHANNELS = 16
 

@@ -560,14 +560,15 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
         return c->fail(PT_ERR_INVALID, "unknown accumulation mode or kernel");
     cudaSetDevice(c->device);
     bool fp64 = p->accum_mode == PT_ACCUM_FP32_FP64;
-    int rc = ensure_image(c, p->width, p->height, fp64, p->sample_index == 0);
+    if (p->flags & ~(PT_RENDER_FEATURES | PT_RENDER_TIME_STAGES | PT_RENDER_FEATURES_FP16 | PT_RENDER_RESTART))
+        return c->fail(PT_ERR_INVALID, "unknown render flags");
+    const bool restart = p->sample_index == 0 || (p->flags & PT_RENDER_RESTART) != 0;
+    int rc = ensure_image(c, p->width, p->height, fp64, restart);
     if (rc != PT_OK)
         return rc;
-    if (p->sample_index == 0)
+    if (restart)
         c->image_epoch++;
     RenderArgs a = render_args(c, p, fp64);
-    if (p->flags & ~(PT_RENDER_FEATURES | PT_RENDER_TIME_STAGES | PT_RENDER_FEATURES_FP16))
-        return c->fail(PT_ERR_INVALID, "unknown render flags");
     const bool features = (p->flags & PT_RENDER_FEATURES) != 0;
     a.fp16_features = (p->flags & PT_RENDER_FEATURES_FP16) ? 1u : 0u;
     if (features) {
@@ -763,10 +764,19 @@ int pt_read_image(pt_ctx* c, void* rgba, size_t pitch, int fp64)
             return c->cuda_fail(e, "image read-back");
         return PT_OK;
     }
-    if (!c->sum64.p)
+    if (fp64 != 1 && fp64 != PT_IMAGE_SUMS64)
+        return c->fail(PT_ERR_INVALID, "unknown image kind");
+    if (!c->sum64.p || !c->have_fp64)
         return c->fail(PT_ERR_STATE, "no FP64 accumulation (render with PT_ACCUM_FP32_FP64)");
     if (pitch < (size_t)c->width * 32)
         return c->fail(PT_ERR_INVALID, "pitch smaller than a row");
+    if (fp64 == PT_IMAGE_SUMS64) {
+        e = cudaMemcpy2DAsync(rgba, pitch, c->sum64.p, (size_t)c->width * 32, (size_t)c->width * 32, c->height,
+                              cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        return e == cudaSuccess ? PT_OK : c->cuda_fail(e, "FP64 sums read-back");
+    }
     size_t n = (size_t)c->width * c->height;
     std::vector<double> sums(4 * n);
     e = cudaMemcpyAsync(sums.data(), c->sum64.p, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);

@@ -151,6 +151,21 @@ def test_stage_timing(ctx, small):
     assert sum(st.stage_ms) <= st.milliseconds * 1.05 + 0.05
 
 
+def test_replica_ranges_merge_to_one_render(ctx, small):
+    """Replicas: sample ranges rendered separately (PT_RENDER_RESTART, FP64
+    sums) add up to one render of all samples."""
+    from pt_gb300 import replicas
+    hs, view = small
+    ctx.upload(view)
+    ctx.build_accel()
+    p = hs.render_params(48, 32, 7, 5, accum_mode=abi.PT_ACCUM_FP32_FP64)
+    ctx.render(p)
+    single = replicas.read_sums(ctx)
+    merged = sum(replicas.render_partial(ctx, p, 7, r, 3) for r in range(3))
+    assert np.array_equal(merged[..., 3], single[..., 3])
+    np.testing.assert_allclose(merged[..., :3], single[..., :3], rtol=1e-12, atol=1e-12)
+
+
 def test_deterministic(ctx, small):
     hs, view = small
     params = hs.render_params(64, 48, 3, 8)
