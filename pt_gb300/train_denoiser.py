@@ -28,10 +28,11 @@ from .denoise import WEIGHTS_DIR, UNet, init_params, save_params
 from . import trainset
 
 
-def render_set(ctx, seeds, size, target_spp, input_spps, bounces=8):
+def render_set(ctx, seeds, size, target_spp, input_spps):
     """Returns (inputs [len(seeds) * len(input_spps), size, size, 16] bf16,
     residual bases [same, 4] fp32, targets [len(seeds), size, size, 4] fp32,
-    noisy images [same as inputs, 4] fp32)."""
+    noisy images [same as inputs, 4] fp32).  Bounce limit and Russian
+    roulette per scene from trainset.render_settings."""
     import torch
 
     k = len(input_spps)
@@ -44,12 +45,14 @@ def render_set(ctx, seeds, size, target_spp, input_spps, bounces=8):
         hs = HostScene.from_raw(raw, cam)
         ctx.upload(hs.pack())
         ctx.build_accel()
-        ctx.render(hs.render_params(size, size, target_spp, bounces, accum_mode=abi.PT_ACCUM_FP32_FP64), stats=False)
+        bounces, rr = trainset.render_settings(seed)
+        ctx.render(hs.render_params(size, size, target_spp, bounces, rr_start=rr, accum_mode=abi.PT_ACCUM_FP32_FP64),
+                   stats=False)
         y = ctx.read_image(fp64=True).astype(np.float32)
         y[..., 3] = 1.0
         Y[i].copy_(torch.from_numpy(y))
         for j, spp in enumerate(input_spps):
-            ctx.render_noisy(hs.render_params(size, size, spp, bounces))
+            ctx.render_noisy(hs.render_params(size, size, spp, bounces, rr_start=rr))
             ctx.denoise_input(spp, X[i * k + j].data_ptr(), B[i * k + j].data_ptr())
             N[i * k + j].copy_(torch.from_numpy(ctx.read_image()))
     torch.cuda.synchronize()

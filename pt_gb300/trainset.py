@@ -18,11 +18,14 @@ import numpy as np
 from . import scenes
 
 
-def material(base, rough=0.5, metal=0.0, emission=0.0) -> np.ndarray:
-    """One pt_material row (24 floats, include/pt_gpu.h layout)."""
+def material(base, rough=0.5, metal=0.0, emission=0.0, alpha=1.0) -> np.ndarray:
+    """One pt_material row (24 floats, include/pt_gpu.h layout); alpha < 1
+    sets the transparency bit (transmission as the reference maps it)."""
     m = np.zeros(24, np.float32)
     m[0:3] = base
-    m[3] = 1.0
+    m[3] = alpha
+    if alpha < 1.0:
+        m[11] = np.frombuffer(np.uint32(1 << 13).tobytes(), np.float32)[0]
     m[4:7] = 1.0 if emission > 0 else 0.0
     m[7] = emission if emission > 0 else 1.0
     m[8] = rough
@@ -64,9 +67,23 @@ def _mesh_library():
     return _LIB
 
 
+def render_settings(seed: int) -> tuple[int, int]:
+    """(max bounces, first Russian-roulette segment) of training scene `seed`:
+    the benchmark's 8 / 1 for 70 % of the scenes, 12 / 4 (the heavy
+    configuration's) for the rest."""
+    rng = np.random.default_rng([seed, 7])
+    return (8, 1) if rng.random() < 0.7 else (12, 4)
+
+
 def training_scene(seed: int):
-    """Returns (raw scene dict, camera dict) for HostScene.from_raw."""
+    """Returns (raw scene dict, camera dict) for HostScene.from_raw.  A third
+    of the scenes are "clutter" scenes modelled on the heavy configuration
+    (hundreds to thousands of randomly rotated instances of displaced grids
+    and spheres in a wide volume, 10 % of the variants transmissive, emitters
+    above, a distant camera); the rest are ground + objects scenes."""
     rng = np.random.default_rng(seed)
+    if rng.random() < 1.0 / 3.0:
+        return _clutter_scene(rng)
     lib = _mesh_library()
     meshes = []  # (mesh arrays, material row, [4x4 matrices])
 
@@ -110,6 +127,39 @@ def training_scene(seed: int):
         strength = float(np.exp(rng.uniform(0, math.log(100))))
         meshes.append((tri, material((0, 0, 0), 1.0, 0.0, strength), [np.eye(4)]))
 
+    return _assemble(meshes, rng), _camera(rng)
+
+
+def _clutter_scene(rng):
+    lib = _mesh_library()
+    kinds = lib["grid"] + lib["sphere"]
+    variants = []
+    for _ in range(int(rng.integers(4, 12))):
+        alpha = float(rng.uniform(0.1, 0.5)) if rng.random() < 0.1 else 1.0
+        m = material(rng.uniform(0.1, 0.9, 3), rng.uniform(0.05, 1.0), 1.0 if rng.random() < 0.3 else 0.0, alpha=alpha)
+        variants.append((kinds[rng.integers(len(kinds))], m, []))
+    extent = float(rng.uniform(20, 120))
+    for _ in range(int(np.exp(rng.uniform(math.log(200), math.log(3000))))):
+        s = rng.uniform(0.3, 2.5)
+        rot = _rotation(rng.uniform(-1, 1, 3), rng.uniform(1e-5, 2 * math.pi))
+        pos = (rng.uniform(-extent, extent), rng.uniform(0, 0.2 * extent), rng.uniform(-extent, extent))
+        variants[rng.integers(len(variants))][2].append(_matrix((s, s, s), rot, pos))
+    meshes = [v for v in variants if v[2]]
+    for _ in range(int(np.exp(rng.uniform(math.log(8), math.log(256))))):
+        cx, cy, cz = rng.uniform(-extent, extent), rng.uniform(0.25, 0.4) * extent, rng.uniform(-extent, extent)
+        size = rng.uniform(0.01, 0.035) * extent
+        tri = scenes.triangle((cx - size, cy, cz - size * 0.5), (cx, cy, cz + size), (cx + size, cy, cz - size * 0.5))
+        strength = float(np.exp(rng.uniform(0, math.log(100))))
+        meshes.append((tri, material((0, 0, 0), 1.0, 0.0, strength), [np.eye(4)]))
+    raw = _assemble(meshes, rng)
+    eye = np.array([rng.uniform(-0.3, 0.3) * extent, rng.uniform(0.2, 0.6) * extent, -rng.uniform(0.9, 1.6) * extent])
+    target = np.array([rng.uniform(-0.2, 0.2) * extent, rng.uniform(0.0, 0.1) * extent, rng.uniform(-0.2, 0.2) * extent])
+    fov = float(np.exp(rng.uniform(math.log(20), math.log(60))))
+    cam = {"position": tuple(-eye), "lookdir": tuple(eye - target), "fov_degrees": fov}
+    return raw, cam
+
+
+def _assemble(meshes, rng) -> dict:
     v, idx, ranges, mm, mio, inst, mats = [], [], [], [], [0], [], []
     voff = ioff = 0
     for (p, n, uv, ix), mat, insts in meshes:
@@ -124,10 +174,13 @@ def training_scene(seed: int):
             inst.append(np.asarray(M, np.float32).T.reshape(-1))  # column-major
         mio.append(mio[-1] + len(insts))
     env = rng.uniform(0.05, 0.5, 3) * np.array([0.7, 0.8, 1.0])
-    raw = {"vertices": np.concatenate(v).astype(np.float32), "indices": np.concatenate(idx).astype(np.uint32),
-           "meshes": np.array(ranges, np.uint32), "mesh_material": np.array(mm, np.uint32),
-           "mesh_instance_offset": np.array(mio, np.uint32), "instance_matrices": np.array(inst, np.float32),
-           "materials": np.array(mats, np.float32), "environment_colour": env.astype(np.float32)}
+    return {"vertices": np.concatenate(v).astype(np.float32), "indices": np.concatenate(idx).astype(np.uint32),
+            "meshes": np.array(ranges, np.uint32), "mesh_material": np.array(mm, np.uint32),
+            "mesh_instance_offset": np.array(mio, np.uint32), "instance_matrices": np.array(inst, np.float32),
+            "materials": np.array(mats, np.float32), "environment_colour": env.astype(np.float32)}
+
+
+def _camera(rng) -> dict:
     # camera: eye around the scene looking at a point near the centre
     dist = rng.uniform(8, 25)
     ang = rng.uniform(-0.6, 0.6) + math.pi
@@ -135,6 +188,5 @@ def training_scene(seed: int):
     target = np.array([rng.uniform(-4, 4), rng.uniform(0, 2), rng.uniform(-2, 4)])
     lens = 0.0 if rng.random() < 0.6 else rng.uniform(0.01, 0.05)
     fov = float(np.exp(rng.uniform(math.log(8), math.log(60))))
-    cam = {"position": tuple(-eye), "lookdir": tuple(eye - target), "fov_degrees": fov,
-           "lens_radius": lens, "focus_dist": float(np.linalg.norm(eye - target))}
-    return raw, cam
+    return {"position": tuple(-eye), "lookdir": tuple(eye - target), "fov_degrees": fov,
+            "lens_radius": lens, "focus_dist": float(np.linalg.norm(eye - target))}
