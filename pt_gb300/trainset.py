@@ -76,13 +76,13 @@ def render_settings(seed: int) -> tuple[int, int]:
 
 
 def training_scene(seed: int):
-    """Returns (raw scene dict, camera dict) for HostScene.from_raw.  A third
+    """Returns (raw scene dict, camera dict) for HostScene.from_raw.  A quarter
     of the scenes are "clutter" scenes modelled on the heavy configuration
     (hundreds to thousands of randomly rotated instances of displaced grids
     and spheres in a wide volume, 10 % of the variants transmissive, emitters
     above, a distant camera); the rest are ground + objects scenes."""
     rng = np.random.default_rng(seed)
-    if rng.random() < 1.0 / 3.0:
+    if rng.random() < 0.25:
         return _clutter_scene(rng)
     lib = _mesh_library()
     meshes = []  # (mesh arrays, material row, [4x4 matrices])
