@@ -107,6 +107,14 @@ struct Scratch {
     uint32_t* counters; // [0] nodes emitted, [1] clusters after the round, [2] merges in the round
     void* scan_temp;
     size_t scan_bytes;
+    // leaf collapse of the BLAS trees
+    uint32_t* cnt;      // triangles under a node
+    float* sah;         // SAH cost of a node's best form
+    uint32_t* collapse; // 1: the node is cheaper as one leaf
+    uint32_t* newpos;   // depth-first position of each triangle (sorted position -> TriRec slot)
+    uint32_t* node_off; // depth-first position of a node's first triangle
+    uint32_t* visits;   // bottom-up arrival counters
+    uint32_t blas_nodes; // host: BLAS nodes emitted by PLOC
 };
 
 template <typename T>
@@ -168,6 +176,13 @@ Scratch carve_scratch(void* base, uint32_t n, uint32_t nseg)
     s.m_scan = carve<uint32_t>(p, nn);
     s.a_scan = carve<uint32_t>(p, nn);
     s.counters = carve<uint32_t>(p, 4);
+    s.cnt = carve<uint32_t>(p, nn);
+    s.sah = carve<float>(p, nn);
+    s.collapse = carve<uint32_t>(p, nn);
+    s.newpos = carve<uint32_t>(p, nn);
+    s.node_off = carve<uint32_t>(p, nn);
+    s.visits = carve<uint32_t>(p, nn);
+    s.blas_nodes = 0;
     s.scan_bytes = cub_scan_bytes(nn);
     s.scan_temp = carve<char>(p, s.scan_bytes);
     s.cub_bytes = cub_sort_bytes(nn);
@@ -568,6 +583,156 @@ __global__ void k_ploc_roots(Scratch s, int cur, int n)
         s.seg_root[s.c_seg[cur][i]] = s.c_ref[cur][i];
 }
 
+// ---- SAH leaf collapse of the BLAS trees (PLOC output, leaves of one triangle)
+constexpr int TREE_DEPTH_CAP = 1 << 16; // walks of a valid tree end far earlier
+// Cost model (unnormalised SAH): leaf of n triangles = CT * n * A, interior
+// node = CI * A + cost(c0) + cost(c1), A the node's surface area.  A node
+// whose best form is a leaf of at most LEAF_MAX triangles is collapsed; the
+// triangles are then laid out depth-first so every leaf is a contiguous range.
+
+__global__ void k_link_parents(Scratch s, const BvhNode* nodes, uint32_t nb)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb)
+        return;
+    const int4 l = nodes[i].link;
+    const int cs[2] = {l.x, l.y};
+    for (int k = 0; k < 2; k++) {
+        if (cs[k] >= 0)
+            s.parent[cs[k]] = (int)i;
+        else
+            s.leaf_parent[leaf_first(cs[k])] = (int)i;
+    }
+    s.visits[i] = 0;
+}
+
+__device__ __forceinline__ float child_area(const BvhNode& nd, int k)
+{
+    return k == 0 ? half_area(make_float4(nd.c0xy.x, nd.c0xy.z, nd.c01z.x, 0.0f), make_float4(nd.c0xy.y, nd.c0xy.w, nd.c01z.y, 0.0f))
+                  : half_area(make_float4(nd.c1xy.x, nd.c1xy.z, nd.c01z.z, 0.0f), make_float4(nd.c1xy.y, nd.c1xy.w, nd.c01z.w, 0.0f));
+}
+
+__device__ __forceinline__ float node_area(const BvhNode& nd)
+{
+    const float4 lo = make_float4(fminf(nd.c0xy.x, nd.c1xy.x), fminf(nd.c0xy.z, nd.c1xy.z), fminf(nd.c01z.x, nd.c01z.z), 0.0f);
+    const float4 hi = make_float4(fmaxf(nd.c0xy.y, nd.c1xy.y), fmaxf(nd.c0xy.w, nd.c1xy.w), fmaxf(nd.c01z.y, nd.c01z.w), 0.0f);
+    return half_area(lo, hi);
+}
+
+// Bottom-up from every triangle: the second arrival at a node evaluates it.
+__global__ void k_sah_up(Scratch s, const BvhNode* nodes, uint32_t n, float ci, float ct, uint32_t leaf_max)
+{
+    const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= n)
+        return;
+    int node = s.leaf_parent[pos];
+    for (int depth = 0; node >= 0 && depth < TREE_DEPTH_CAP; depth++) {
+        __threadfence();
+        if (atomicAdd(&s.visits[node], 1u) == 0)
+            return; // the sibling subtree finishes this node
+        const BvhNode nd = nodes[node];
+        const int cs[2] = {nd.link.x, nd.link.y};
+        uint32_t cnt = 0;
+        float sub = 0.0f;
+        for (int k = 0; k < 2; k++) {
+            if (cs[k] < 0) {
+                cnt += 1;
+                sub += ct * child_area(nd, k);
+            } else {
+                cnt += __ldcg(&s.cnt[cs[k]]);
+                sub += __ldcg(&s.sah[cs[k]]);
+            }
+        }
+        const float a = node_area(nd);
+        const float inner = ci * a + sub;
+        const float leaf = ct * (float)cnt * a;
+        const bool col = cnt <= leaf_max && leaf <= inner;
+        __stcg(&s.cnt[node], cnt);
+        __stcg(&s.sah[node], col ? leaf : inner);
+        __stcg(&s.collapse[node], col ? 1u : 0u);
+        __threadfence();
+        node = s.parent[node];
+    }
+}
+
+// Depth-first positions: a triangle's (or node's) offset inside its mesh is
+// the sum of the left siblings' triangle counts along the path to the root.
+__device__ __forceinline__ uint32_t dfs_offset(const Scratch& s, const BvhNode* nodes, int node, int from_ref, int& root)
+{
+    uint32_t off = 0;
+    int child = from_ref;
+    for (int depth = 0; node >= 0 && depth < TREE_DEPTH_CAP; depth++) {
+        const int4 l = nodes[node].link;
+        if (child == l.y)
+            off += l.x < 0 ? 1u : s.cnt[l.x];
+        root = node;
+        child = node;
+        node = s.parent[node];
+    }
+    return off;
+}
+
+__global__ void k_dfs_positions(Scratch s, const BvhNode* nodes, uint32_t n)
+{
+    const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= n)
+        return;
+    const uint32_t seg = (uint32_t)(s.keys_out[pos] >> KEY_SEG_SHIFT);
+    int root = -1;
+    const uint32_t off = dfs_offset(s, nodes, s.leaf_parent[pos], make_leaf(pos, 1), root);
+    s.newpos[pos] = s.seg_base[seg] + off;
+}
+
+// A subtree's first depth-first slot is its leftmost triangle's.
+__global__ void k_node_offsets(Scratch s, const BvhNode* nodes, uint32_t nb)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb)
+        return;
+    int c = (int)i;
+    for (int depth = 0; c >= 0 && depth < TREE_DEPTH_CAP; depth++)
+        c = nodes[c].link.x;
+    s.node_off[i] = c < 0 ? s.newpos[leaf_first(c)] : 0u;
+}
+
+__global__ void k_rewrite_links(Scratch s, BvhNode* nodes, uint32_t nb)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb)
+        return;
+    int4 l = nodes[i].link;
+    int* cs[2] = {&l.x, &l.y};
+    for (int k = 0; k < 2; k++) {
+        const int c = *cs[k];
+        if (c < 0)
+            *cs[k] = make_leaf(s.newpos[leaf_first(c)], 1);
+        else if (s.collapse[c])
+            *cs[k] = make_leaf(s.node_off[c], s.cnt[c]);
+    }
+    nodes[i].link = l;
+}
+
+__global__ void k_rewrite_roots(Scratch s, uint32_t nseg)
+{
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nseg)
+        return;
+    const int r = s.seg_root[m];
+    if (r >= 0) {
+        if (s.collapse[r])
+            s.seg_root[m] = make_leaf(s.node_off[r], s.cnt[r]);
+    } else if (ref_is_leaf(r)) {
+        s.seg_root[m] = make_leaf(s.newpos[leaf_first(r)], 1);
+    }
+}
+
+__global__ void k_identity_positions(Scratch s, uint32_t n)
+{
+    const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos < n)
+        s.newpos[pos] = pos;
+}
+
 __global__ void k_write_tris(BvhBuildInput in, Scratch s, TriRec* tris)
 {
     uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
@@ -585,7 +750,7 @@ __global__ void k_write_tris(BvhBuildInput in, Scratch s, TriRec* tris)
     r.v0 = make_float4(a.x, a.y, a.z, __uint_as_float(local));
     r.v1 = make_float4(b.x, b.y, b.z, 0.0f);
     r.v2 = make_float4(c.x, c.y, c.z, 0.0f);
-    tris[pos] = r;
+    tris[s.newpos[pos]] = r;
 }
 
 __global__ void k_set_roots(BvhBuildInput in, const int* mesh_root, DevInstance* dinst)
@@ -646,10 +811,40 @@ cudaError_t build_ploc(Scratch& s, uint32_t n, BvhNode* nodes, int node_base, in
             return e;
         cur ^= 1;
         live = c[1];
+        s.blas_nodes = c[0];
         if (c[2] == 0)
             break;
     }
     k_ploc_roots<<<blocks(live, 128), 128, 0, st>>>(s, cur, (int)live);
+    return cudaGetLastError();
+}
+
+float env_float(const char* name, float dflt)
+{
+    const char* e = std::getenv(name);
+    return e ? (float)std::atof(e) : dflt;
+}
+
+// Collapses the BLAS trees of `nb` nodes over n triangles and fills newpos
+// (identity when collapse is off: PT_LEAF_MAX=1 or the radix tree).
+cudaError_t collapse_leaves(Scratch& s, uint32_t n, uint32_t nseg, BvhNode* nodes, uint32_t nb, cudaStream_t st)
+{
+    static const uint32_t leaf_max = (uint32_t)std::min(4, std::max(1, (int)env_float("PT_LEAF_MAX", 4.0f)));
+    static const float ct = env_float("PT_SAH_CT", 1.0f);
+    if (n == 0)
+        return cudaSuccess;
+    if (!use_ploc() || leaf_max <= 1 || nb == 0) {
+        k_identity_positions<<<blocks(n, 256), 256, 0, st>>>(s, n);
+        return cudaGetLastError();
+    }
+    cudaMemsetAsync(s.parent, 0xFF, sizeof(int) * nb, st);
+    cudaMemsetAsync(s.leaf_parent, 0xFF, sizeof(int) * n, st); // single-triangle meshes have no parent node
+    k_link_parents<<<blocks(nb, 256), 256, 0, st>>>(s, nodes, nb);
+    k_sah_up<<<blocks(n, 256), 256, 0, st>>>(s, nodes, n, 1.0f, ct, leaf_max);
+    k_dfs_positions<<<blocks(n, 256), 256, 0, st>>>(s, nodes, n);
+    k_node_offsets<<<blocks(nb, 256), 256, 0, st>>>(s, nodes, nb);
+    k_rewrite_links<<<blocks(nb, 256), 256, 0, st>>>(s, nodes, nb);
+    k_rewrite_roots<<<blocks(nseg, 128), 128, 0, st>>>(s, nseg);
     return cudaGetLastError();
 }
 
@@ -718,7 +913,10 @@ cudaError_t bvh_build(const BvhBuildInput& in, BvhBuildOutput& out, void* scratc
             sb.seg_box = mesh_box;
             k_tri_boxes<<<blocks(in.tri_count, 256), 256, 0, st>>>(in, sb);
         }
+        s.blas_nodes = 0;
         e = build_tree(s, in.tri_count, in.mesh_count, out.nodes, 0, 0, st);
+        if (e == cudaSuccess)
+            e = collapse_leaves(s, in.tri_count, in.mesh_count, out.nodes, s.blas_nodes, st);
         if (e != cudaSuccess)
             return e;
         if (in.tri_count > 0)
