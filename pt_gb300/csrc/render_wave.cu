@@ -132,7 +132,8 @@ struct WaveState {
     // queues
     uint32_t* queue[2];
     uint32_t* shadow_queue;
-    uint32_t* counts;   // [0],[1] path queues, [2] shadow queue, [3] work fetch, [4] shadow fetch
+    uint32_t* hit_queue; // paths whose ray hit something this segment (shade's input)
+    uint32_t* counts;   // [0],[1] path queues, [2] shadow queue, [3] work fetch, [4] shadow fetch, [5] hit queue
 };
 
 template <class Src>
@@ -183,12 +184,18 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs<Src> a)
         a.w.counts[2] = 0;
         a.w.counts[3] = 0;
         a.w.counts[4] = 0;
+        a.w.counts[5] = 0;
     }
 }
 
 // Persistent traversal: warps fetch 32 queue entries at a time.
 // WW selects the while-while traversal with speculative leaves; MINB is the
 // resident-block target of the launch bounds (the register budget).
+// A ray that misses is finished here (pathtrace.ms.hlsl:6-11: radiance +=
+// throughput * envcol, the path ends; zero first-hit features); hits go to
+// the hit queue, so shade runs on hit paths only.  The previous segment's
+// shadow stage ran before this launch, so the radiance terms keep the
+// reference's order.
 template <class Src, bool WW, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
 {
@@ -196,6 +203,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32
     const uint32_t count = *(volatile uint32_t*)&a.w.counts[qi];
     unsigned lane = threadIdx.x & 31;
     TraceCounters tc{0u, 0u};
+    uint32_t misses = 0;
     while (true) {
         uint32_t base = 0;
         if (lane == 0)
@@ -204,31 +212,52 @@ __global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32
         if (base >= count)
             break;
         uint32_t i = base + lane;
+        uint32_t p = 0;
+        bool hit = false;
         if (i < count) {
-            uint32_t p = queue[i];
-            const DevScene& s = a.src.args(a.src.job_of(p)).s;
+            p = queue[i];
+            const RenderArgs& R = a.src.args(a.src.job_of(p));
+            const DevScene& s = R.s;
             float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
             Hit h;
-            bool hit = WW ? trace_closest_ww(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc)
-                          : trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
-            a.w.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
-            a.w.hit_prim[p] = hit ? h.prim : 0xFFFFFFFFu;
+            hit = WW ? trace_closest_ww(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc)
+                     : trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
+            if (hit) {
+                a.w.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
+                a.w.hit_prim[p] = h.prim;
+            } else {
+                misses++;
+                PathState pl;
+                const float4 t4 = a.w.tp[p], r4 = a.w.rad[p];
+                pl.throughput = mk3(t4.x, t4.y, t4.z);
+                pl.radiance = mk3(r4.x, r4.y, r4.z);
+                shade_miss(s, pl);
+                a.w.rad[p] = make_float4(pl.radiance.x, pl.radiance.y, pl.radiance.z, 0.0f);
+                if (R.feat_a && a.w.seg[p] == 0) {
+                    a.w.f_a[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    a.w.f_n[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                }
+            }
         }
+        push_warp(a.w.hit_queue, &a.w.counts[5], hit, p);
     }
     uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
     uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
+    misses = __reduce_add_sync(0xffffffffu, misses);
     if (lane == 0) {
         atomicAdd(a.src.counters() + 3, (unsigned long long)nodes);
         atomicAdd(a.src.counters() + 4, (unsigned long long)tris);
+        if (misses)
+            atomicAdd(a.src.counters() + 0, (unsigned long long)misses);
     }
 }
 
 template <class Src, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_t qi)
 {
-    const uint32_t* qin = a.w.queue[qi];
+    const uint32_t* qin = a.w.hit_queue;
     uint32_t* qout = a.w.queue[qi ^ 1];
-    const uint32_t count = a.w.counts[qi];
+    const uint32_t count = a.w.counts[5];
     uint32_t segments = 0, shadow_rays = 0;
     // grid-stride over whole warps so the warp-wide pushes see full warps
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < count; base += gridDim.x * blockDim.x) {
@@ -257,13 +286,8 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_
             NeeRequest nee;
             nee.add = false;
             nee.trace = false;
-            if (prim == 0xFFFFFFFFu) {
-                if (sg == 0 && R.feat_a) {
-                    a.w.f_a[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    a.w.f_n[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                }
-                shade_miss(s, pl);
-            } else {
+            {
+                // the hit queue holds hits only (extend finished the misses)
                 float4 hh = a.w.hit[p];
                 Hit h;
                 h.t = hh.x;
@@ -362,10 +386,11 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shadow(WaveArgs<Src> a)
 // Clears the consumed queue count and the fetch counters between stages.
 __global__ void k_wf_reset(uint32_t* counts, uint32_t qi)
 {
-    counts[qi] = 0; // the queue just consumed by shade
+    counts[qi] = 0; // the queue just consumed by extend
     counts[2] = 0;  // shadow queue consumed
     counts[3] = 0;
     counts[4] = 0;
+    counts[5] = 0;  // hit queue consumed by shade
 }
 
 template <class Src>
@@ -419,7 +444,7 @@ __global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs<Src> a)
 
 size_t wave_state_bytes(uint32_t n_paths)
 {
-    return (size_t)n_paths * (16 * 13 + 4 * 5) + 4096;
+    return (size_t)n_paths * (16 * 13 + 4 * 6) + 4096;
 }
 
 static inline char* bump(char*& p, size_t bytes)
@@ -452,6 +477,7 @@ static bool carve_state(WaveState& w, void* state, size_t state_bytes, size_t n)
     w.queue[0] = (uint32_t*)bump(p, 4 * n);
     w.queue[1] = (uint32_t*)bump(p, 4 * n);
     w.shadow_queue = (uint32_t*)bump(p, 4 * n);
+    w.hit_queue = (uint32_t*)bump(p, 4 * n);
     w.counts = (uint32_t*)bump(p, 64);
     return (size_t)(p - (char*)state) <= state_bytes;
 }
