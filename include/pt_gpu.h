@@ -210,9 +210,10 @@ typedef struct pt_render_stats {
     uint32_t kernel_used;     /* PT_KERNEL_MEGA or PT_KERNEL_WAVEFRONT     */
     uint32_t error_word;      /* device error word (0 = none)              */
     /* With PT_RENDER_TIME_STAGES (wavefront): device time of the raygen,
-     * extend (closest hit), shade, shadow (any hit), queue-reset and
-     * accumulate launches, in ms, summed over the call; `stage_launches`
-     * counts the extend launches.  Zero otherwise. */
+     * extend (closest hit), shade (hit shading and the escaped rays' miss
+     * shading), shadow (any hit), queue-reset and accumulate launches, in ms,
+     * summed over the call; `stage_launches` counts the extend launches.
+     * Zero otherwise. */
     float stage_ms[6];
     uint32_t stage_launches;
 } pt_render_stats;
