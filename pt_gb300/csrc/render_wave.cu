@@ -132,9 +132,8 @@ struct WaveState {
     // queues
     uint32_t* queue[2];
     uint32_t* shadow_queue;
-    uint32_t* hit_queue;  // paths whose ray hit something this segment (shade's input)
-    uint32_t* miss_queue; // paths whose ray escaped (k_wf_miss's input)
-    uint32_t* counts;   // [0],[1] path queues, [2] shadow queue, [3] work fetch, [4] shadow fetch, [5] hit queue, [6] miss queue
+    uint32_t* hit_queue; // paths whose ray hit something this segment (shade's input)
+    uint32_t* counts;   // [0],[1] path queues, [2] shadow queue, [3] work fetch, [4] shadow fetch, [5] hit queue
 };
 
 template <class Src>
@@ -186,15 +185,13 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs<Src> a)
         a.w.counts[3] = 0;
         a.w.counts[4] = 0;
         a.w.counts[5] = 0;
-        a.w.counts[6] = 0;
     }
 }
 
 // Persistent traversal: warps fetch 32 queue entries at a time.
 // WW selects the while-while traversal with speculative leaves; MINB is the
 // resident-block target of the launch bounds (the register budget).
-// Hits go to the hit queue (shade's input), misses to the miss queue
-// (k_wf_miss), so neither stage carries the other's lanes.
+// Only traces: k_wf_split then separates hits from misses.
 template <class Src, bool WW, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
 {
@@ -220,13 +217,9 @@ __global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32
             Hit h;
             hit = WW ? trace_closest_ww(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc)
                      : trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
-            if (hit) {
-                a.w.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
-                a.w.hit_prim[p] = h.prim;
-            }
+            a.w.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
+            a.w.hit_prim[p] = hit ? h.prim : 0xFFFFFFFFu;
         }
-        push_warp(a.w.hit_queue, &a.w.counts[5], hit, p);
-        push_warp(a.w.miss_queue, &a.w.counts[6], i < count && !hit, p);
     }
     uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
     uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
@@ -236,33 +229,62 @@ __global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32
     }
 }
 
-// Escaped rays (pathtrace.ms.hlsl:6-11): radiance += throughput * envcol and
-// the path ends; a camera ray that escapes has zero first-hit features.  The
-// previous segment's shadow stage ran before this segment's extend, so the
-// radiance terms keep the reference's order.
+// Splits the segment's queue: escaped rays are finished here
+// (pathtrace.ms.hlsl:6-11: radiance += throughput * envcol, the path ends;
+// a camera ray that escapes has zero first-hit features), hits go to the hit
+// queue, so shade runs on hit paths only.  One atomic per block of 256 paths.
+// The previous segment's shadow stage ran before this segment's extend, so
+// the radiance terms keep the reference's order.
 template <class Src>
-__global__ void __launch_bounds__(256) k_wf_miss(WaveArgs<Src> a)
+__global__ void __launch_bounds__(256) k_wf_split(WaveArgs<Src> a, uint32_t qi)
 {
-    const uint32_t count = a.w.counts[6];
-    uint32_t segments = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const uint32_t p = a.w.miss_queue[i];
-        const RenderArgs& R = a.src.args(a.src.job_of(p));
-        PathState pl;
-        const float4 t4 = a.w.tp[p], r4 = a.w.rad[p];
-        pl.throughput = mk3(t4.x, t4.y, t4.z);
-        pl.radiance = mk3(r4.x, r4.y, r4.z);
-        shade_miss(R.s, pl);
-        a.w.rad[p] = make_float4(pl.radiance.x, pl.radiance.y, pl.radiance.z, 0.0f);
-        if (R.feat_a && a.w.seg[p] == 0) {
-            a.w.f_a[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            a.w.f_n[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    __shared__ uint32_t s_warp[8];
+    __shared__ uint32_t s_base;
+    const uint32_t* queue = a.w.queue[qi];
+    const uint32_t count = a.w.counts[qi];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t misses = 0;
+    // the loop bound is the same for the whole block, so the barriers below are uniform
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < count;
+        const uint32_t p = valid ? queue[i] : 0u;
+        const bool hit = valid && a.w.hit_prim[p] != 0xFFFFFFFFu;
+        if (valid && !hit) {
+            const RenderArgs& R = a.src.args(a.src.job_of(p));
+            PathState pl;
+            const float4 t4 = a.w.tp[p], r4 = a.w.rad[p];
+            pl.throughput = mk3(t4.x, t4.y, t4.z);
+            pl.radiance = mk3(r4.x, r4.y, r4.z);
+            shade_miss(R.s, pl);
+            a.w.rad[p] = make_float4(pl.radiance.x, pl.radiance.y, pl.radiance.z, 0.0f);
+            if (R.feat_a && a.w.seg[p] == 0) {
+                a.w.f_a[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                a.w.f_n[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+            misses++;
         }
-        segments++;
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0)
+            s_warp[warp] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t total = 0;
+            for (uint32_t w = 0; w < blockDim.x / 32; w++) {
+                const uint32_t c = s_warp[w];
+                s_warp[w] = total;
+                total += c;
+            }
+            s_base = total ? atomicAdd(&a.w.counts[5], total) : 0u;
+        }
+        __syncthreads();
+        if (hit)
+            a.w.hit_queue[s_base + s_warp[warp] + __popc(m & ((1u << lane) - 1u))] = p;
+        __syncthreads();
     }
-    segments = __reduce_add_sync(0xffffffffu, segments);
-    if ((threadIdx.x & 31) == 0 && segments)
-        atomicAdd(a.src.counters() + 0, (unsigned long long)segments);
+    misses = __reduce_add_sync(0xffffffffu, misses);
+    if (lane == 0 && misses)
+        atomicAdd(a.src.counters() + 0, (unsigned long long)misses);
 }
 
 template <class Src, int MINB>
@@ -404,7 +426,6 @@ __global__ void k_wf_reset(uint32_t* counts, uint32_t qi)
     counts[3] = 0;
     counts[4] = 0;
     counts[5] = 0;  // hit queue consumed by shade
-    counts[6] = 0;  // miss queue consumed by k_wf_miss
 }
 
 template <class Src>
@@ -458,7 +479,7 @@ __global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs<Src> a)
 
 size_t wave_state_bytes(uint32_t n_paths)
 {
-    return (size_t)n_paths * (16 * 13 + 4 * 7) + 4096;
+    return (size_t)n_paths * (16 * 13 + 4 * 6) + 4096;
 }
 
 static inline char* bump(char*& p, size_t bytes)
@@ -492,7 +513,6 @@ static bool carve_state(WaveState& w, void* state, size_t state_bytes, size_t n)
     w.queue[1] = (uint32_t*)bump(p, 4 * n);
     w.shadow_queue = (uint32_t*)bump(p, 4 * n);
     w.hit_queue = (uint32_t*)bump(p, 4 * n);
-    w.miss_queue = (uint32_t*)bump(p, 4 * n);
     w.counts = (uint32_t*)bump(p, 64);
     return (size_t)(p - (char*)state) <= state_bytes;
 }
@@ -601,7 +621,7 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32
         else
             k_wf_extend<Src, false, 0><<<trace_blocks, 128, 0, st>>>(a, qi);
         mark(2);
-        k_wf_miss<Src><<<sgrid, 256, 0, st>>>(a);
+        k_wf_split<Src><<<capped_grid(a.src.n_paths, 256, sm_count), 256, 0, st>>>(a, qi);
         if (sv.shade == 5)
             k_wf_shade<Src, 5><<<sgrid, 128, 0, st>>>(a, qi);
         else if (sv.shade == 6)
