@@ -6,10 +6,11 @@
 //
 //   raygen      camera rays of all N paths (pathtrace.rg.hlsl:18-35)
 //   extend      closest hit of every queued path (TraceRay, rg.hlsl:35,51)
-//   shade       hit/miss shading up to the NEE shadow ray, BSDF sampling and
-//               Russian roulette (pathtrace.ch.hlsl:227-360, ms.hlsl,
+//   split       finishes escaped rays (pathtrace.ms.hlsl) and queues the hits
+//   shade       hit shading up to the NEE shadow ray, BSDF sampling and
+//               Russian roulette (pathtrace.ch.hlsl:227-360,
 //               pathtrace.hlsli:118-139); pushes continuing paths and shadow
-//               requests with warp-aggregated atomics (ballot + popc)
+//               requests (ballot + popc per warp, one atomic per block)
 //   shadow      any-hit traversal + the light term (ch.hlsl:190-224)
 //   accumulate  running mean of the wave's samples in sample order
 //               (rg.hlsl:59-67), optional FP64 sums
@@ -142,19 +143,38 @@ struct WaveArgs {
     WaveState w;
 };
 
-__device__ __forceinline__ void push_warp(uint32_t* queue, uint32_t* count, bool pred, uint32_t value)
+
+// Two queue pushes for a whole block at once: one atomic per queue per block.
+// Every thread of the block must call it (block-uniform control flow).
+template <int WARPS>
+__device__ __forceinline__ void push_block2(uint32_t* q0, uint32_t* n0, bool p0, uint32_t* q1, uint32_t* n1, bool p1,
+                                            uint32_t value)
 {
-    unsigned mask = __ballot_sync(__activemask(), pred);
-    if (mask == 0)
-        return;
-    unsigned lane = threadIdx.x & 31;
-    int leader = __ffs(mask) - 1;
-    uint32_t base = 0;
-    if (lane == (unsigned)leader)
-        base = atomicAdd(count, (uint32_t)__popc(mask));
-    base = __shfl_sync(__activemask(), base, leader);
-    if (pred)
-        queue[base + __popc(mask & ((1u << lane) - 1u))] = value;
+    __shared__ uint32_t s_off[2][WARPS];
+    __shared__ uint32_t s_base[2];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned m0 = __ballot_sync(0xffffffffu, p0), m1 = __ballot_sync(0xffffffffu, p1);
+    if (lane == 0) {
+        s_off[0][warp] = __popc(m0);
+        s_off[1][warp] = __popc(m1);
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        uint32_t total = 0;
+        for (int w = 0; w < WARPS; w++) {
+            const uint32_t c = s_off[threadIdx.x][w];
+            s_off[threadIdx.x][w] = total;
+            total += c;
+        }
+        s_base[threadIdx.x] = total ? atomicAdd(threadIdx.x == 0 ? n0 : n1, total) : 0u;
+    }
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+    if (p0)
+        q0[s_base[0] + s_off[0][warp] + __popc(m0 & lt)] = value;
+    if (p1)
+        q1[s_base[1] + s_off[1][warp] + __popc(m1 & lt)] = value;
+    __syncthreads();
 }
 
 template <class Src>
@@ -295,8 +315,9 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_
     const uint32_t count = a.w.counts[5];
     uint32_t segments = 0, shadow_rays = 0;
     // grid-stride over whole warps so the warp-wide pushes see full warps
-    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < count; base += gridDim.x * blockDim.x) {
-        uint32_t i = base + (threadIdx.x & 31);
+    // block-uniform loop: the queue pushes below synchronise the block
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + threadIdx.x;
         bool active = i < count;
         bool cont = false, trace = false;
         uint32_t p = active ? qin[i] : 0;
@@ -364,8 +385,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_
                 a.w.ray_d[p] = make_float4(pl.next_d.x, pl.next_d.y, pl.next_d.z, __int_as_float(0x7f800000));
             }
         }
-        push_warp(qout, &a.w.counts[qi ^ 1], cont, p);
-        push_warp(a.w.shadow_queue, &a.w.counts[2], trace, p);
+        push_block2<4>(qout, &a.w.counts[qi ^ 1], cont, a.w.shadow_queue, &a.w.counts[2], trace, p);
     }
     segments = __reduce_add_sync(0xffffffffu, segments);
     shadow_rays = __reduce_add_sync(0xffffffffu, shadow_rays);
