@@ -137,10 +137,6 @@ struct WaveState {
     uint32_t* counts;   // [0],[1] path queues, [2] shadow queue, [3] work fetch, [4] shadow fetch, [5] hit queue
 };
 
-// Queue entries a warp of the persistent traversal kernels takes per fetch:
-// 32 x FETCH_ROUNDS (one atomic per fetch).
-constexpr uint32_t FETCH_ROUNDS = 4;
-
 template <class Src>
 struct WaveArgs {
     Src src;
@@ -227,20 +223,20 @@ __global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32
     while (true) {
         uint32_t base = 0;
         if (lane == 0)
-            base = atomicAdd(&a.w.counts[3], 32u * FETCH_ROUNDS);
+            base = atomicAdd(&a.w.counts[3], 32u);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= count)
             break;
-        for (uint32_t r = 0; r < FETCH_ROUNDS; r++) {
-            const uint32_t i = base + 32u * r + lane;
-            if (i >= count)
-                break;
-            const uint32_t p = queue[i];
+        uint32_t i = base + lane;
+        uint32_t p = 0;
+        bool hit = false;
+        if (i < count) {
+            p = queue[i];
             const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
             Hit h;
-            const bool hit = WW ? trace_closest_ww(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc)
-                                : trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
+            hit = WW ? trace_closest_ww(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc)
+                     : trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
             a.w.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
             a.w.hit_prim[p] = hit ? h.prim : 0xFFFFFFFFu;
         }
@@ -408,14 +404,12 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shadow(WaveArgs<Src> a)
     while (true) {
         uint32_t base = 0;
         if (lane == 0)
-            base = atomicAdd(&a.w.counts[4], 32u * FETCH_ROUNDS);
+            base = atomicAdd(&a.w.counts[4], 32u);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= count)
             break;
-        for (uint32_t r = 0; r < FETCH_ROUNDS; r++) {
-            const uint32_t i = base + 32u * r + lane;
-            if (i >= count)
-                break;
+        uint32_t i = base + lane;
+        if (i < count) {
             uint32_t p = a.w.shadow_queue[i];
             const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.nee_o[p], d = a.w.nee_d[p];
