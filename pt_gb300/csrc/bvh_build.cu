@@ -242,38 +242,9 @@ __global__ void k_tri_boxes(BvhBuildInput in, Scratch s)
     atomic_bounds(s.seg_box + 6 * m, lo, hi);
 }
 
-// Union of the 8 transformed corners of an object-space box.
-__device__ __forceinline__ void add_transformed_box(const float4 rows[3], const float blo[3], const float bhi[3], float4& lo, float4& hi)
-{
-    for (int corner = 0; corner < 8; corner++) {
-        double p[3] = {(corner & 1) ? bhi[0] : blo[0], (corner & 2) ? bhi[1] : blo[1], (corner & 4) ? bhi[2] : blo[2]};
-        float w[3];
-        for (int r = 0; r < 3; r++)
-            w[r] = (float)((double)rows[r].x * p[0] + (double)rows[r].y * p[1] + (double)rows[r].z * p[2] + (double)rows[r].w);
-        lo.x = fminf(lo.x, w[0]);
-        lo.y = fminf(lo.y, w[1]);
-        lo.z = fminf(lo.z, w[2]);
-        hi.x = fmaxf(hi.x, w[0]);
-        hi.y = fmaxf(hi.y, w[1]);
-        hi.z = fmaxf(hi.z, w[2]);
-    }
-}
-
-__device__ __forceinline__ void child_box(const BvhNode& nd, int k, float lo[3], float hi[3])
-{
-    if (k == 0) {
-        lo[0] = nd.c0xy.x, hi[0] = nd.c0xy.y, lo[1] = nd.c0xy.z, hi[1] = nd.c0xy.w, lo[2] = nd.c01z.x, hi[2] = nd.c01z.y;
-    } else {
-        lo[0] = nd.c1xy.x, hi[0] = nd.c1xy.y, lo[1] = nd.c1xy.z, hi[1] = nd.c1xy.w, lo[2] = nd.c01z.z, hi[2] = nd.c01z.w;
-    }
-}
-
-// World box of each instance: the union of the transformed (padded) boxes two
-// levels below its BLAS root — up to four boxes, tighter than the transformed
-// mesh box under rotation — or the transformed mesh box for a one-triangle
-// mesh.  Every box contains its triangles, so the union contains the
-// instance's geometry.
-__global__ void k_inst_boxes(BvhBuildInput in, const int* mesh_box, const int* mesh_root, const BvhNode* nodes, Scratch s)
+// World box of each instance: the 8 corners of its mesh box under the
+// object-to-world transform, padded.
+__global__ void k_inst_boxes(BvhBuildInput in, const int* mesh_box, Scratch s)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= in.instance_count)
@@ -286,28 +257,22 @@ __global__ void k_inst_boxes(BvhBuildInput in, const int* mesh_box, const int* m
     float4 rows[3] = {d.t0, d.t1, d.t2};
     float4 lo = make_float4(__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000), 0.0f);
     float4 hi = make_float4(-lo.x, -lo.y, -lo.z, 0.0f);
-    const int root = m < in.mesh_count ? mesh_root[m] : REF_EMPTY;
     if (!(blo[0] <= bhi[0])) {
         // empty mesh: a point at the instance origin (its BLAS root is empty)
         lo = make_float4(rows[0].w, rows[1].w, rows[2].w, 0.0f);
         hi = lo;
-    } else if (root < 0) {
-        add_transformed_box(rows, blo, bhi, lo, hi);
     } else {
-        const BvhNode nd = nodes[root];
-        const int cs[2] = {nd.link.x, nd.link.y};
-        for (int k = 0; k < 2; k++) {
-            float clo[3], chi[3];
-            if (cs[k] >= 0) {
-                const BvhNode ch = nodes[cs[k]];
-                for (int g = 0; g < 2; g++) {
-                    child_box(ch, g, clo, chi);
-                    add_transformed_box(rows, clo, chi, lo, hi);
-                }
-            } else {
-                child_box(nd, k, clo, chi);
-                add_transformed_box(rows, clo, chi, lo, hi);
-            }
+        for (int corner = 0; corner < 8; corner++) {
+            double p[3] = {(corner & 1) ? bhi[0] : blo[0], (corner & 2) ? bhi[1] : blo[1], (corner & 4) ? bhi[2] : blo[2]};
+            float w[3];
+            for (int r = 0; r < 3; r++)
+                w[r] = (float)((double)rows[r].x * p[0] + (double)rows[r].y * p[1] + (double)rows[r].z * p[2] + (double)rows[r].w);
+            lo.x = fminf(lo.x, w[0]);
+            lo.y = fminf(lo.y, w[1]);
+            lo.z = fminf(lo.z, w[2]);
+            hi.x = fmaxf(hi.x, w[0]);
+            hi.y = fmaxf(hi.y, w[1]);
+            hi.z = fmaxf(hi.z, w[2]);
         }
     }
     s.lo[i] = lo;
@@ -972,7 +937,7 @@ cudaError_t bvh_build(const BvhBuildInput& in, BvhBuildOutput& out, void* scratc
     uint32_t tb[2] = {0, in.instance_count};
     k_init_bounds<<<1, 32, 0, st>>>(s.seg_cb, s.seg_box, s.seg_root, 1);
     cudaMemcpyAsync(s.seg_base, tb, sizeof(tb), cudaMemcpyHostToDevice, st);
-    k_inst_boxes<<<blocks(in.instance_count, 128), 128, 0, st>>>(in, mesh_box, out.mesh_root, out.nodes, s);
+    k_inst_boxes<<<blocks(in.instance_count, 128), 128, 0, st>>>(in, mesh_box, s);
     e = build_tree(s, in.instance_count, 1, out.nodes, tlas_base, 1, st);
     if (e != cudaSuccess)
         return e;
