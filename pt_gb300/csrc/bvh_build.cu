@@ -782,6 +782,20 @@ bool use_ploc()
     return v;
 }
 
+// The TLAS builder may differ (PT_BVH_TLAS=lbvh|ploc; default: as PT_BVH).
+bool use_ploc_tlas()
+{
+    static const bool v = [] {
+        const char* e = std::getenv("PT_BVH_TLAS");
+        if (e && std::strcmp(e, "lbvh") == 0)
+            return false;
+        if (e && std::strcmp(e, "ploc") == 0)
+            return true;
+        return use_ploc();
+    }();
+    return v;
+}
+
 // PLOC rounds over the sorted primitives; ends when a round merges nothing
 // (then every non-empty segment is one cluster).
 cudaError_t build_ploc(Scratch& s, uint32_t n, BvhNode* nodes, int node_base, int mode_tlas, cudaStream_t st)
@@ -866,7 +880,7 @@ cudaError_t build_tree(Scratch& s, uint32_t n, uint32_t nseg, BvhNode* nodes, in
     cudaError_t e = cub::DeviceRadixSort::SortPairs(s.cub_temp, bytes, s.keys_in, s.keys_out, s.vals_in, s.vals_out, (int)n, 0, end_bit, st);
     if (e != cudaSuccess)
         return e;
-    if (use_ploc()) {
+    if (mode_tlas ? use_ploc_tlas() : use_ploc()) {
         k_small_roots<<<blocks(nseg, 128), 128, 0, st>>>(s, nseg, mode_tlas);
         return build_ploc(s, n, nodes, node_base, mode_tlas, st);
     }
