@@ -4,15 +4,18 @@
 //   .scn parsing            src/scene/scenebuild.cpp:132-365, src/io/parseutil.cpp,
 //                           src/io/tokenstream.cpp, src/io/ioutil.cpp
 //   transforms              src/lalgebra.cpp:5-94
-//   model import (glTF 2.0) src/scene/scene.cpp:74-488 (the reference imports
-//                           through Assimp 5.4.3, absent here; see the notes
-//                           at load_gltf for the Assimp behaviour reproduced)
+//   model import (glTF 2.0, src/scene/scene.cpp:74-488 (the reference imports
+//   and Wavefront OBJ)      through Assimp 5.4.3, absent here; see the notes
+//                           at load_gltf and load_obj for the Assimp behaviour
+//                           reproduced)
 //   packing                 src/scene/scenebuffer.cpp:65-168
 //   light-sampler tables    src/scene/lightsample.cpp:5-221, src/aliastable.h:21-67
 //   camera matrices         src/scene/camera.h:16, camera.cpp:21-26,
 //                           scenebuild.cpp:251-264, pathtrace.cpp:381-396
 //   image output            src/io/imagewrite.cpp:19-67
 #include <algorithm>
+#include <array>
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -214,6 +217,39 @@ bool has_alpha_below_one(const HostTexture& t)
         if (t.texels[4 * i + 3] < 255)
             return true;
     return false;
+}
+
+// An encoded texture image as TextureData keeps it (texturedata.cpp:30-48:
+// the file's channel count with 3 widened to 4; sRGB only for 4 channels).
+// PNG only: JPEG and other formats are rejected.
+HostTexture decode_texture(const std::vector<uint8_t>& bytes, const std::string& what, bool srgb)
+{
+    if (bytes.size() >= 3 && bytes[0] == 0xFF && bytes[1] == 0xD8 && bytes[2] == 0xFF)
+        throw std::runtime_error("Failed to read texture " + what + " (JPEG textures are not supported)");
+    pt::host::PngImage png;
+    std::string err;
+    if (!pt::host::png_decode(bytes.data(), bytes.size(), png, err))
+        throw std::runtime_error("Failed to read texture " + what + ": " + err);
+    HostTexture ht;
+    ht.width = png.width;
+    ht.height = png.height;
+    ht.channels = png.channels;
+    ht.srgb = (png.channels == 4 && srgb) ? 1u : 0u;
+    ht.texels = std::move(png.texels);
+    return ht;
+}
+
+// has_transparency (scene.cpp:344-355): a base-colour map with alpha below
+// one, or a base-colour alpha (opacity) below one.
+void mark_transparency(Model& md)
+{
+    for (pt_material& pm : md.materials) {
+        uint32_t bits = fbits(pm.rough_metal_normal_map_bits[3]);
+        bool transparent = (bits & PT_BASE_COLOUR_MAP_BIT) ? has_alpha_below_one(md.textures[fbits(pm.base_colour[0])])
+                                                            : pm.base_colour[3] < 1.0f;
+        if (transparent)
+            pm.rough_metal_normal_map_bits[3] = bitsf(bits | PT_MATERIAL_IS_TRANSPARENT_BIT);
+    }
 }
 
 std::vector<uint8_t> decode_base64(const std::string& s)
@@ -481,28 +517,9 @@ Model load_gltf(const std::string& path)
             bytes.assign(buffers[buf].begin() + off, buffers[buf].begin() + off + len);
             what = "embedded image " + std::to_string(src.image);
         }
-        if (bytes.size() >= 3 && bytes[0] == 0xFF && bytes[1] == 0xD8 && bytes[2] == 0xFF)
-            throw std::runtime_error("Failed to read texture " + what + " (JPEG textures are not supported)");
-        pt::host::PngImage png;
-        std::string err;
-        if (!pt::host::png_decode(bytes.data(), bytes.size(), png, err))
-            throw std::runtime_error("Failed to read texture " + what + ": " + err);
-        HostTexture ht;
-        ht.width = png.width;
-        ht.height = png.height;
-        ht.channels = png.channels;
-        ht.srgb = (png.channels == 4 && src.srgb) ? 1u : 0u;
-        ht.texels = std::move(png.texels);
-        md.textures.push_back(std::move(ht));
+        md.textures.push_back(decode_texture(bytes, what, src.srgb));
     }
-    // transparency (has_transparency, scene.cpp:344-355)
-    for (pt_material& pm : md.materials) {
-        uint32_t bits = fbits(pm.rough_metal_normal_map_bits[3]);
-        bool transparent = (bits & PT_BASE_COLOUR_MAP_BIT) ? has_alpha_below_one(md.textures[fbits(pm.base_colour[0])])
-                                                            : pm.base_colour[3] < 1.0f;
-        if (transparent)
-            pm.rough_metal_normal_map_bits[3] = bitsf(bits | PT_MATERIAL_IS_TRANSPARENT_BIT);
-    }
+    mark_transparency(md);
     // meshes: one entry per primitive
     std::vector<std::vector<uint32_t>> gltf_mesh_prims(doc["meshes"].size());
     for (size_t mi = 0; mi < doc["meshes"].size(); mi++) {
@@ -655,6 +672,315 @@ Model load_gltf(const std::string& path)
             stack.push_back({ch[k].integer(-1), M});
     }
     return md;
+}
+
+// Wavefront OBJ + MTL import with the behaviour of Assimp 5.4.3's OBJ importer
+// as the reference's material extraction reads it (scene.cpp:74-296; Assimp is
+// absent here, so this restates its documented format handling and parity is
+// unpinned):
+//  - one mesh per run of faces with the same object / group and material
+//    (`o`, `g`, `usemtl`), all instanced once with the identity transform;
+//  - polygons are fanned into triangles (aiProcess_Triangulate on convex
+//    faces); negative indices count back from the last vertex read;
+//  - aiProcess_FlipUVs: v is stored as 1 - v; faces without `vn` get the flat
+//    face normal (aiProcess_GenNormals);
+//  - material keys: Kd -> COLOR_DIFFUSE (the base colour, sRGB-decoded like
+//    every factor, :94), `d` -> OPACITY (or 1 - `Tr`), Ke -> COLOR_EMISSIVE
+//    (sRGB-decoded, strength 1), Pr / Pm -> roughness / metallic factors
+//    (defaults 0.5 / 0, :190-202), `aniso` -> anisotropy; maps map_Kd
+//    (diffuse), map_Ke (emissive), map_Pr (roughness), map_Pm (metalness; the
+//    same image as map_Pr makes a combined map, :160-167), norm (normals),
+//    map_Ks (specular colour); faces without a material use Assimp's default
+//    material (diffuse 0.6, opacity 1).
+struct ObjMaterial {
+    float kd[3] = {0.6f, 0.6f, 0.6f}, ke[3] = {0.0f, 0.0f, 0.0f};
+    float opacity = 1.0f, roughness = 0.5f, metallic = 0.0f, aniso = 0.0f;
+    std::string map_kd, map_ke, map_pr, map_pm, norm, map_ks;
+};
+
+std::vector<std::string> line_tokens(const std::string& line)
+{
+    std::vector<std::string> out;
+    std::istringstream is(line);
+    std::string t;
+    while (is >> t)
+        out.push_back(t);
+    return out;
+}
+
+// A map statement's file name: the last token (options such as -bm come first).
+std::string map_file(const std::vector<std::string>& tk)
+{
+    if (tk.size() < 2)
+        throw std::runtime_error("map statement without a file");
+    return tk.back();
+}
+
+void load_mtl(const std::string& path, std::unordered_map<std::string, ObjMaterial>& out)
+{
+    std::istringstream in(read_file(path));
+    std::string line;
+    ObjMaterial* cur = nullptr;
+    auto vec3 = [](const std::vector<std::string>& tk, float v[3]) {
+        if (tk.size() < 2)
+            throw std::runtime_error("colour without components");
+        for (int k = 0; k < 3; k++)
+            v[k] = std::stof(tk[std::min<size_t>(1 + k, tk.size() - 1)]);
+    };
+    while (std::getline(in, line)) {
+        std::vector<std::string> tk = line_tokens(line);
+        if (tk.empty() || tk[0][0] == '#')
+            continue;
+        const std::string& k = tk[0];
+        if (k == "newmtl") {
+            cur = &out[tk.size() > 1 ? tk[1] : ""];
+            *cur = ObjMaterial();
+            continue;
+        }
+        if (!cur)
+            continue;
+        if (k == "Kd")
+            vec3(tk, cur->kd);
+        else if (k == "Ke")
+            vec3(tk, cur->ke);
+        else if (k == "d" && tk.size() > 1)
+            cur->opacity = std::stof(tk[1]);
+        else if (k == "Tr" && tk.size() > 1)
+            cur->opacity = 1.0f - std::stof(tk[1]);
+        else if (k == "Pr" && tk.size() > 1)
+            cur->roughness = std::stof(tk[1]);
+        else if (k == "Pm" && tk.size() > 1)
+            cur->metallic = std::stof(tk[1]);
+        else if (k == "aniso" && tk.size() > 1)
+            cur->aniso = std::stof(tk[1]);
+        else if (k == "map_Kd")
+            cur->map_kd = map_file(tk);
+        else if (k == "map_Ke")
+            cur->map_ke = map_file(tk);
+        else if (k == "map_Pr")
+            cur->map_pr = map_file(tk);
+        else if (k == "map_Pm")
+            cur->map_pm = map_file(tk);
+        else if (k == "norm")
+            cur->norm = map_file(tk);
+        else if (k == "map_Ks")
+            cur->map_ks = map_file(tk);
+    }
+}
+
+Model load_obj(const std::string& path)
+{
+    const std::string dir = directory_of(path);
+    std::istringstream in(read_file(path));
+    std::vector<float> pos, uv, nrm;
+    std::unordered_map<std::string, ObjMaterial> mtl;
+    struct Face {
+        uint32_t corners[3][3]; // position, uv, normal index (~0u: none)
+    };
+    struct Run {
+        std::string material;
+        std::vector<Face> faces;
+    };
+    std::vector<Run> runs(1);
+    runs[0].material = "\x01default";
+    std::string cur_mat = "\x01default";
+    auto new_run = [&]() {
+        if (!runs.back().faces.empty())
+            runs.push_back(Run());
+        runs.back().material = cur_mat;
+    };
+    auto index = [](const std::string& t, size_t count, const char* what) -> uint32_t {
+        if (t.empty())
+            return ~0u;
+        long v = std::stol(t);
+        long i = v > 0 ? v - 1 : (long)count + v;
+        if (v == 0 || i < 0 || (size_t)i >= count)
+            throw std::runtime_error(std::string("face refers to a missing ") + what);
+        return (uint32_t)i;
+    };
+    std::string line;
+    while (std::getline(in, line)) {
+        std::vector<std::string> tk = line_tokens(line);
+        if (tk.empty() || tk[0][0] == '#')
+            continue;
+        const std::string& k = tk[0];
+        if (k == "v" && tk.size() >= 4) {
+            for (int c = 0; c < 3; c++)
+                pos.push_back(std::stof(tk[1 + c]));
+        } else if (k == "vt" && tk.size() >= 2) {
+            uv.push_back(std::stof(tk[1]));
+            uv.push_back(tk.size() >= 3 ? std::stof(tk[2]) : 0.0f);
+        } else if (k == "vn" && tk.size() >= 4) {
+            for (int c = 0; c < 3; c++)
+                nrm.push_back(std::stof(tk[1 + c]));
+        } else if (k == "f" && tk.size() >= 4) {
+            std::vector<std::array<uint32_t, 3>> poly;
+            for (size_t t = 1; t < tk.size(); t++) {
+                std::array<std::string, 3> part;
+                size_t field = 0;
+                for (char ch : tk[t]) {
+                    if (ch == '/') {
+                        if (++field > 2)
+                            throw std::runtime_error("malformed face vertex " + tk[t]);
+                        continue;
+                    }
+                    part[field] += ch;
+                }
+                poly.push_back({index(part[0], pos.size() / 3, "position"), index(part[1], uv.size() / 2, "texture coordinate"),
+                                index(part[2], nrm.size() / 3, "normal")});
+                if (poly.back()[0] == ~0u)
+                    throw std::runtime_error("face vertex without a position");
+            }
+            for (size_t t = 1; t + 1 < poly.size(); t++) {
+                Face f;
+                const std::array<uint32_t, 3>* c3[3] = {&poly[0], &poly[t], &poly[t + 1]};
+                for (int c = 0; c < 3; c++)
+                    for (int a = 0; a < 3; a++)
+                        f.corners[c][a] = (*c3[c])[a];
+                runs.back().faces.push_back(f);
+            }
+        } else if (k == "usemtl") {
+            cur_mat = tk.size() > 1 ? tk[1] : "";
+            new_run();
+        } else if (k == "o" || k == "g") {
+            new_run();
+        } else if (k == "mtllib") {
+            for (size_t t = 1; t < tk.size(); t++)
+                load_mtl(dir + tk[t], mtl);
+        }
+    }
+    Model md;
+    // materials in first-use order, textures in first-use order of the files
+    std::unordered_map<std::string, uint32_t> mat_index, tex_index;
+    std::vector<std::pair<std::string, bool>> tex_files;
+    auto texture = [&](const std::string& file, bool srgb) -> uint32_t {
+        auto it = tex_index.find(file);
+        if (it != tex_index.end())
+            return it->second;
+        const uint32_t idx = (uint32_t)tex_files.size();
+        tex_index[file] = idx;
+        tex_files.push_back({file, srgb});
+        return idx;
+    };
+    auto material = [&](const std::string& name) -> uint32_t {
+        auto it = mat_index.find(name);
+        if (it != mat_index.end())
+            return it->second;
+        ObjMaterial om;
+        auto found = mtl.find(name);
+        if (found != mtl.end())
+            om = found->second;
+        pt_material pm;
+        std::memset(&pm, 0, sizeof(pm));
+        uint32_t bits = 0;
+        if (!om.map_kd.empty()) {
+            bits |= PT_BASE_COLOUR_MAP_BIT;
+            pm.base_colour[0] = bitsf(texture(om.map_kd, true));
+        } else {
+            for (int c = 0; c < 3; c++)
+                pm.base_colour[c] = from_srgb(om.kd[c]);
+            pm.base_colour[3] = om.opacity;
+        }
+        if (!om.map_ke.empty()) {
+            bits |= PT_EMISSION_MAP_BIT;
+            pm.emission[0] = bitsf(texture(om.map_ke, true));
+        } else {
+            for (int c = 0; c < 3; c++)
+                pm.emission[c] = from_srgb(om.ke[c]);
+        }
+        pm.emission[3] = 1.0f;
+        if (!om.map_pr.empty() && om.map_pr == om.map_pm) {
+            bits |= PT_ROUGHNESS_METALNESS_MAP_BIT;
+            pm.rough_metal_normal_map_bits[0] = bitsf(texture(om.map_pr, false));
+        } else {
+            if (!om.map_pr.empty()) {
+                bits |= PT_ROUGHNESS_MAP_BIT;
+                pm.rough_metal_normal_map_bits[0] = bitsf(texture(om.map_pr, false));
+            } else {
+                pm.rough_metal_normal_map_bits[0] = om.roughness;
+            }
+            if (!om.map_pm.empty()) {
+                bits |= PT_METALNESS_MAP_BIT;
+                pm.rough_metal_normal_map_bits[1] = bitsf(texture(om.map_pm, false));
+            } else {
+                pm.rough_metal_normal_map_bits[1] = om.metallic;
+            }
+        }
+        if (!om.norm.empty()) {
+            bits |= PT_NORMAL_MAP_BIT;
+            pm.rough_metal_normal_map_bits[2] = bitsf(texture(om.norm, false));
+        }
+        if (!om.map_ks.empty()) {
+            bits |= PT_SPECULAR_MAP_BIT;
+            pm.specular[0] = bitsf(texture(om.map_ks, false));
+        } else {
+            pm.specular[0] = pm.specular[1] = pm.specular[2] = 0.5f;
+        }
+        pm.cc_ccrgh_aniso[1] = 0.5f;
+        pm.cc_ccrgh_aniso[2] = om.aniso;
+        pm.rough_metal_normal_map_bits[3] = bitsf(bits);
+        md.materials.push_back(pm);
+        mat_index[name] = (uint32_t)md.materials.size() - 1;
+        return (uint32_t)md.materials.size() - 1;
+    };
+    for (const Run& r : runs) {
+        if (r.faces.empty())
+            continue;
+        const uint32_t mi = material(r.material);
+        pt_mesh_range range{(uint32_t)(md.vertices.size() / PT_VERTEX_FLOATS), (uint32_t)md.indices.size(),
+                            (uint32_t)r.faces.size(), (uint32_t)(3 * r.faces.size())};
+        for (const Face& f : r.faces) {
+            float p[3][3];
+            for (int c = 0; c < 3; c++)
+                for (int a = 0; a < 3; a++)
+                    p[c][a] = pos[3 * (size_t)f.corners[c][0] + a];
+            // flat face normal for corners without one (aiProcess_GenNormals)
+            float e1[3], e2[3], fn[3];
+            for (int a = 0; a < 3; a++) {
+                e1[a] = p[1][a] - p[0][a];
+                e2[a] = p[2][a] - p[0][a];
+            }
+            fn[0] = e1[1] * e2[2] - e1[2] * e2[1];
+            fn[1] = e1[2] * e2[0] - e1[0] * e2[2];
+            fn[2] = e1[0] * e2[1] - e1[1] * e2[0];
+            const float len = std::sqrt((fn[0] * fn[0] + fn[1] * fn[1]) + fn[2] * fn[2]);
+            for (int a = 0; a < 3; a++)
+                fn[a] = len > 0.0f ? fn[a] / len : 0.0f;
+            for (int c = 0; c < 3; c++) {
+                const uint32_t ti = f.corners[c][1], ni = f.corners[c][2];
+                float v[PT_VERTEX_FLOATS] = {p[c][0], p[c][1], p[c][2], fn[0], fn[1], fn[2], 0.0f, 0.0f};
+                if (ni != ~0u)
+                    for (int a = 0; a < 3; a++)
+                        v[3 + a] = nrm[3 * (size_t)ni + a];
+                if (ti != ~0u) {
+                    v[6] = uv[2 * (size_t)ti];
+                    v[7] = 1.0f - uv[2 * (size_t)ti + 1];
+                }
+                md.indices.push_back((uint32_t)(md.vertices.size() / PT_VERTEX_FLOATS) - range.vertex_offset);
+                md.vertices.insert(md.vertices.end(), v, v + PT_VERTEX_FLOATS);
+            }
+        }
+        md.meshes.push_back(range);
+        md.mesh_material.push_back(mi);
+        md.mesh_instances.push_back({Mat4::identity()});
+    }
+    for (const auto& tf : tex_files) {
+        std::string f = read_file(dir + tf.first);
+        md.textures.push_back(decode_texture(std::vector<uint8_t>(f.begin(), f.end()), tf.first, tf.second));
+    }
+    mark_transparency(md);
+    return md;
+}
+
+// Model import by file extension: .obj (Wavefront + MTL), otherwise glTF 2.0.
+Model load_model(const std::string& path)
+{
+    std::string ext;
+    const size_t dot = path.find_last_of('.');
+    if (dot != std::string::npos)
+        for (char c : path.substr(dot + 1))
+            ext += (char)std::tolower((unsigned char)c);
+    return ext == "obj" ? load_obj(path) : load_gltf(path);
 }
 
 // ---------------------------------------------------------------- 4x4 inverse (FP64 cofactors)
@@ -982,7 +1308,7 @@ pt_host_scene* load_scn(const std::string& path)
     for (const Subscene& s : subs) {
         if (s.instances.empty())
             continue;
-        Model md = load_gltf(dir + s.path);
+        Model md = load_model(dir + s.path);
         host->append_model(md, s.instances);
     }
     return host.release();

@@ -278,3 +278,56 @@ def test_textured_pack_matches_oracle():
         else:
             assert a[k] == b[k], k
     assert a["textures"].size == 6 * len(raw["textures"]) and a["texels"].size == sum(t.size for t, _ in raw["textures"])
+
+
+def _bits(f):
+    return int(np.float32(f).view(np.uint32))
+
+
+def test_obj_import(tmp_path):
+    """Wavefront OBJ + MTL with the reference's Assimp material keys: one
+    mesh per object/group/material run, fan triangulation, negative indices,
+    v flipped, flat normals where faces have none, Kd/Ke sRGB-decoded, d as
+    opacity (transparency bit), Pr/Pm factors, maps in first-use order."""
+    (tmp_path / "rm.png").write_bytes(scenes.png_bytes(np.full((2, 2, 4), 200, np.uint8)))
+    (tmp_path / "kd.png").write_bytes(scenes.png_bytes(np.full((2, 2, 3), 90, np.uint8)))
+    (tmp_path / "m.mtl").write_text(
+        "newmtl red\nKd 0.5 0.25 0.125\nd 0.5\nPr 0.3\nPm 1\n"
+        "newmtl glow\nKd 0 0 0\nKe 1 0.5 0\n"
+        "newmtl tex\nmap_Kd kd.png\nmap_Pr rm.png\nmap_Pm rm.png\n")
+    (tmp_path / "o.obj").write_text(
+        "mtllib m.mtl\n"
+        "v 0 0 0\nv 1 0 0\nv 1 0 1\nv 0 0 1\n"
+        "vt 0 0\nvt 1 0\nvt 1 0.25\nvt 0 1\n"
+        "vn 0 1 0\n"
+        "f 1/1 2/2 3/3 4/4\n"           # default material, quad -> 2 triangles, flat normals
+        "usemtl red\nf -4//1 -3//1 -2//1\n"  # negative indices, given normal
+        "o second\nusemtl glow\nf 1 3 2\n"
+        "usemtl tex\nf 1/1 2/2 3/3\n")
+    hs = P.HostScene.load(scn(tmp_path, "camera:\n\nobjects:\nob o.obj\nob\n"))
+    raw = hs.raw()
+    meshes = raw["meshes"]
+    assert meshes.shape[0] == 4 and meshes[:, 2].tolist() == [2, 1, 1, 1]
+    v = raw["vertices"]
+    first = v[meshes[0, 0]:meshes[0, 0] + 6]
+    assert np.allclose(first[:, 3:6], [0, -1, 0]) or np.allclose(first[:, 3:6], [0, 1, 0])
+    assert np.allclose(first[:3, 7], [1, 1, 0.75])  # 1 - v
+    assert np.array_equal(first[3:, 0:3], np.array([[0, 0, 0], [1, 0, 1], [0, 0, 1]], np.float32))  # fan (0, 2, 3)
+    mats = raw["materials"]
+    mm = raw["mesh_material"]
+    default, red, glow, tex = (mats[i] for i in mm)
+    assert np.allclose(default[0:4], [P.abi.lib().pt_from_srgb(0.6)] * 3 + [1.0])
+    assert red[0] == np.float32(P.abi.lib().pt_from_srgb(0.5)) and red[3] == 0.5
+    assert (_bits(red[11]) & abi.PT_MATERIAL_IS_TRANSPARENT_BIT) and red[8] == np.float32(0.3) and red[9] == 1.0
+    assert glow[4] == 1.0 and glow[5] == np.float32(P.abi.lib().pt_from_srgb(0.5)) and glow[7] == 1.0
+    tb = _bits(tex[11])
+    assert tb & abi.PT_BASE_COLOUR_MAP_BIT and tb & abi.PT_ROUGHNESS_METALNESS_MAP_BIT
+    assert (_bits(tex[0]), _bits(tex[8])) == (0, 1)
+    t = raw["textures"]
+    assert len(t) == 2 and t[0][1] is True and t[0][0].shape == (2, 2, 4) and t[1][1] is False
+    assert "2 textures" in hs.details()
+
+
+def test_obj_errors(tmp_path):
+    (tmp_path / "bad.obj").write_text("v 0 0 0\nf 1 2 3\n")
+    assert "missing position" in load_error(scn(tmp_path, "camera:\n\nobjects:\nb bad.obj\nb\n"))
