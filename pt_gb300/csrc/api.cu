@@ -602,9 +602,14 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     uint32_t kernel = p->kernel == PT_KERNEL_MEGA ? PT_KERNEL_MEGA : PT_KERNEL_WAVEFRONT;
     uint32_t launches = 0;
     if (kernel == PT_KERNEL_WAVEFRONT) {
-        // Waves of k samples, k * pixels <= 2^23 paths (at least one sample):
-        // ~1.6 GB of path state keeps the tail segments of a wave busy.
-        uint64_t k = std::max<uint64_t>(1, std::min<uint64_t>(p->samples, (1ull << 23) / pixels));
+        // Waves of k samples, k * pixels <= 2^n paths (at least one sample),
+        // n = PT_WAVE_PATHS_LOG2 (20..26, default 23: ~1.9 GB of path state).
+        static const int wave_log2 = [] {
+            const char* e = std::getenv("PT_WAVE_PATHS_LOG2");
+            const int v = e ? std::atoi(e) : 23;
+            return v < 20 ? 20 : (v > 26 ? 26 : v);
+        }();
+        uint64_t k = std::max<uint64_t>(1, std::min<uint64_t>(p->samples, (1ull << wave_log2) / pixels));
         uint64_t n = k * pixels;
         if (c->wave_paths < n) {
             cudaError_t e = c->wave_state.alloc(wave_state_bytes((uint32_t)n));
