@@ -603,11 +603,11 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     uint32_t launches = 0;
     if (kernel == PT_KERNEL_WAVEFRONT) {
         // Waves of k samples, k * pixels <= 2^n paths (at least one sample),
-        // n = PT_WAVE_PATHS_LOG2 (20..26, default 23: ~1.9 GB of path state).
+        // n = PT_WAVE_PATHS_LOG2 (20..27, default 23: ~1.9 GB of path state).
         static const int wave_log2 = [] {
             const char* e = std::getenv("PT_WAVE_PATHS_LOG2");
             const int v = e ? std::atoi(e) : 23;
-            return v < 20 ? 20 : (v > 26 ? 26 : v);
+            return v < 20 ? 20 : (v > 27 ? 27 : v);
         }();
         uint64_t k = std::max<uint64_t>(1, std::min<uint64_t>(p->samples, (1ull << wave_log2) / pixels));
         uint64_t n = k * pixels;
