@@ -324,7 +324,8 @@ int pt_mse_noalloc(const float* image_rgba, const float* reference_rgba, uint32_
  * CUDA graph and launched as one unit, and small jobs may instead run as
  * megakernel launches on a parallel branch of the same graph.  An autotuner
  * times short trial batches (every job at 1/32 of its samples, at least one)
- * and picks the wave capacity (paths in flight), the megakernel tile and the
+ * and picks the wave capacity (2^21, 2^23 or 2^25 paths in flight, within a
+ * quarter of the free device memory), the megakernel tile and the
  * work size below which a job runs on the megakernel; its choice is cached
  * per batch.  Every job's image equals, bit for bit, rendering that job alone
  * with pt_render.  The reference renders one scene per process and has no
@@ -339,7 +340,7 @@ typedef struct pt_batch_job {
 #define PT_BATCH_NO_TUNE 1u  /* skip the tuner: every AUTO job on the wavefront, 2^23 paths per wave */
 #define PT_BATCH_NO_GRAPH 2u /* issue the launch sequence directly instead of through a CUDA graph */
 #define PT_BATCH_RETUNE 4u   /* ignore the tuning cache */
-/* Fixes the wave capacity at 2^n paths (10 <= n <= 23) instead of tuning it. */
+/* Fixes the wave capacity at 2^n paths (10 <= n <= 25) instead of tuning it. */
 #define PT_BATCH_CAPACITY_LOG2(n) ((uint32_t)(n) << 8)
 
 typedef struct pt_batch_stats {

@@ -12,7 +12,7 @@
 //
 // The autotuner times trial batches (each job at 1/32 of its samples, at
 // least 1) for a few candidate settings and keeps the fastest, per batch:
-//   1. wave capacity 2^21, 2^22, 2^23 paths (all jobs on the wavefront);
+//   1. wave capacity 2^21, 2^23, 2^25 paths (all jobs on the wavefront);
 //   2. megakernel threshold 0, 2^18, 2^21 on a job's trial work, pixels x
 //      trial samples x (bounces + 1) (tile 16x8);
 //   3. if a threshold won: megakernel tile 8x16 or 32x4 against 16x8.
@@ -343,9 +343,16 @@ int tune(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vector<p
         max_px = std::max<uint64_t>(max_px, (uint64_t)q.width * q.height);
     float best_ms = 0.0f;
     bool have = false;
+    // capacities whose path state would take more than a quarter of the free memory are skipped
+    size_t free_b = 0, total_b = 0;
+    uint64_t mem_paths = ~0ull;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+        mem_paths = ((uint64_t)free_b + (uint64_t)b->state.n) / 4 / (wave_state_bytes(1u << 20) >> 20);
     auto consider = [&](const BatchChoice& ch) -> int {
         if (max_px > ch.capacity)
             return PT_OK; // the largest job would not fit a wave
+        if (ch.capacity > mem_paths && ch.capacity > (1u << 21))
+            return PT_OK;
         float ms = 0.0f;
         int rc = trial(c, b, jobs, tp, ch, ms);
         if (rc != PT_OK)
@@ -358,7 +365,7 @@ int tune(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vector<p
         return PT_OK;
     };
     int rc;
-    for (uint32_t lg : {21u, 22u, 23u}) {
+    for (uint32_t lg : {21u, 23u, 25u}) {
         BatchChoice ch;
         ch.capacity = fixed_capacity ? fixed_capacity : 1u << lg;
         if ((rc = consider(ch)) != PT_OK)
@@ -401,8 +408,8 @@ int pt_render_batch(pt_ctx* c, const pt_batch_job* jobs, uint32_t count, uint32_
     if (flags & ~(PT_BATCH_NO_TUNE | PT_BATCH_NO_GRAPH | PT_BATCH_RETUNE | PT_BATCH_CAPACITY_LOG2(31)))
         return c->fail(PT_ERR_INVALID, "unknown batch flags");
     const uint32_t cap_log2 = (flags >> 8) & 31u;
-    if (cap_log2 && (cap_log2 < 10 || cap_log2 > 23))
-        return c->fail(PT_ERR_INVALID, "wave capacity must be 2^10 .. 2^23 paths");
+    if (cap_log2 && (cap_log2 < 10 || cap_log2 > 25))
+        return c->fail(PT_ERR_INVALID, "wave capacity must be 2^10 .. 2^25 paths");
     const uint32_t fixed_capacity = cap_log2 ? 1u << cap_log2 : 0u;
     cudaSetDevice(c->device);
     std::vector<pt_render_params> p(count);
@@ -416,8 +423,8 @@ int pt_render_batch(pt_ctx* c, const pt_batch_job* jobs, uint32_t count, uint32_
             return c->fail(PT_ERR_INVALID, at + "scene on another device");
         if (q.width == 0 || q.height == 0 || q.samples == 0)
             return c->fail(PT_ERR_INVALID, at + "zero width, height or sample count");
-        if ((uint64_t)q.width * q.height > (1ull << 23))
-            return c->fail(PT_ERR_UNSUPPORTED, at + "more than 2^23 pixels");
+        if ((uint64_t)q.width * q.height > (1ull << 25))
+            return c->fail(PT_ERR_UNSUPPORTED, at + "more than 2^25 pixels");
         if (q.sample_index != 0 || q.flags != 0)
             return c->fail(PT_ERR_INVALID, at + "batch jobs start at sample 0 and take no flags");
         if (q.accum_mode > PT_ACCUM_FP32_FP64 || q.kernel > PT_KERNEL_WAVEFRONT)
