@@ -233,7 +233,8 @@ int prepare(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vecto
         e = b->jobs.alloc(args.size());
     if (e == cudaSuccess && b->shares.n < std::max<size_t>(plan.shares.size(), 1))
         e = b->shares.alloc(std::max<size_t>(plan.shares.size(), 1));
-    if (e == cudaSuccess && !plan.waves.empty() && b->state_paths < capacity) {
+    // the state is sized to the capacity exactly: a wave's arrays stay close together
+    if (e == cudaSuccess && !plan.waves.empty() && b->state_paths != capacity) {
         b->state.release();
         b->path_share.release();
         e = b->state.alloc(wave_state_bytes(capacity));
