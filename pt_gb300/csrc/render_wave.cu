@@ -56,7 +56,7 @@ struct OneJob {
     __device__ __forceinline__ const RenderArgs& args(uint32_t) const { return r; }
     __device__ __forceinline__ unsigned long long* counters() const { return r.counters; }
     __device__ __forceinline__ uint32_t accum_threads() const { return pixels; }
-    // one job's share: its args, pixel, first path id, pixels, first sample, samples
+    // the share (the whole wave) and the pixel of accumulation thread t
     __device__ __forceinline__ const WaveShare share_of_pixel(uint32_t t, uint32_t& pix) const
     {
         pix = t;
@@ -142,7 +142,6 @@ struct WaveArgs {
     Src src;
     WaveState w;
 };
-
 
 // Two queue pushes for a whole block at once: one atomic per queue per block.
 // Every thread of the block must call it (block-uniform control flow).
