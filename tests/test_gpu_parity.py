@@ -205,17 +205,41 @@ def test_invalid_calls(ctx):
     fresh.close()
 
 
-def test_wavefront_many_waves(ctx, small):
-    """More samples than one wave holds: waves must chain in sample order."""
+_MANY_WAVES = """
+import sys, numpy as np, pathlib
+import pt_gb300 as P
+from pt_gb300 import abi, scenes
+hs = P.HostScene.load(scenes.small_scene(pathlib.Path(sys.argv[1]), seed=0))
+ctx = P.Context(0)
+ctx.upload(hs.pack())
+ctx.build_accel()
+st = ctx.render(hs.render_params(1024, 1024, 3, 3, kernel=abi.PT_KERNEL_WAVEFRONT))
+assert st.error_word == 0 and st.paths == 3 * 1024 * 1024, (st.error_word, st.paths)
+np.save(sys.argv[2], ctx.read_image())
+print("launches", st.kernel_launches)
+"""
+
+
+def test_wavefront_many_waves(ctx, small, tmp_path):
+    """More samples than one wave holds: waves must chain in sample order.
+    The child process caps waves at 2^20 paths (PT_WAVE_PATHS_LOG2, read once
+    per process), so 3 samples of 1024^2 pixels take three waves."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    out = tmp_path / "waves.npy"
+    env = dict(os.environ, PT_WAVE_PATHS_LOG2="20")
+    root = Path(__file__).resolve().parent.parent
+    r = subprocess.run([sys.executable, "-c", _MANY_WAVES, str(tmp_path / "scene"), str(out)], env=env, cwd=root,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "launches" in r.stdout and int(r.stdout.split()[-1]) == 3 * (2 + 5 * 4)  # 3 waves of 4 segments
+    gpu = np.load(out)
     hs, view = small
-    params = hs.render_params(1024, 1024, 3, 3, kernel=abi.PT_KERNEL_WAVEFRONT)
     ctx.upload(view)
     ctx.build_accel()
-    st = ctx.render(params)
-    assert st.error_word == 0 and st.paths == 3 * 1024 * 1024
-    gpu = ctx.read_image()
-    params.kernel = abi.PT_KERNEL_MEGA
-    ctx.render(params)
+    ctx.render(hs.render_params(1024, 1024, 3, 3, kernel=abi.PT_KERNEL_MEGA))
     mega = ctx.read_image()
     assert np.array_equal(gpu.view(np.uint32), mega.view(np.uint32))
 
