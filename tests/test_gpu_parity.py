@@ -107,6 +107,37 @@ def test_textured_scene_bitexact(ctx, textured, kernel):
     assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
 
 
+def test_obj_scene_bitexact(ctx, kernel, tmp_path):
+    """A Wavefront OBJ scene with MTL materials, a base-colour map, a quad
+    emitter and polygons fanned into triangles, through the loader."""
+    rng = np.random.default_rng(9)
+    (tmp_path / "kd.png").write_bytes(scenes.png_bytes(rng.integers(0, 256, (8, 8, 3), dtype=np.uint8)))
+    (tmp_path / "m.mtl").write_text("newmtl floor\nmap_Kd kd.png\nPr 0.4\n"
+                                    "newmtl gold\nKd 0.9 0.7 0.3\nPm 1\nPr 0.2\n"
+                                    "newmtl lamp\nKd 0 0 0\nKe 1 0.9 0.8\n")
+    sphere = scenes.icosphere(2)
+    lines = ["mtllib m.mtl", "v -3 0 -3", "v 3 0 -3", "v 3 0 3", "v -3 0 3", "vt 0 0", "vt 2 0", "vt 2 2", "vt 0 2",
+             "usemtl floor", "f 1/1 4/4 3/3 2/2"]
+    base = 5
+    for p_ in sphere[0]:
+        lines.append(f"v {p_[0] * 0.8:.6f} {p_[1] * 0.8 + 0.9:.6f} {p_[2] * 0.8:.6f}")
+    for n_ in sphere[1]:
+        lines.append(f"vn {n_[0]:.6f} {n_[1]:.6f} {n_[2]:.6f}")
+    lines.append("o ball\nusemtl gold")
+    for a, b, c in sphere[3]:
+        lines.append(f"f {a + base}//{a + 1} {b + base}//{b + 1} {c + base}//{c + 1}")
+    lines += ["o lamp", "usemtl lamp", "v -0.7 3 -0.7", "v 0.7 3 -0.7", "v 0.7 3 0.7", "v -0.7 3 0.7", "f -1 -2 -3 -4"]
+    (tmp_path / "s.obj").write_text("\n".join(lines) + "\n")
+    (tmp_path / "s.scn").write_text("camera:\nposition 0 -2 -6\nlookdir 0 1.5 6\nfov 50\n\nobjects:\nsc s.obj\nsc\n"
+                                    "envcol 0.1 0.12 0.2\n")
+    hs = P.HostScene.load(tmp_path / "s.scn")
+    view = hs.pack()
+    params = hs.render_params(64, 48, 4, 6, kernel=kernel)
+    gpu, ref, st, ost = _render_both(ctx, view, params)
+    _assert_bitexact(gpu, ref)
+    assert st.segments == ost.segments and gpu[..., :3].max() > 0
+
+
 def test_progressive_equals_single_call(ctx, small, kernel):
     """Rendering spp in several calls gives the same running mean as one call
     (the reference dispatches one sample per submission, ptdispatch.cpp:101)."""
