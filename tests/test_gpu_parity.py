@@ -126,7 +126,7 @@ def test_obj_scene_bitexact(ctx, kernel, tmp_path):
     lines.append("o ball\nusemtl gold")
     for a, b, c in sphere[3]:
         lines.append(f"f {a + base}//{a + 1} {b + base}//{b + 1} {c + base}//{c + 1}")
-    lines += ["o lamp", "usemtl lamp", "v -0.7 3 -0.7", "v 0.7 3 -0.7", "v 0.7 3 0.7", "v -0.7 3 0.7", "f -1 -2 -3 -4"]
+    lines += ["o lamp", "usemtl lamp", "v -0.7 3 -0.7", "v 0.7 3 -0.7", "v 0.7 3 0.7", "v -0.7 3 0.7", "f -4 -3 -2 -1"]
     (tmp_path / "s.obj").write_text("\n".join(lines) + "\n")
     (tmp_path / "s.scn").write_text("camera:\nposition 0 -2 -6\nlookdir 0 1.5 6\nfov 50\n\nobjects:\nsc s.obj\nsc\n"
                                     "envcol 0.1 0.12 0.2\n")
