@@ -720,7 +720,9 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
             stats->stage_launches += sg == 1 ? 1u : 0u;
         }
         if (ew != 0)
-            return c->fail(PT_ERR_DEVICE, "device error word " + std::to_string(ew));
+            return c->fail((ew & ERR_WATCHDOG) ? PT_ERR_TIMEOUT : PT_ERR_DEVICE,
+                          std::string((ew & ERR_WATCHDOG) ? "traversal iteration cap hit" : "device error") + " (error word " +
+                              std::to_string(ew) + ")");
     }
     return PT_OK;
 }

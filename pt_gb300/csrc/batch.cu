@@ -573,7 +573,9 @@ int pt_render_batch(pt_ctx* c, const pt_batch_job* jobs, uint32_t count, uint32_
         stats->error_word = ew;
     }
     if (ew != 0)
-        return c->fail(PT_ERR_DEVICE, "device error word " + std::to_string(ew));
+        return c->fail((ew & ERR_WATCHDOG) ? PT_ERR_TIMEOUT : PT_ERR_DEVICE,
+                      std::string((ew & ERR_WATCHDOG) ? "traversal iteration cap hit" : "device error") + " (error word " +
+                          std::to_string(ew) + ")");
     return PT_OK;
 }
 
