@@ -2005,10 +2005,18 @@ or_scene* or_scene_create(const pt_scene_view* v, int brute_force)
                 for (int c = 0; c < 4; c++)
                     in.w2o[r][c] = (float)inv[r][c];
         }
-        // world box: transform the 8 corners of the padded mesh box in FP64
+        // world box: transform the 8 corners of the padded mesh box in FP64;
+        // a mesh without triangles is a point at the instance origin
         const Box& mb = mesh_box[in.mesh];
         Box wb;
         wb.reset();
+        if (v->meshes[in.mesh].tri_count == 0) {
+            const float o[3] = {in.data.transform[0][3], in.data.transform[1][3], in.data.transform[2][3]};
+            wb.grow(o);
+            inst_boxes[i] = wb;
+            in.world_box = wb;
+            continue;
+        }
         for (int corner = 0; corner < 8; corner++) {
             double p[3] = {(corner & 1) ? mb.hi[0] : mb.lo[0], (corner & 2) ? mb.hi[1] : mb.lo[1], (corner & 4) ? mb.hi[2] : mb.lo[2]};
             float w[3];
