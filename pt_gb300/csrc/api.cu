@@ -315,6 +315,13 @@ int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
     if (v->light_count > 0 && v->light_word_count < v->light_count * PT_LIGHT_BIN_SIZE)
         return c->fail(PT_ERR_INVALID, "light stream shorter than its top-level table");
     // meshes
+    // non-finite positions would give the BVH build NaN boxes (no consistent
+    // merge order) and the light tables NaN weights: rejected up front
+    for (uint64_t i = 0; i < v->vertex_count; i++) {
+        const float* f = v->vertices + i * PT_VERTEX_FLOATS;
+        if (!std::isfinite(f[0]) || !std::isfinite(f[1]) || !std::isfinite(f[2]))
+            return c->fail(PT_ERR_INVALID, "vertex " + std::to_string(i) + " has a non-finite position");
+    }
     std::vector<uint32_t> vo(v->mesh_count), io(v->mesh_count), tb(v->mesh_count + 1);
     uint64_t tris = 0;
     for (uint32_t m = 0; m < v->mesh_count; m++) {
@@ -519,6 +526,14 @@ RenderArgs render_args(const pt_ctx* c, const pt_render_params* p, bool fp64)
     // A traversal of a valid BVH visits each node at most once; the cap only
     // stops a malformed tree from spinning.
     a.s.max_iterations = 4u * (uint32_t)std::min<size_t>(c->nodes.n + c->tri_count + c->instance_count, 1u << 28) + 4096u;
+    // PT_TRAVERSAL_CAP lowers the cap (tests make the watchdog fire with it: a
+    // traversal that reaches the cap stops and reports PT_ERR_TIMEOUT)
+    static const uint32_t cap = [] {
+        const char* e = std::getenv("PT_TRAVERSAL_CAP");
+        return e ? (uint32_t)std::max(1, std::atoi(e)) : 0u;
+    }();
+    if (cap)
+        a.s.max_iterations = std::min(a.s.max_iterations, cap);
     a.s.nodes = c->nodes.p;
     a.s.tris = c->tris.p;
     a.s.dinst = c->dinst.p;
