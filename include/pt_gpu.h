@@ -281,6 +281,18 @@ int pt_render_next(pt_ctx* ctx, uint32_t samples, pt_render_stats* stats_out);
 #define PT_IMAGE_SUMS64 3
 int pt_read_image(pt_ctx* ctx, void* rgba, size_t pitch_bytes, int fp64);
 
+/* Checkpoint / resume of long progressive renders (no reference
+ * counterpart: the reference keeps its running mean only in device memory).
+ * A checkpoint is pt_read_image (the FP32 running mean, and PT_IMAGE_SUMS64
+ * for renders with FP64 sums) after `samples_done` samples; pt_restore_image
+ * puts both back into a context (same or new), after which pt_render with
+ * sample_index = samples_done continues the image exactly as if it had
+ * never stopped (the per-sample values depend only on pixel and sample
+ * index).  sums64 may be NULL for FP32-only renders; pitch is the rgba rows'
+ * byte stride; sums64 rows are packed (4 doubles per pixel). */
+int pt_restore_image(pt_ctx* ctx, const float* rgba, size_t pitch_bytes, const double* sums64, uint32_t width,
+                     uint32_t height, uint32_t samples_done);
+
 /* Wait for all work of the context. */
 int pt_synchronize(pt_ctx* ctx);
 

@@ -157,6 +157,8 @@ SIGNATURES = [
     ("pt_render_next", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(RenderStats)]),
     ("pt_read_image", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]),
     ("pt_synchronize", C.c_int, [C.c_void_p]),
+    ("pt_restore_image", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_size_t, C.POINTER(C.c_double), C.c_uint32,
+                                   C.c_uint32, C.c_uint32]),
     ("pt_tonemap", C.c_int, [C.c_void_p]),
     ("pt_mse_host", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     ("pt_mse_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),

@@ -159,6 +159,16 @@ class Context:
         _check(lib().pt_read_image(self._h, out.ctypes.data, out.strides[0], 1 if fp64 else 0), self._h)
         return out
 
+    def restore_image(self, rgba: np.ndarray, samples_done: int, sums64: np.ndarray | None = None) -> None:
+        """Puts a checkpoint (read_image(), and read_image sums for FP64
+        renders) back; render from sample_index = samples_done to resume."""
+        img = np.ascontiguousarray(rgba, np.float32)
+        h, w = img.shape[:2]
+        s64 = None if sums64 is None else np.ascontiguousarray(sums64, np.float64)
+        _check(lib().pt_restore_image(self._h, _ptr(img, C.c_float), img.strides[0],
+                                      None if s64 is None else _ptr(s64, C.c_double), w, h, samples_done), self._h)
+        self.width, self.height = w, h
+
     def read_denoised(self, out: np.ndarray | None = None) -> np.ndarray:
         """The image of the last denoise() (RGBA float32)."""
         if out is None:

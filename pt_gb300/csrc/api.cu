@@ -742,6 +742,35 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     return PT_OK;
 }
 
+int pt_restore_image(pt_ctx* c, const float* rgba, size_t pitch, const double* sums64, uint32_t width, uint32_t height,
+                     uint32_t samples_done)
+{
+    if (!c || !rgba || width == 0 || height == 0 || samples_done == 0)
+        return PT_ERR_INVALID;
+    if ((uint64_t)width * height > (1ull << 31))
+        return c->fail(PT_ERR_UNSUPPORTED, "image larger than 2^31 pixels");
+    if (pitch < (size_t)width * 16)
+        return c->fail(PT_ERR_INVALID, "pitch smaller than a row");
+    cudaSetDevice(c->device);
+    if (!sums64)
+        c->sum64.release(); // no stale sums behind a restored FP32-only image
+    int rc = ensure_image(c, width, height, sums64 != nullptr, false);
+    if (rc != PT_OK)
+        return rc;
+    cudaError_t e = cudaMemcpy2DAsync(c->image.p, (size_t)width * 16, rgba, pitch, (size_t)width * 16, height,
+                                      cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && sums64)
+        e = cudaMemcpyAsync(c->sum64.p, sums64, (size_t)width * height * 4 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+        return c->cuda_fail(e, "image restore");
+    c->samples_done = samples_done;
+    c->have_fp64 = sums64 != nullptr;
+    c->image_epoch++;
+    return PT_OK;
+}
+
 int pt_set_camera(pt_ctx* c, const pt_render_params* p)
 {
     if (!c || !p)

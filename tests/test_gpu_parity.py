@@ -197,6 +197,30 @@ def test_replica_ranges_merge_to_one_render(ctx, small):
     np.testing.assert_allclose(merged[..., :3], single[..., :3], rtol=1e-12, atol=1e-12)
 
 
+def test_checkpoint_resume_is_exact(ctx, small):
+    """A render stopped after 3 samples, its image and FP64 sums restored into
+    a fresh context, and continued for 4 more equals 7 samples in one call."""
+    from pt_gb300 import replicas
+    hs, view = small
+    ctx.upload(view)
+    ctx.build_accel()
+    full = hs.render_params(40, 32, 7, 5, accum_mode=abi.PT_ACCUM_FP32_FP64)
+    ctx.render(full)
+    want, want64 = ctx.read_image().copy(), replicas.read_sums(ctx)
+    ctx.render(hs.render_params(40, 32, 3, 5, accum_mode=abi.PT_ACCUM_FP32_FP64))
+    ckpt, ckpt64 = ctx.read_image().copy(), replicas.read_sums(ctx)
+    fresh = P.Context(0)
+    fresh.upload(view)
+    fresh.build_accel()
+    fresh.restore_image(ckpt, 3, ckpt64)
+    fresh.render(hs.render_params(40, 32, 4, 5, sample_index=3, accum_mode=abi.PT_ACCUM_FP32_FP64))
+    assert np.array_equal(fresh.read_image().view(np.uint32), want.view(np.uint32))
+    got64 = replicas.read_sums(fresh)
+    assert np.array_equal(got64[..., 3], want64[..., 3])
+    np.testing.assert_allclose(got64[..., :3], want64[..., :3], rtol=1e-15, atol=0)
+    fresh.close()
+
+
 def test_deterministic(ctx, small):
     hs, view = small
     params = hs.render_params(64, 48, 3, 8)
