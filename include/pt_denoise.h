@@ -74,6 +74,12 @@ int pt_unet_forward(pt_unet* u, float* output, void* stream);
 int pt_unet_backward(pt_unet* u, const float* target, double* loss, void* stream);
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) with learning rate lr. */
 int pt_unet_adam(pt_unet* u, float lr, void* stream);
+/* Optimizer state for training checkpoints: the first and second Adam
+ * moments (fp32, parameter order, `count` = pt_unet_param_count()) and the
+ * number of Adam steps taken (bias correction).  pt_unet_set_params clears
+ * the state, so a resume sets the parameters first and the state second. */
+int pt_unet_get_adam_state(pt_unet* u, float* m, float* v, size_t count, uint32_t* step);
+int pt_unet_set_adam_state(pt_unet* u, const float* m, const float* v, size_t count, uint32_t step);
 
 /* Single layers, for tests.  `in` is bf16 [n][h][w][in_pitch] read at
  * channels [c0, c0 + c_in); `weights` fp32 [9][c_in][c_out] (device).

@@ -197,6 +197,10 @@ SIGNATURES = [
     ("pt_unet_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("pt_unet_backward", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
     ("pt_unet_adam", C.c_int, [C.c_void_p, C.c_float, C.c_void_p]),
+    ("pt_unet_get_adam_state", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_size_t,
+                                         C.POINTER(C.c_uint32)]),
+    ("pt_unet_set_adam_state", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_size_t,
+                                         C.c_uint32]),
     ("pt_nn_conv3x3", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                 C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p, C.c_void_p]),
     ("pt_nn_conv3x3_dgrad", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32,

@@ -177,6 +177,20 @@ int pt_unet_get_grads(pt_unet* u, float* g, size_t count)
     return u->net.get_grads(g, count, u->err) ? PT_OK : PT_ERR_INVALID;
 }
 
+int pt_unet_get_adam_state(pt_unet* u, float* m, float* v, size_t count, uint32_t* step)
+{
+    if (!u || !m || !v || !step)
+        return PT_ERR_INVALID;
+    return u->net.get_adam_state(m, v, count, step, u->err) ? PT_OK : PT_ERR_INVALID;
+}
+
+int pt_unet_set_adam_state(pt_unet* u, const float* m, const float* v, size_t count, uint32_t step)
+{
+    if (!u || !m || !v)
+        return PT_ERR_INVALID;
+    return u->net.set_adam_state(m, v, count, step, u->err) ? PT_OK : PT_ERR_INVALID;
+}
+
 void pt_unet_shape(const pt_unet* u, uint32_t* batch, uint32_t* height, uint32_t* width)
 {
     if (batch)

@@ -248,6 +248,42 @@ bool UNet::get_grads(float* host, size_t count, std::string& err)
     return cudaMemcpy(host, grads_, count * sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
 }
 
+bool UNet::get_adam_state(float* m, float* v, size_t count, uint32_t* step, std::string& err)
+{
+    if (count != param_count()) {
+        err = "parameter count mismatch";
+        return false;
+    }
+    cudaSetDevice(device_);
+    if (cudaMemcpy(m, adam_m_, count * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(v, adam_v_, count * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        err = "optimizer state download failed";
+        return false;
+    }
+    *step = (uint32_t)adam_t_;
+    return true;
+}
+
+bool UNet::set_adam_state(const float* m, const float* v, size_t count, uint32_t step, std::string& err)
+{
+    if (count != param_count()) {
+        err = "parameter count mismatch";
+        return false;
+    }
+    if (step > (uint32_t)INT32_MAX) {
+        err = "optimizer step out of range";
+        return false;
+    }
+    cudaSetDevice(device_);
+    if (cudaMemcpy(adam_m_, m, count * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(adam_v_, v, count * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+        err = "optimizer state upload failed";
+        return false;
+    }
+    adam_t_ = (int)step;
+    return true;
+}
+
 uint32_t UNet::device_error()
 {
     uint32_t e = 0;

@@ -50,6 +50,9 @@ class UNet {
     bool set_params(const float* host, size_t count, std::string& err);
     bool get_params(float* host, size_t count, std::string& err);
     bool get_grads(float* host, size_t count, std::string& err);
+    // Adam moments (fp32, parameter order) and the number of steps taken.
+    bool get_adam_state(float* m, float* v, size_t count, uint32_t* step, std::string& err);
+    bool set_adam_state(const float* m, const float* v, size_t count, uint32_t step, std::string& err);
 
     // Input: bf16 [n][h][w][16] (device).  Output fp32 [n][h][w][16] in output().
     uint16_t* input() { return x0_.a.p; }

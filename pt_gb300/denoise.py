@@ -149,6 +149,21 @@ class UNet:
         self._check(self._lib.pt_unet_get_grads(self._h, g.ctypes.data_as(C.POINTER(C.c_float)), g.size))
         return g
 
+    def adam_state(self) -> tuple[np.ndarray, np.ndarray, int]:
+        """(first moments, second moments, Adam steps taken)."""
+        m, v = np.empty(param_count(), np.float32), np.empty(param_count(), np.float32)
+        t = C.c_uint32(0)
+        self._check(self._lib.pt_unet_get_adam_state(self._h, m.ctypes.data_as(C.POINTER(C.c_float)),
+                                                      v.ctypes.data_as(C.POINTER(C.c_float)), m.size, C.byref(t)))
+        return m, v, int(t.value)
+
+    def set_adam_state(self, m: np.ndarray, v: np.ndarray, step: int) -> None:
+        """Puts optimizer state back (after set_params, which clears it)."""
+        m = np.ascontiguousarray(m, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        self._check(self._lib.pt_unet_set_adam_state(self._h, m.ctypes.data_as(C.POINTER(C.c_float)),
+                                                      v.ctypes.data_as(C.POINTER(C.c_float)), m.size, step))
+
     def forward(self, output_ptr: int | None = None, stream: int | None = None) -> None:
         self._check(self._lib.pt_unet_forward(self._h, output_ptr, stream))
 

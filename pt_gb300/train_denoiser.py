@@ -11,6 +11,11 @@
    using the library's BF16 tensor-core forward and backward passes.
 3. Held-out scenes report the MSE of the noisy input and of the denoised
    output against their targets, per sample count.
+
+With --checkpoint PATH the parameters, Adam state, step and batch sampler
+RNG are saved every --checkpoint-every steps; a run started again with the
+same PATH and --resume continues from the last save (the training set is
+re-rendered, bit-identically, from its seeds).
 """
 from __future__ import annotations
 
@@ -25,7 +30,7 @@ import numpy as np
 from . import abi
 from .core import Context, HostScene
 from .denoise import WEIGHTS_DIR, UNet, init_params, save_params
-from . import trainset
+from . import checkpoint, trainset
 
 
 def render_set(ctx, seeds, size, target_spp, input_spps):
@@ -98,6 +103,9 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--init", type=str, default="", help="start from these parameters instead of a fresh init")
     ap.add_argument("--out", type=str, default=str(WEIGHTS_DIR / "unet.bin"))
+    ap.add_argument("--checkpoint", type=str, default="", help="training checkpoint file (.npz)")
+    ap.add_argument("--checkpoint-every", type=int, default=500)
+    ap.add_argument("--resume", action="store_true", help="continue from --checkpoint when it exists")
     args = ap.parse_args(argv)
     spps = [int(s) for s in args.input_spp.split(",")]
     k = len(spps)
@@ -115,9 +123,14 @@ def main(argv=None):
     net.set_params(params)
     tgt = torch.empty((args.batch, args.size, args.size, 4), dtype=torch.float32, device="cuda")
     gen = torch.Generator(device="cpu").manual_seed(args.seed)
+    first = 0
+    if args.resume and args.checkpoint and Path(args.checkpoint).exists():
+        first, rng, _ = checkpoint.load_training(args.checkpoint, net)
+        gen.set_state(torch.from_numpy(rng))
+        print(f"resumed from {args.checkpoint} at step {first}", flush=True)
     losses = []
     t1 = time.perf_counter()
-    for step in range(args.steps):
+    for step in range(first, args.steps):
         idx = torch.randint(0, X.shape[0], (args.batch,), generator=gen)
         net.input_tensor().copy_(X[idx.cuda()])
         net.base_tensor().copy_(B[idx.cuda()])
@@ -128,6 +141,8 @@ def main(argv=None):
         net.adam(lr)
         if step % 100 == 0 or step == args.steps - 1:
             print(f"step {step:5d} loss {np.mean(losses[-100:]):.5f} lr {lr:.2e}", flush=True)
+        if args.checkpoint and ((step + 1) % args.checkpoint_every == 0 or step == args.steps - 1):
+            checkpoint.save_training(args.checkpoint, net, step + 1, gen.get_state(), {"seed": args.seed})
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t1
     params = net.params()
@@ -140,8 +155,11 @@ def main(argv=None):
     res = evaluate(ev, Xe, Be, Ye, Ne, k, spps)
     summary = {"scenes": args.scenes, "size": args.size, "target_spp": args.target_spp, "input_spp": spps,
                "steps": args.steps, "batch": args.batch, "lr": args.lr, "data_seconds": round(t_data, 2),
-               "train_seconds": round(t_train, 2), "ms_per_step": round(1000 * t_train / max(1, args.steps), 3),
-               "final_loss": float(np.mean(losses[-100:])), "eval_mse": res}
+               "train_seconds": round(t_train, 2),
+               "ms_per_step": round(1000 * t_train / max(1, args.steps - first), 3),
+               "final_loss": float(np.mean(losses[-100:])) if losses else None, "eval_mse": res}
+    if first:
+        summary["resumed_at_step"] = first
     out.with_suffix(".json").write_text(json.dumps(summary, indent=1) + "\n")
     print(json.dumps(summary))
 
