@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define PT_ABI_VERSION 1
+#define PT_ABI_VERSION 2
 
 /* Status codes (0 = ok, < 0 = error class).  The reference throws
  * std::runtime_error instead (e.g. src/pathtrace/ptdispatch.cpp:44-47,127-128). */
@@ -144,6 +144,14 @@ typedef struct pt_scene_view {
     uint64_t texel_bytes;
     const pt_texture* textures;
     uint32_t texture_count;
+    /* Optional (NULL = none), material_count entries.  An extension of this
+     * library (the reference's materials have no refraction): a material
+     * whose entry is > 0 is a smooth dielectric of that index of refraction
+     * against vacuum.  It reflects or refracts by the exact Fresnel
+     * reflectance, tints refracted light by its base colour, takes no light
+     * samples (a delta BSDF, so emission reached through it counts in full),
+     * and is opaque to shadow rays.  Entries must be 0 or finite and >= 1. */
+    const float* material_ior;
 } pt_scene_view;
 
 /* Accumulation modes. */

@@ -45,6 +45,10 @@ typedef struct pt_raw_scene {
     uint64_t texel_bytes;
     const pt_texture* textures;
     uint32_t texture_count;
+    /* Optional (NULL = none), material_count entries: an index of refraction
+     * > 0 makes the material a smooth refractive dielectric (see
+     * pt_scene_view.material_ior); 0 keeps the reference's BSDF. */
+    const float* material_ior;
 } pt_raw_scene;
 
 /* Camera description as parsed from a .scn camera section

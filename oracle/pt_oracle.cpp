@@ -728,6 +728,7 @@ struct or_scene {
     bool brute = false;
     std::vector<uint8_t> texels;
     std::vector<pt_texture> textures;
+    std::vector<float> material_ior; // empty, or per material: > 0 = smooth dielectric
     float srgb[256]; // sRGB decode of 8-bit values, FP64 curve rounded once
     std::vector<Bvh> blas;
     Bvh tlas;
@@ -1256,6 +1257,40 @@ V3 light_contribution(const or_scene& s, const BrdfInput& bi, V3 o, V3 pt, const
     return (((w * emission) * brdf) * cos_theta(i)) / pdf;
 }
 
+// Smooth dielectric, this library's extension (the reference has no
+// refraction), restated from the Fresnel equations for unpolarised light:
+// with eta = n(viewer side) / n(far side), cos_t = sqrt(1 - eta^2 sin^2_i),
+// r_s = (eta cos_i - cos_t) / (eta cos_i + cos_t),
+// r_p = (cos_i - eta cos_t) / (cos_i + eta cos_t), F = (r_s^2 + r_p^2) / 2
+// (1 under total internal reflection).  Reflection with probability F,
+// else refraction t = -eta o_xy - cos_t z with throughput x tint x eta^2.
+void shade_dielectric(Payload& pl, V3 tint, float eta, V3 o, const V3 fw[3], V3 twn, V3 hit)
+{
+    const float cos_i = o.z;
+    const float sin2_t = (eta * eta) * (1.0f - cos_i * cos_i);
+    float F = 1.0f, cos_t = 0.0f;
+    if (sin2_t < 1.0f) {
+        cos_t = std::sqrt(1.0f - sin2_t);
+        const float rs = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+        const float rp = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
+        F = 0.5f * (rs * rs + rp * rp);
+    }
+    V3 i;
+    if (sample_1d(pl.smp) < F) {
+        i = v3(-o.x, -o.y, o.z);
+        pl.next_origin = hit + twn * ORIGIN_OFFSET;
+    } else {
+        i = v3(-eta * o.x, -eta * o.y, -cos_t);
+        pl.throughput = pl.throughput * (tint * (eta * eta));
+        pl.next_origin = hit - twn * ORIGIN_OFFSET;
+    }
+    pl.brdf_pdf = -1.0f; // delta lobe: the next emitter hit counts in full
+    const V3 &wx = fw[0], &wy = fw[1], &wn = fw[2];
+    V3 wi = v3((wx.x * i.x + wy.x * i.y) + wn.x * i.z, (wx.y * i.x + wy.y * i.y) + wn.y * i.z,
+               (wx.z * i.x + wy.z * i.y) + wn.z * i.z);
+    pl.next_dir = normalize(wi);
+}
+
 // pathtrace.ch.hlsl:227-360 for a hit; pathtrace.ms.hlsl for a miss.
 void shade(const or_scene& s, Payload& pl, V3 ray_o, V3 ray_d, const Hit& h, Stats& st)
 {
@@ -1344,7 +1379,8 @@ void shade(const or_scene& s, Payload& pl, V3 ray_o, V3 ray_d, const Hit& h, Sta
     V3 wx = normalize(mul3n(id.normal, tangent));
     V3 wy = normalize(mul3n(id.normal, bitangent));
     V3 wn = normalize(mul3n(id.normal, obj_normal));
-    if (dot(wn, ray_d) > 0.0f) {
+    const bool back_face = dot(wn, ray_d) > 0.0f;
+    if (back_face) {
         wx = -wx;
         wy = -wy;
         wn = -wn;
@@ -1371,7 +1407,13 @@ void shade(const or_scene& s, Payload& pl, V3 ray_o, V3 ray_d, const Hit& h, Sta
         pl.final_segment = true;
         return;
     }
-    V3 ip = (ray_o + ray_d * h.t) + twn * ORIGIN_OFFSET;
+    const V3 hit = ray_o + ray_d * h.t;
+    if (!s.material_ior.empty() && s.material_ior[id.material_index] > 0.0f) {
+        const float ior = s.material_ior[id.material_index];
+        shade_dielectric(pl, bi.base_colour, back_face ? ior : 1.0f / ior, o, fw, twn, hit);
+        return;
+    }
+    V3 ip = hit + twn * ORIGIN_OFFSET;
     add_radiance(pl, light_contribution(s, bi, o, ip, fw, pl, st));
 
     V3 m;
@@ -1690,6 +1732,7 @@ struct or_packed {
     float env[3] = {0, 0, 0};
     std::vector<uint8_t> texels;
     std::vector<pt_texture> textures;
+    std::vector<float> material_ior;
 };
 
 namespace {
@@ -1810,6 +1853,8 @@ or_packed* or_pack(const pt_raw_scene* raw)
         P->texels.assign(raw->texels, raw->texels + raw->texel_bytes);
         P->textures.assign(raw->textures, raw->textures + raw->texture_count);
     }
+    if (raw->material_ior)
+        P->material_ior.assign(raw->material_ior, raw->material_ior + raw->material_count);
 
     // scenebuffer.cpp:201-220
     uint32_t emitter_index = 0;
@@ -1938,6 +1983,7 @@ void or_packed_view(const or_packed* P, pt_scene_view* v)
     v->texel_bytes = P->texels.size();
     v->textures = P->textures.data();
     v->texture_count = (uint32_t)P->textures.size();
+    v->material_ior = P->material_ior.empty() ? nullptr : P->material_ior.data();
 }
 
 void or_packed_free(or_packed* p) { delete p; }
@@ -1958,6 +2004,8 @@ or_scene* or_scene_create(const pt_scene_view* v, int brute_force)
         s->texels.assign(v->texels, v->texels + v->texel_bytes);
         s->textures.assign(v->textures, v->textures + v->texture_count);
     }
+    if (v->material_ior)
+        s->material_ior.assign(v->material_ior, v->material_ior + v->material_count);
     for (int i = 0; i < 256; i++) {
         const double c = i / 255.0;
         s->srgb[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));

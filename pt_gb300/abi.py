@@ -11,6 +11,7 @@ from pathlib import Path
 
 _HERE = Path(__file__).resolve().parent
 LIB_PATH = _HERE / "_build" / "libptgpu.so"
+ABI_VERSION = 2  # PT_ABI_VERSION of include/pt_gpu.h that these declarations follow
 
 PT_OK = 0
 PT_ERR_INVALID = -1
@@ -76,7 +77,7 @@ class SceneView(C.Structure):
                 ("light_words", C.POINTER(C.c_uint32)), ("light_word_count", C.c_uint32), ("light_count", C.c_uint32),
                 ("environment_colour", C.c_float * 3),
                 ("texels", C.POINTER(C.c_uint8)), ("texel_bytes", C.c_uint64), ("textures", C.POINTER(Texture)),
-                ("texture_count", C.c_uint32)]
+                ("texture_count", C.c_uint32), ("material_ior", C.POINTER(C.c_float))]
 
 
 class RenderParams(C.Structure):
@@ -135,7 +136,7 @@ class RawScene(C.Structure):
                 ("directional_lights", C.POINTER(C.c_float)), ("directional_light_count", C.c_uint32),
                 ("environment_colour", C.c_float * 3),
                 ("texels", C.POINTER(C.c_uint8)), ("texel_bytes", C.c_uint64), ("textures", C.POINTER(Texture)),
-                ("texture_count", C.c_uint32)]
+                ("texture_count", C.c_uint32), ("material_ior", C.POINTER(C.c_float))]
 
 
 class CameraDesc(C.Structure):
@@ -244,6 +245,9 @@ def lib():
             f = getattr(L, name)
             f.restype = res
             f.argtypes = args
+        if L.pt_abi_version() != ABI_VERSION:
+            raise NativeLibraryMissing(f"{LIB_PATH} has ABI version {L.pt_abi_version()}, these bindings "
+                                       f"expect {ABI_VERSION}: rebuild it")
         _lib = L
     return _lib
 

@@ -344,6 +344,13 @@ def raw_to_struct(raw: dict):
         rs.texel_bytes = texels.size
         rs.textures = descs
         rs.texture_count = len(texs)
+    # refractive extension: raw["material_ior"] = float per material (0 = the reference's BSDF)
+    if raw.get("material_ior") is not None:
+        ior = np.ascontiguousarray(raw["material_ior"], np.float32).reshape(-1)
+        if ior.size != rs.material_count:
+            raise ValueError("material_ior needs one entry per material")
+        keep.append(ior)
+        rs.material_ior = _ptr(ior, C.c_float)
     return rs, keep
 
 
@@ -368,6 +375,7 @@ def struct_to_raw(rs: abi.RawScene) -> dict:
                           t.offset:t.offset + t.width * t.height * t.channels].reshape(
                           (t.height, t.width) if t.channels == 1 else (t.height, t.width, t.channels)).copy(), bool(t.srgb))
                      for t in (rs.textures[i] for i in range(rs.texture_count))],
+        "material_ior": a(rs.material_ior, rs.material_count, np.float32) if rs.material_ior else None,
     }
 
 
@@ -405,4 +413,5 @@ def view_arrays(v: abi.SceneView) -> dict:
         "env": np.array(list(v.environment_colour), np.float32),
         "texels": a(v.texels, v.texel_bytes, np.uint8),
         "textures": a(C.cast(v.textures, C.POINTER(C.c_uint32)), v.texture_count * 6, np.uint32),
+        "material_ior": a(v.material_ior, v.material_count, np.float32),
     }

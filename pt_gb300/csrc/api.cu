@@ -243,6 +243,8 @@ void pt_destroy(pt_ctx* c)
     c->indices.release();
     c->inst_data.release();
     c->materials.release();
+    c->material_ior.release();
+    c->has_ior = false;
     c->light.release();
     c->mesh_vertex_offset.release();
     c->mesh_index_offset.release();
@@ -351,6 +353,12 @@ int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
             t.offset + (uint64_t)t.width * t.height * t.channels > v->texel_bytes)
             return c->fail(PT_ERR_INVALID, "texture " + std::to_string(i) + " is malformed");
     }
+    if (v->material_ior)
+        for (uint32_t i = 0; i < v->material_count; i++) {
+            const float n = v->material_ior[i];
+            if (!(n == 0.0f || (n >= 1.0f && std::isfinite(n))))
+                return c->fail(PT_ERR_INVALID, "material " + std::to_string(i) + ": index of refraction must be 0 or >= 1");
+        }
     // instances
     c->h_dinst.assign(v->instance_count, DevInstance{});
     for (uint32_t i = 0; i < v->instance_count; i++) {
@@ -389,6 +397,7 @@ int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
         (e = upload(c, c->indices, v->indices, v->index_count)) != cudaSuccess ||
         (e = upload(c, c->inst_data, (const DevInstanceData*)v->instances, v->instance_count)) != cudaSuccess ||
         (e = upload(c, c->materials, (const DevMaterial*)v->materials, v->material_count)) != cudaSuccess ||
+        (e = upload(c, c->material_ior, v->material_ior, v->material_ior ? v->material_count : 0)) != cudaSuccess ||
         (e = upload(c, c->light, v->light_words, v->light_word_count)) != cudaSuccess ||
         (e = upload(c, c->mesh_vertex_offset, vo.data(), vo.size())) != cudaSuccess ||
         (e = upload(c, c->mesh_index_offset, io.data(), io.size())) != cudaSuccess ||
@@ -406,6 +415,7 @@ int pt_upload_scene(pt_ctx* c, const pt_scene_view* v)
     c->tri_count = (uint32_t)tris;
     c->instance_count = v->instance_count;
     c->material_count = v->material_count;
+    c->has_ior = v->material_ior != nullptr && v->material_count != 0;
     c->texture_count = v->texture_count;
     c->light_words = v->light_word_count;
     c->light_count = v->light_count;
@@ -515,6 +525,7 @@ RenderArgs render_args(const pt_ctx* c, const pt_render_params* p, bool fp64)
     a.s.indices = c->indices.p;
     a.s.inst_data = c->inst_data.p;
     a.s.materials = c->materials.p;
+    a.s.material_ior = c->has_ior ? c->material_ior.p : nullptr;
     a.s.light = c->light.p;
     a.s.light_words = c->light_words;
     a.s.light_count = c->light_count;

@@ -63,6 +63,8 @@ struct pt_ctx {
     DevBuf<uint32_t> indices;
     DevBuf<DevInstanceData> inst_data;
     DevBuf<DevMaterial> materials;
+    DevBuf<float> material_ior; // refractive extension; meaningful only when has_ior
+    bool has_ior = false;
     DevBuf<uint8_t> texels;
     DevBuf<DevTexture> textures;
     uint32_t texture_count = 0;

@@ -74,6 +74,7 @@ struct DevScene {
     const uint32_t* indices;
     const DevInstanceData* inst_data;
     const DevMaterial* materials;
+    const float* material_ior; // null, or per material: > 0 = smooth dielectric of that index
     const uint32_t* light;
     uint32_t light_words;
     uint32_t light_count;

@@ -294,6 +294,41 @@ __device__ __forceinline__ void shade_miss(const DevScene& s, PathState& pl)
     pl.final_segment = true;
 }
 
+// Smooth dielectric: an extension of this library (the reference's BSDF has
+// no refraction).  `o` is the direction to the viewer in the shading frame
+// (o.z > 0), eta = index on the viewer's side / index on the far side.  The
+// Fresnel reflectance of unpolarised light, F = (r_s^2 + r_p^2) / 2, picks
+// reflection (probability F) or refraction, so the chosen lobe's weight is 1;
+// refraction multiplies the throughput by the base colour (tint) and by eta^2
+// (radiance is scaled by the squared index ratio across an interface; the
+// factors cancel over a way in and out).  Total internal reflection gives
+// F = 1.  One sampler dimension is used.  The next ray leaves from the side
+// of the geometric normal `twn` (facing the viewer) it travels to.
+__device__ __forceinline__ void shade_dielectric(PathState& pl, f3 tint, float eta, f3 o, f3 wx, f3 wy, f3 wn, f3 twn, f3 hit)
+{
+    const float cos_i = o.z;
+    const float sin2_t = (eta * eta) * (1.0f - cos_i * cos_i);
+    float F = 1.0f, cos_t = 0.0f;
+    if (sin2_t < 1.0f) {
+        cos_t = sqrtf(1.0f - sin2_t);
+        const float rs = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+        const float rp = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
+        F = 0.5f * (rs * rs + rp * rp);
+    }
+    f3 i;
+    if (sample_1d(pl.smp) < F) {
+        i = mk3(-o.x, -o.y, o.z);
+        pl.next_o = hit + twn * ORIGIN_OFFSET;
+    } else {
+        i = mk3(-eta * o.x, -eta * o.y, -cos_t);
+        pl.throughput = pl.throughput * (tint * (eta * eta));
+        pl.next_o = hit - twn * ORIGIN_OFFSET;
+    }
+    pl.brdf_pdf = -1.0f; // a delta lobe: emission reached next counts in full
+    f3 wi = mk3((wx.x * i.x + wy.x * i.y) + wn.x * i.z, (wx.y * i.x + wy.y * i.y) + wn.y * i.z, (wx.z * i.x + wy.z * i.y) + wn.z * i.z);
+    pl.next_d = normalize(wi);
+}
+
 // Closest-hit shader (pathtrace.ch.hlsl:227-360) without the shadow ray.
 __device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 ray_o, f3 ray_d, const Hit& h, NeeRequest& nee)
 {
@@ -381,7 +416,8 @@ __device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 r
     f3 wx = normalize(mul3_rows(n0, n1, n2, tangent));
     f3 wy = normalize(mul3_rows(n0, n1, n2, bitangent));
     f3 wn = normalize(mul3_rows(n0, n1, n2, obj_normal));
-    if (dot(wn, ray_d) > 0.0f) {
+    const bool back_face = dot(wn, ray_d) > 0.0f; // the side the vertex normals point away from
+    if (back_face) {
         wx = -wx;
         wy = -wy;
         wn = -wn;
@@ -407,7 +443,15 @@ __device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 r
         pl.final_segment = true;
         return;
     }
-    f3 ip = (ray_o + ray_d * h.t) + twn * ORIGIN_OFFSET;
+    const f3 hit = ray_o + ray_d * h.t;
+    if (s.material_ior) {
+        const float ior = __ldg(s.material_ior + __ldg(&id->material_index));
+        if (ior > 0.0f) {
+            shade_dielectric(pl, bi.base_colour, back_face ? ior : 1.0f / ior, o, wx, wy, wn, twn, hit);
+            return;
+        }
+    }
+    f3 ip = hit + twn * ORIGIN_OFFSET;
 
     // light_contribution (pathtrace.ch.hlsl:159-225) up to the shadow ray.
     nee.add = true;

@@ -1070,6 +1070,7 @@ struct pt_host_scene {
     pt_camera_desc camera{};
     std::vector<pt_texture> textures;
     std::vector<uint8_t> texels;
+    std::vector<float> material_ior; // empty, or one per material (refractive extension)
     // packed
     bool packed = false;
     std::vector<pt_instance_data> inst;
@@ -1366,6 +1367,14 @@ pt_host_scene* pt_scene_from_raw(const pt_raw_scene* raw, const pt_camera_desc* 
                 throw std::runtime_error("texture " + std::to_string(i) + " is malformed");
             s->add_texture(t.width, t.height, t.channels, t.srgb ? 1u : 0u, raw->texels + t.offset);
         }
+        if (raw->material_ior) {
+            s->material_ior.assign(raw->material_ior, raw->material_ior + raw->material_count);
+            for (uint32_t i = 0; i < raw->material_count; i++) {
+                const float n = s->material_ior[i];
+                if (!(n == 0.0f || (n >= 1.0f && std::isfinite(n))))
+                    throw std::runtime_error("material " + std::to_string(i) + ": index of refraction must be 0 or >= 1");
+            }
+        }
         for (uint32_t m = 0; m < raw->mesh_count; m++) {
             if (s->mesh_material[m] >= raw->material_count)
                 throw std::runtime_error("mesh " + std::to_string(m) + " names a missing material");
@@ -1409,6 +1418,7 @@ int pt_scene_raw(const pt_host_scene* s, pt_raw_scene* out)
     out->texel_bytes = s->texels.size();
     out->textures = s->textures.data();
     out->texture_count = (uint32_t)s->textures.size();
+    out->material_ior = s->material_ior.empty() ? nullptr : s->material_ior.data();
     return PT_OK;
 }
 
@@ -1636,6 +1646,7 @@ int pt_scene_pack(pt_host_scene* s, pt_scene_view* v)
         v->texel_bytes = s->texels.size();
         v->textures = s->textures.data();
         v->texture_count = (uint32_t)s->textures.size();
+        v->material_ior = s->material_ior.empty() ? nullptr : s->material_ior.data();
         return PT_OK;
     } catch (const std::exception& e) {
         g_error = e.what();

@@ -456,6 +456,39 @@ def assemble_raw(meshes, env) -> dict:
             "materials": np.array(mats, np.float32), "environment_colour": np.asarray(env, np.float32)}
 
 
+def glass_raw(kind: str = "glass") -> tuple[dict, dict]:
+    """Scenes for the refractive dielectric (raw["material_ior"], an extension
+    of this library).  "glass": a diffuse ground lit by an emissive quad, a
+    clear glass icosphere (index 1.5), a green-tinted one (1.33) and a rough
+    metal one.  "furnace": one clear glass icosphere (index 1.5) alone in a
+    uniform white environment and no lights; a lossless dielectric keeps every
+    pixel at radiance 1 when Russian roulette is off (the white furnace test)."""
+    p, n, uv, ix = icosphere(3)
+    if kind == "furnace":
+        raw = assemble_raw([((p, n, uv, ix), material_row((1.0, 1.0, 1.0), 0.5), [np.eye(4)])], (1.0, 1.0, 1.0))
+        raw["material_ior"] = np.array([1.5], np.float32)
+        cam = {"position": (0.0, 0.0, -3.0), "lookdir": (0.0, 0.0, 3.0), "fov_degrees": 45.0}
+        return raw, cam
+    if kind != "glass":
+        raise ValueError(kind)
+
+    def at(x, y, z, s):
+        M = np.eye(4)
+        M[:3, :3] *= s
+        M[:3, 3] = (x, y, z)
+        return M
+
+    meshes = [(quad(6.0, 0.0, False), material_row((0.7, 0.65, 0.55), 0.8), [np.eye(4)]),
+              (quad(1.2, 3.0, True), material_row((0, 0, 0), 1.0, 0.0, 12.0), [np.eye(4)]),
+              ((p, n, uv, ix), material_row((1.0, 1.0, 1.0), 0.5), [at(-1.1, 0.7, 0.0, 0.7)]),
+              ((p, n, uv, ix), material_row((0.6, 0.95, 0.7), 0.5), [at(0.5, 0.5, 0.6, 0.5)]),
+              ((p, n, uv, ix), material_row((0.9, 0.8, 0.6), 0.3, 1.0), [at(1.2, 0.6, -0.8, 0.6)])]
+    raw = assemble_raw(meshes, (0.1, 0.15, 0.3))
+    raw["material_ior"] = np.array([0.0, 0.0, 1.5, 1.33, 0.0], np.float32)
+    cam = {"position": (0.0, -1.8, -4.5), "lookdir": (0.0, 1.3, 4.5), "fov_degrees": 50.0}
+    return raw, cam
+
+
 def _bits(i: int) -> np.float32:
     return np.frombuffer(np.uint32(i).tobytes(), np.float32)[0]
 
@@ -636,7 +669,7 @@ def _displaced_sphere(subdiv: int, rng: np.random.Generator):
 
 
 def heavy_scene(seed: int = 3, instances: int = 10000, grids: int = 32, spheres: int = 32, grid_n: int = 144,
-                sphere_subdiv: int = 5, emitters: int = 256):
+                sphere_subdiv: int = 5, emitters: int = 256, dielectric: bool = False):
     """The heavy benchmark scene as a raw scene: 64 BLASes totalling ~2M unique
     triangles (32 displaced 144x144 grids of 41,472 triangles, 32 displaced
     subdivision-5 icospheres of 20,480), 10,000 instances with random rotation
@@ -644,16 +677,20 @@ def heavy_scene(seed: int = 3, instances: int = 10000, grids: int = 32, spheres:
     transmissive (opacity 0.1: the reference maps glTF transmission to
     opacity), 256 single-triangle emitters with radiance log-uniform in
     [1, 100].  Returns (raw, camera) for HostScene.from_raw; render at
-    1920x1080 with 12 bounces and Russian roulette from segment 4."""
+    1920x1080 with 12 bounces and Russian roulette from segment 4.  With
+    `dielectric` the transmissive meshes are opaque refractive dielectrics of
+    index 1.5 instead (raw["material_ior"]; the same random draws otherwise)."""
     rng = np.random.default_rng(seed)
     srng = SceneRng(seed)
     base = [displaced_grid(grid_n, srng, amplitude=0.1) for _ in range(grids)] + \
            [_displaced_sphere(sphere_subdiv, rng) for _ in range(spheres)]
-    mats = []
+    mats, glass = [], []
     for k in range(len(base)):
         transmissive = rng.random() < 0.1
         mats.append(material_row(rng.uniform(0.1, 0.9, 3), rng.uniform(0.05, 1.0),
-                                 1.0 if rng.random() < 0.3 else 0.0, alpha=0.1 if transmissive else 1.0))
+                                 1.0 if rng.random() < 0.3 else 0.0,
+                                 alpha=0.1 if transmissive and not dielectric else 1.0))
+        glass.append(transmissive and dielectric)
     per_mesh = [[] for _ in base]
     for i in range(instances):
         k = int(rng.integers(len(base)))
@@ -671,6 +708,7 @@ def heavy_scene(seed: int = 3, instances: int = 10000, grids: int = 32, spheres:
         M[:3, 3] = (rng.uniform(-120, 120), rng.uniform(0, 25), rng.uniform(-120, 120))
         per_mesh[k].append(M)
     meshes = [(m, mat, ms) for m, mat, ms in zip(base, mats, per_mesh) if ms]
+    ior = [1.5 if g else 0.0 for g, ms in zip(glass, per_mesh) if ms]
     for e in range(emitters):
         cx, cy, cz = rng.uniform(-110, 110), rng.uniform(30, 45), rng.uniform(-110, 110)
         size = rng.uniform(1.0, 4.0)
@@ -678,6 +716,8 @@ def heavy_scene(seed: int = 3, instances: int = 10000, grids: int = 32, spheres:
         strength = float(math.exp(rng.uniform(0.0, math.log(100.0))))
         meshes.append((tri, material_row((0, 0, 0), 1.0, 0.0, strength), [np.eye(4)]))
     raw = assemble_raw(meshes, (0.25, 0.3, 0.45))
+    if dielectric:
+        raw["material_ior"] = np.array(ior + [0.0] * emitters, np.float32)
     eye, target = np.array([0.0, 60.0, -170.0]), np.array([0.0, 5.0, 0.0])
     cam = {"position": tuple(-eye), "lookdir": tuple(eye - target), "fov_degrees": 50.0}
     return raw, cam

@@ -41,7 +41,7 @@ def test_ctypes_signatures_cover_declarations():
 
 
 def test_abi_version():
-    assert abi.lib().pt_abi_version() == 1
+    assert abi.lib().pt_abi_version() == abi.ABI_VERSION == 2
 
 
 def test_struct_layouts_match_c():

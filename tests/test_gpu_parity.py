@@ -107,6 +107,36 @@ def test_textured_scene_bitexact(ctx, textured, kernel):
     assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
 
 
+def test_glass_scene_bitexact(ctx, kernel):
+    """Refractive dielectrics (clear and tinted glass, the library's extension):
+    reflection/refraction choice, radiance scaling and the full-weight
+    emission after a delta bounce equal the oracle bit for bit."""
+    raw, cam = scenes.glass_raw("glass")
+    hs = P.HostScene.from_raw(raw, cam)
+    view = hs.pack()
+    params = hs.render_params(96, 72, 4, 10, kernel=kernel)
+    gpu, ref, st, ost = _render_both(ctx, view, params)
+    _assert_bitexact(gpu, ref)
+    assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
+    # the same scene without indices renders differently (the branch is taken)
+    raw["material_ior"] = None
+    hs2 = P.HostScene.from_raw(raw, cam)
+    ctx.upload(hs2.pack())
+    ctx.build_accel()
+    ctx.render(params)
+    assert not np.array_equal(ctx.read_image().view(np.uint32), gpu.view(np.uint32))
+
+
+def test_white_furnace_on_gpu(ctx):
+    raw, cam = scenes.glass_raw("furnace")
+    hs = P.HostScene.from_raw(raw, cam)
+    view = hs.pack()
+    params = hs.render_params(64, 64, 16, 64, rr_start=1000)
+    gpu, ref, st, ost = _render_both(ctx, view, params)
+    _assert_bitexact(gpu, ref)
+    assert np.mean(np.abs(gpu[..., :3] - 1.0) < 1e-4) > 0.98
+
+
 def test_obj_scene_bitexact(ctx, kernel, tmp_path):
     """A Wavefront OBJ scene with MTL materials, a base-colour map, a quad
     emitter and polygons fanned into triangles, through the loader."""
@@ -348,6 +378,19 @@ def test_heavy_scene_bitexact(ctx, heavy, kernel):
     instances, transmissive materials, 256 emitters, 12 bounces, Russian
     roulette from segment 4) equals the oracle bit for bit at low resolution."""
     hs, view = heavy
+    params = hs.render_params(96, 54, 2, 12, rr_start=4, kernel=kernel)
+    gpu, ref, st, ost = _render_both(ctx, view, params)
+    _assert_bitexact(gpu, ref)
+    assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
+
+
+def test_heavy_scene_dielectric_bitexact(ctx, kernel):
+    """The heavy configuration with its transmissive meshes as index-1.5
+    refractive dielectrics (the build-only option of that configuration)."""
+    raw, cam = scenes.heavy_scene(dielectric=True)
+    assert (raw["material_ior"] > 0).sum() > 0
+    hs = P.HostScene.from_raw(raw, cam)
+    view = hs.pack()
     params = hs.render_params(96, 54, 2, 12, rr_start=4, kernel=kernel)
     gpu, ref, st, ost = _render_both(ctx, view, params)
     _assert_bitexact(gpu, ref)
