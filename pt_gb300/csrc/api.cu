@@ -89,19 +89,56 @@ void inverse4(const double m[16], double out[16])
 
 static thread_local std::string g_create_error;
 
+// The 4-wide node a reachable BVH2 node must have (k_make_bvh4 restated).
+// The node's children are in range (checked by the caller); its
+// grandchildren are read only when in range.
+static bool bvh4_matches(const std::vector<BvhNode>& nodes, size_t i, const Bvh4Node& got)
+{
+    const BvhNode& nd = nodes[i];
+    float b[6][4] = {};
+    int ref[4] = {REF_EMPTY, REF_EMPTY, REF_EMPTY, REF_EMPTY};
+    int k = 0;
+    auto put = [&](float4 xy, float zlo, float zhi, int r) {
+        b[0][k] = xy.x, b[1][k] = xy.y, b[2][k] = xy.z, b[3][k] = xy.w, b[4][k] = zlo, b[5][k] = zhi;
+        ref[k++] = r;
+    };
+    for (int c = 0; c < 2; c++) {
+        const int cr = c == 0 ? nd.link.x : nd.link.y;
+        if (cr >= 0 && (size_t)cr < nodes.size()) {
+            const BvhNode& g = nodes[cr];
+            put(g.c0xy, g.c01z.x, g.c01z.y, g.link.x);
+            put(g.c1xy, g.c01z.z, g.c01z.w, g.link.y);
+        } else if (c == 0) {
+            put(nd.c0xy, nd.c01z.x, nd.c01z.y, cr);
+        } else {
+            put(nd.c1xy, nd.c01z.z, nd.c01z.w, cr);
+        }
+    }
+    const float4* planes[6] = {&got.lox, &got.hix, &got.loy, &got.hiy, &got.loz, &got.hiz};
+    for (int a = 0; a < 6; a++)
+        if (std::memcmp(planes[a], b[a], sizeof(float) * k) != 0)
+            return false;
+    const int gl[4] = {got.link.x, got.link.y, got.link.z, got.link.w};
+    return std::memcmp(gl, ref, sizeof(gl)) == 0;
+}
+
 // Host-side structural check of a freshly built acceleration structure
 // (enabled by PT_VALIDATE_BVH=1): every reference in range, every BLAS
 // covering each of its mesh's triangles exactly once, the TLAS covering each
-// instance exactly once, and no cycles.  Returns an empty string when valid.
+// instance exactly once, no cycles, and each reachable node's 4-wide copy
+// holding its grandchildren.  Returns an empty string when valid.
 static std::string validate_accel(pt_ctx* c, const std::vector<uint32_t>& tri_base)
 {
     const uint32_t T = c->tri_count, I = c->instance_count, M = c->mesh_count;
     const size_t blas_nodes = T > 1 ? T - 1 : 0;
     std::vector<BvhNode> nodes(c->nodes.n);
+    std::vector<Bvh4Node> nodes4(c->nodes4.p ? c->nodes4.n : 0);
     std::vector<TriRec> tris(T);
     std::vector<int> roots(M);
     std::vector<DevInstance> dinst(I);
     if (cudaMemcpy(nodes.data(), c->nodes.p, nodes.size() * sizeof(BvhNode), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        (!nodes4.empty() &&
+         cudaMemcpy(nodes4.data(), c->nodes4.p, nodes4.size() * sizeof(Bvh4Node), cudaMemcpyDeviceToHost) != cudaSuccess) ||
         (T && cudaMemcpy(tris.data(), c->tris.p, T * sizeof(TriRec), cudaMemcpyDeviceToHost) != cudaSuccess) ||
         (M && cudaMemcpy(roots.data(), c->mesh_root.p, M * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) ||
         (I && cudaMemcpy(dinst.data(), c->dinst.p, I * sizeof(DevInstance), cudaMemcpyDeviceToHost) != cudaSuccess))
@@ -119,6 +156,11 @@ static std::string validate_accel(pt_ctx* c, const std::vector<uint32_t>& tri_ba
                     return "node reference " + std::to_string(r) + " out of range";
                 if (++internal > (size_t)expect)
                     return "cycle or duplicate nodes";
+                for (int ch : {nodes[r].link.x, nodes[r].link.y})
+                    if (ch >= 0 && ((size_t)ch < node_lo || (size_t)ch >= node_hi))
+                        return "node reference " + std::to_string(ch) + " out of range";
+                if (!nodes4.empty() && !bvh4_matches(nodes, (size_t)r, nodes4[r]))
+                    return "4-wide node " + std::to_string(r) + " differs from its BVH2 grandchildren";
                 st.push_back(nodes[r].link.x);
                 st.push_back(nodes[r].link.y);
             } else if (ref_is_leaf(r)) {
@@ -252,6 +294,7 @@ void pt_destroy(pt_ctx* c)
     c->inst_mesh.release();
     c->dinst.release();
     c->nodes.release();
+    c->nodes4.release();
     c->tris.release();
     c->mesh_root.release();
     c->image.release();
@@ -433,8 +476,11 @@ int pt_build_accel(pt_ctx* c, pt_accel_info* info)
     cudaSetDevice(c->device);
     cudaError_t e;
     size_t n_nodes = bvh_node_count(c->tri_count, c->instance_count);
+    const bool wide = use_bvh4();
+    if (!wide)
+        c->nodes4.release();
     if ((e = c->nodes.alloc(n_nodes)) != cudaSuccess || (e = c->tris.alloc(c->tri_count)) != cudaSuccess ||
-        (e = c->mesh_root.alloc(c->mesh_count)) != cudaSuccess)
+        (e = c->mesh_root.alloc(c->mesh_count)) != cudaSuccess || (wide && (e = c->nodes4.alloc(n_nodes)) != cudaSuccess))
         return c->cuda_fail(e, "acceleration structure allocation");
     size_t scratch_bytes = bvh_scratch_bytes(c->mesh_count, c->tri_count, c->instance_count);
     void* scratch = nullptr;
@@ -458,6 +504,8 @@ int pt_build_accel(pt_ctx* c, pt_accel_info* info)
     out.mesh_root = c->mesh_root.p;
     cudaEventRecord(c->ev0, c->stream);
     e = bvh_build(in, out, scratch, scratch_bytes, c->stream);
+    if (e == cudaSuccess && wide)
+        e = build_bvh4(c->nodes.p, (uint32_t)n_nodes, c->nodes4.p, c->stream);
     cudaEventRecord(c->ev1, c->stream);
     cudaError_t e2 = cudaStreamSynchronize(c->stream);
     cudaFree(scratch);
@@ -482,7 +530,8 @@ int pt_build_accel(pt_ctx* c, pt_accel_info* info)
     c->accel.tlas_nodes = c->instance_count > 1 ? c->instance_count - 1 : 0;
     c->accel.blas_nodes = c->tri_count > 1 ? c->tri_count - 1 : 0;
     c->accel.triangles = c->tri_count;
-    c->accel.device_bytes = n_nodes * sizeof(BvhNode) + (size_t)c->tri_count * sizeof(TriRec) + (size_t)c->instance_count * sizeof(DevInstance);
+    c->accel.device_bytes = n_nodes * sizeof(BvhNode) + (wide ? n_nodes * sizeof(Bvh4Node) : 0) +
+                            (size_t)c->tri_count * sizeof(TriRec) + (size_t)c->instance_count * sizeof(DevInstance);
     c->accel.build_ms = ms;
     if (info)
         *info = c->accel;
@@ -546,6 +595,7 @@ RenderArgs render_args(const pt_ctx* c, const pt_render_params* p, bool fp64)
     if (cap)
         a.s.max_iterations = std::min(a.s.max_iterations, cap);
     a.s.nodes = c->nodes.p;
+    a.s.nodes4 = c->nodes4.p;
     a.s.tris = c->tris.p;
     a.s.dinst = c->dinst.p;
     a.s.tlas_root = c->tlas_root;

@@ -49,6 +49,7 @@ struct BatchState {
     DevBuf<uint32_t> path_share;
     DevBuf<char> state;
     uint32_t state_paths = 0;
+    bool w4 = true; // every job's scene has 4-wide nodes (else the BVH2 kernels run)
     DevBuf<unsigned long long> counters;
     DevBuf<uint32_t> error_word;
     cudaStream_t side = nullptr;
@@ -218,8 +219,10 @@ int prepare(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vecto
 {
     b->graph_key.clear();
     std::vector<RenderArgs> args(p.size());
+    b->w4 = true;
     for (size_t j = 0; j < p.size(); j++) {
         RenderArgs a = render_args(jobs[j].scene, &p[j], false);
+        b->w4 = b->w4 && a.s.nodes4 != nullptr;
         a.image = b->image.p + b->img_off[j];
         a.sum64 = b->sum_off[j] == SIZE_MAX ? nullptr : b->sum64.p + 4 * b->sum_off[j];
         a.counters = b->counters.p;
@@ -296,7 +299,7 @@ cudaError_t issue(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std:
     if (!plan.waves.empty()) {
         uint32_t wl = 0;
         e = launch_wavefront_batch(b->jobs.p, b->shares.p, plan.waves.data(), (uint32_t)plan.waves.size(), b->path_share.p,
-                                   b->counters.p, b->state.p, b->state.n, b->state_paths, c->sm_count, &wl, st);
+                                   b->counters.p, b->state.p, b->state.n, b->state_paths, b->w4, c->sm_count, &wl, st);
         if (e != cudaSuccess)
             return e;
         nl += wl;

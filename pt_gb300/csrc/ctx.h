@@ -17,6 +17,7 @@ struct BatchState; // batch.cu
 void batch_free(BatchState* b);
 } // namespace pt
 
+using pt::Bvh4Node;
 using pt::BvhNode;
 using pt::DevInstance;
 using pt::DevInstanceData;
@@ -78,6 +79,7 @@ struct pt_ctx {
     // acceleration structure
     bool accel_ok = false;
     DevBuf<BvhNode> nodes;
+    DevBuf<Bvh4Node> nodes4; // empty when the BVH2 is traversed (PT_BVH_WIDTH=2)
     DevBuf<TriRec> tris;
     DevBuf<int> mesh_root;
     int tlas_root = REF_EMPTY;

@@ -8,6 +8,9 @@
 //   light      u32 light-sampler stream (lightsample.cpp:89-221)
 //   nodes      BvhNode, 64 B: both child boxes of a BVH2 node (one array for
 //              every BLAS and the TLAS)
+//   nodes4     Bvh4Node, 128 B (one cache line), same indices as `nodes`: node
+//              i's grandchildren (a child that is a leaf stands for itself),
+//              so the traversal descends two BVH2 levels per dependent fetch
 //   tris       TriRec, 48 B: the three object-space vertices of a triangle in
 //              BVH leaf order plus its mesh-local primitive index
 //   dinst      DevInstance, 64 B: world-to-object rows + BLAS root reference
@@ -37,6 +40,14 @@ struct __align__(16) BvhNode {
     float4 c1xy; // c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y
     float4 c01z; // c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z
     int4 link;   // child0, child1, -, -
+};
+
+// Four child boxes as x/y/z planes across the children (lane k = child k)
+// and their references; REF_EMPTY marks an unused slot.
+struct __align__(128) Bvh4Node {
+    float4 lox, hix, loy, hiy, loz, hiz;
+    int4 link;
+    int4 pad;
 };
 
 struct __align__(16) TriRec {
@@ -85,6 +96,7 @@ struct DevScene {
     const DevTexture* textures;
     uint32_t texture_count;
     const BvhNode* nodes;
+    const Bvh4Node* nodes4; // null: traverse the BVH2 `nodes`
     const TriRec* tris;
     const DevInstance* dinst;
     int tlas_root;
@@ -269,6 +281,85 @@ __device__ __forceinline__ int node_children(const BvhNode* node, const ObjRay& 
     return (e0 <= x0 ? 1 : 0) | (e1 <= x1 ? 2 : 0);
 }
 
+// Intersect the four child boxes of a 4-wide node; bit k of the result is
+// set when child k is hit, e[k] its entry distance.
+__device__ __forceinline__ int node4_children(const Bvh4Node* node, const ObjRay& r, float tmin, float tmax, float (&e)[4], int (&c)[4])
+{
+    const float4 lx = ldg4(&node->lox), hx = ldg4(&node->hix), ly = ldg4(&node->loy), hy = ldg4(&node->hiy);
+    const float4 lz = ldg4(&node->loz), hz = ldg4(&node->hiz);
+    const int4 l = ldg4i(&node->link);
+    c[0] = l.x;
+    c[1] = l.y;
+    c[2] = l.z;
+    c[3] = l.w;
+    int m = 0;
+#define PT_NODE4_CHILD(k, q)                                                                     \
+    {                                                                                            \
+        float fx, fy, fz;                                                                        \
+        const float nx = slab_enter(lx.q, hx.q, r.inv_d.x, r.o_inv.x, fx);                       \
+        const float ny = slab_enter(ly.q, hy.q, r.inv_d.y, r.o_inv.y, fy);                       \
+        const float nz = slab_enter(lz.q, hz.q, r.inv_d.z, r.o_inv.z, fz);                       \
+        e[k] = fmaxf(fmaxf(fmaxf(nx, ny), nz), tmin);                                            \
+        const float x = fminf(fminf(fminf(fx, fy), fz), tmax);                                   \
+        m |= (e[k] <= x && l.q != REF_EMPTY) ? (1 << k) : 0;                                     \
+    }
+    PT_NODE4_CHILD(0, x)
+    PT_NODE4_CHILD(1, y)
+    PT_NODE4_CHILD(2, z)
+    PT_NODE4_CHILD(3, w)
+#undef PT_NODE4_CHILD
+    return m;
+}
+
+// One interior step of a 4-wide traversal: the nearest hit child becomes
+// `ref`, the others are pushed far to near; nothing hit pops the stack.  A
+// push that would overflow sets ERR_STACK_OVERFLOW and drops those children.
+template <int N>
+__device__ __forceinline__ void step4(const DevScene& s, const ObjRay& r, float tmin, float tmax, int& ref, int (&stack)[N], int& sp)
+{
+    float e[4];
+    int c[4];
+    const int m = node4_children(s.nodes4 + ref, r, tmin, tmax, e, c);
+    const int cnt = __popc(m);
+    if (cnt == 0) {
+        ref = stack[--sp];
+        return;
+    }
+    if (cnt == 1) {
+        ref = c[__ffs(m) - 1];
+        return;
+    }
+    // sort (entry, child) ascending with misses keyed +inf: a five-exchange network
+    const float inf = __int_as_float(0x7f800000);
+    float k0 = (m & 1) ? e[0] : inf, k1 = (m & 2) ? e[1] : inf, k2 = (m & 4) ? e[2] : inf, k3 = (m & 8) ? e[3] : inf;
+    int r0 = c[0], r1 = c[1], r2 = c[2], r3 = c[3];
+#define PT_CSWAP(ka, ra, kb, rb)  \
+    if (kb < ka) {                \
+        const float tk = ka;      \
+        ka = kb;                  \
+        kb = tk;                  \
+        const int tr = ra;        \
+        ra = rb;                  \
+        rb = tr;                  \
+    }
+    PT_CSWAP(k0, r0, k1, r1)
+    PT_CSWAP(k2, r2, k3, r3)
+    PT_CSWAP(k0, r0, k2, r2)
+    PT_CSWAP(k1, r1, k3, r3)
+    PT_CSWAP(k1, r1, k2, r2)
+#undef PT_CSWAP
+    if (sp + cnt - 1 > N) {
+        atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+    } else {
+        if (cnt == 4)
+            stack[sp++] = r3;
+        if (cnt >= 3)
+            stack[sp++] = r2;
+        stack[sp++] = r1;
+    }
+    ref = r0;
+}
+
 // Watertight ray/triangle test (Woop, Benthin & Wald 2013) without culling.
 __device__ __forceinline__ bool watertight(const ObjRay& r, f3 p0, f3 p1, f3 p2, float& t, float& b1, float& b2)
 {
@@ -333,110 +424,150 @@ __device__ __forceinline__ bool better(float t, uint32_t inst, uint32_t prim, co
 
 constexpr int STACK_SIZE = 96;
 
-// Closest hit with the (t, instance, primitive) order of the oracle.  Returns
-// true on a hit.  The stack lives in local memory (L1-resident).
-static __device__ __forceinline__ bool trace_closest_inl(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
+// BVH2 interior step: the nearer hit child becomes `ref`, the farther is
+// pushed; nothing hit pops the stack.
+template <int N>
+__device__ __forceinline__ void step2(const DevScene& s, const ObjRay& r, float tmin, float tmax, int& ref, int (&stack)[N], int& sp)
 {
-    uint32_t n_nodes = 0, n_tris = 0;
-    h.t = tmax;
-    h.inst = 0xFFFFFFFFu;
-    h.prim = 0xFFFFFFFFu;
-    h.b1 = h.b2 = 0.0f;
-    bool found = false;
-    ObjRay world;
-    world.o = o;
-    world.d = d;
-    setup_slab(world);
-    ObjRay r = world;
-    int stack[STACK_SIZE];
-    int sp = 0;
-    stack[sp++] = REF_DONE;
-    int ref = s.tlas_root;
-    bool in_blas = false;
-    uint32_t cur_inst = 0;
-    if (ref == REF_EMPTY)
-        return false;
-    for (uint32_t iter = 0;; iter++) {
-        if (iter >= s.max_iterations) {
-            // A well-formed BVH never gets here; a malformed one must not hang the GPU.
-            atomicOr(s.error_word, ERR_WATCHDOG);
-            break;
+    float e0, e1;
+    int c0, c1;
+    const int m = node_children(s.nodes + ref, r, tmin, tmax, e0, e1, c0, c1);
+    if (m == 3) {
+        int near = c0, far = c1;
+        if (e1 < e0) {
+            near = c1;
+            far = c0;
         }
-        if (ref >= 0) {
-            float e0, e1;
-            int c0, c1;
-            n_nodes++;
-            int m = node_children(s.nodes + ref, r, tmin, h.t, e0, e1, c0, c1);
-            if (m == 3) {
-                int near = c0, far = c1;
-                if (e1 < e0) {
-                    near = c1;
-                    far = c0;
-                }
-                if (sp < STACK_SIZE)
-                    stack[sp++] = far;
-                else
-                    atomicOr(s.error_word, ERR_STACK_OVERFLOW);
-                ref = near;
-            } else if (m == 1) {
-                ref = c0;
-            } else if (m == 2) {
-                ref = c1;
-            } else {
-                ref = stack[--sp];
-            }
-            continue;
-        }
-        if (ref == REF_DONE)
-            break;
-        if (ref == REF_EXIT_BLAS) {
-            r = world;
-            in_blas = false;
-            ref = stack[--sp];
-            continue;
-        }
-        uint32_t first = leaf_first(ref), count = leaf_count(ref);
-        if (!in_blas) {
-            // TLAS leaf: instances [first, first + count); one per leaf here.
-            cur_inst = first;
-            const DevInstance* di = s.dinst + cur_inst;
-            int root = __ldg(&di->blas_root);
-            if (root == REF_EMPTY || count != 1) {
-                ref = stack[--sp];
-                continue;
-            }
-            to_object(di, o, d, r);
-            if (sp >= STACK_SIZE) {
-                atomicOr(s.error_word, ERR_STACK_OVERFLOW);
-                ref = stack[--sp];
-                continue;
-            }
-            stack[sp++] = REF_EXIT_BLAS;
-            in_blas = true;
-            ref = root;
-            continue;
-        }
-        n_tris += count;
-        for (uint32_t k = 0; k < count; k++) {
-            const TriRec* tr = s.tris + first + k;
-            float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
-            float t, b1, b2;
-            uint32_t prim = __float_as_uint(a.w);
-            if (watertight(r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), t, b1, b2) && t >= tmin && t <= h.t &&
-                better(t, cur_inst, prim, h)) {
-                h.t = t;
-                h.b1 = b1;
-                h.b2 = b2;
-                h.inst = cur_inst;
-                h.prim = prim;
-                found = true;
-            }
-        }
+        if (sp < N)
+            stack[sp++] = far;
+        else
+            atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+        ref = near;
+    } else if (m == 1) {
+        ref = c0;
+    } else if (m == 2) {
+        ref = c1;
+    } else {
         ref = stack[--sp];
     }
-    tc.nodes += n_nodes;
-    tc.tris += n_tris;
-    return found;
+}
+
+// Closest-hit traversal of one ray as a resumable state: closest_begin sets
+// it up and each closest_step advances it by one node visit, leaf or
+// instance transition, returning true when the ray is finished.  The hit is
+// the (t, instance, primitive) minimum of the oracle whatever the BVH.  The
+// stack lives in local memory (L1-resident).  W4 walks the 4-wide nodes
+// (s.nodes4, which must be present), else the BVH2.
+struct ClosestTrace {
+    ObjRay world, r;
+    Hit h;
+    float tmin;
+    int ref, sp;
+    uint32_t cur_inst, iter;
+    bool in_blas, found;
+};
+// The traversal stack is a separate array: inside the state it would pull
+// every field of the state into local memory with it.
+typedef int TraceStack[STACK_SIZE];
+
+__device__ __forceinline__ void closest_begin(const DevScene& s, f3 o, f3 d, float tmin, float tmax, ClosestTrace& t, TraceStack& stack)
+{
+    t.h.t = tmax;
+    t.h.inst = 0xFFFFFFFFu;
+    t.h.prim = 0xFFFFFFFFu;
+    t.h.b1 = t.h.b2 = 0.0f;
+    t.found = false;
+    t.world.o = o;
+    t.world.d = d;
+    setup_slab(t.world);
+    t.r = t.world;
+    t.tmin = tmin;
+    t.sp = 0;
+    stack[t.sp++] = REF_DONE;
+    t.ref = s.tlas_root == REF_EMPTY ? REF_DONE : s.tlas_root;
+    t.in_blas = false;
+    t.cur_inst = 0;
+    t.iter = 0;
+}
+
+template <bool W4>
+__device__ __forceinline__ bool closest_step(const DevScene& s, ClosestTrace& t, TraceStack& stack, TraceCounters& tc)
+{
+    if (t.iter >= s.max_iterations) {
+        // A well-formed BVH never gets here; a malformed one must not hang the GPU.
+        atomicOr(s.error_word, ERR_WATCHDOG);
+        return true;
+    }
+    t.iter++;
+    const int ref = t.ref;
+    if (ref >= 0) {
+        tc.nodes++;
+        if (W4)
+            step4(s, t.r, t.tmin, t.h.t, t.ref, stack, t.sp);
+        else
+            step2(s, t.r, t.tmin, t.h.t, t.ref, stack, t.sp);
+        return false;
+    }
+    if (ref == REF_DONE)
+        return true;
+    if (ref == REF_EXIT_BLAS) {
+        t.r = t.world;
+        t.in_blas = false;
+        t.ref = stack[--t.sp];
+        return false;
+    }
+    const uint32_t first = leaf_first(ref), count = leaf_count(ref);
+    if (!t.in_blas) {
+        // TLAS leaf: instances [first, first + count); one per leaf here.
+        t.cur_inst = first;
+        const DevInstance* di = s.dinst + first;
+        const int root = __ldg(&di->blas_root);
+        if (root == REF_EMPTY || count != 1) {
+            t.ref = stack[--t.sp];
+            return false;
+        }
+        to_object(di, t.world.o, t.world.d, t.r);
+        if (t.sp >= STACK_SIZE) {
+            atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+            t.ref = stack[--t.sp];
+            return false;
+        }
+        stack[t.sp++] = REF_EXIT_BLAS;
+        t.in_blas = true;
+        t.ref = root;
+        return false;
+    }
+    tc.tris += count;
+    for (uint32_t k = 0; k < count; k++) {
+        const TriRec* tr = s.tris + first + k;
+        const float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
+        float tt, b1, b2;
+        const uint32_t prim = __float_as_uint(a.w);
+        if (watertight(t.r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), tt, b1, b2) && tt >= t.tmin &&
+            tt <= t.h.t && better(tt, t.cur_inst, prim, t.h)) {
+            t.h.t = tt;
+            t.h.b1 = b1;
+            t.h.b2 = b2;
+            t.h.inst = t.cur_inst;
+            t.h.prim = prim;
+            t.found = true;
+        }
+    }
+    t.ref = stack[--t.sp];
+    return false;
+}
+
+// Closest hit of one ray, traversed to the end.  Returns true on a hit.
+template <bool W4>
+static __device__ __forceinline__ bool trace_closest_inl(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
+{
+    ClosestTrace t;
+    TraceStack stack;
+    closest_begin(s, o, d, tmin, tmax, t, stack);
+    while (!closest_step<W4>(s, t, stack, tc)) {
+    }
+    h = t.h;
+    return t.found;
 }
 
 // Closest hit as trace_closest_inl, traversed "while-while" with speculative
@@ -567,129 +698,150 @@ static __device__ __forceinline__ bool trace_closest_ww(const DevScene& s, f3 o,
 // Shadow ray of shadowray.ah.hlsl / shadowray.ms.hlsl: the first opaque hit in
 // [tmin, tmax] occludes; transparent instances attenuate by (1 - alpha).
 // Returns the visibility throughput (0 = occluded).
+// Any-hit shadow traversal of one ray as a resumable state (shadowray.ah.hlsl:
+// 12-40): opaque hits end it with visibility 0, transparent instances scale
+// the throughput by 1 - alpha and it ends occluded below 1e-5.
+struct ShadowTrace {
+    ObjRay world, r;
+    float tmin, tmax, throughput, alpha_pass;
+    int ref, sp;
+    uint32_t iter, alpha_tex, alpha_inst;
+    bool in_blas, opaque, alpha_map; // alpha_map: the transparent instance's alpha comes from a base colour map
+};
+
+__device__ __forceinline__ void shadow_begin(const DevScene& s, f3 o, f3 d, float tmin, float tmax, ShadowTrace& t, TraceStack& stack)
+{
+    t.world.o = o;
+    t.world.d = d;
+    setup_slab(t.world);
+    t.r = t.world;
+    t.tmin = tmin;
+    t.tmax = tmax;
+    t.sp = 0;
+    stack[t.sp++] = REF_DONE;
+    t.ref = s.tlas_root == REF_EMPTY ? REF_DONE : s.tlas_root;
+    t.in_blas = false;
+    t.opaque = true;
+    t.alpha_map = false;
+    t.alpha_tex = t.alpha_inst = 0;
+    t.alpha_pass = 1.0f;
+    t.throughput = 1.0f;
+    t.iter = 0;
+}
+
+// Visibility of a finished shadow ray.
+__device__ __forceinline__ float shadow_result(const ShadowTrace& t) { return t.throughput < 1e-5f ? 0.0f : t.throughput; }
+
+template <bool W4>
+__device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, TraceStack& stack, TraceCounters& tc)
+{
+    if (t.iter >= s.max_iterations) {
+        // A well-formed BVH never gets here; a malformed one must not hang the GPU.
+        atomicOr(s.error_word, ERR_WATCHDOG);
+        return true;
+    }
+    t.iter++;
+    const int ref = t.ref;
+    if (ref >= 0) {
+        tc.nodes++;
+        if (W4)
+            step4(s, t.r, t.tmin, t.tmax, t.ref, stack, t.sp);
+        else
+            step2(s, t.r, t.tmin, t.tmax, t.ref, stack, t.sp);
+        return false;
+    }
+    if (ref == REF_DONE)
+        return true;
+    if (ref == REF_EXIT_BLAS) {
+        t.r = t.world;
+        t.in_blas = false;
+        t.ref = stack[--t.sp];
+        return false;
+    }
+    const uint32_t first = leaf_first(ref), count = leaf_count(ref);
+    if (!t.in_blas) {
+        const DevInstance* di = s.dinst + first;
+        const int root = __ldg(&di->blas_root);
+        if (root == REF_EMPTY || count != 1) {
+            t.ref = stack[--t.sp];
+            return false;
+        }
+        const uint32_t flags = __ldg(&di->flags);
+        t.opaque = (flags & 1u) != 0;
+        if (!t.opaque) {
+            const uint32_t mi = __ldg(&s.inst_data[first].material_index);
+            t.alpha_map = (__float_as_uint(__ldg(&s.materials[mi].rmn.w)) & MAP_BASE_COLOUR) != 0;
+            t.alpha_tex = __float_as_uint(__ldg(&s.materials[mi].base_colour.x));
+            t.alpha_inst = first;
+            t.alpha_pass = 1.0f - __ldg(&s.materials[mi].base_colour.w);
+        }
+        to_object(di, t.world.o, t.world.d, t.r);
+        if (t.sp >= STACK_SIZE) {
+            atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+            t.ref = stack[--t.sp];
+            return false;
+        }
+        stack[t.sp++] = REF_EXIT_BLAS;
+        t.in_blas = true;
+        t.ref = root;
+        return false;
+    }
+    tc.tris += count;
+    for (uint32_t k = 0; k < count; k++) {
+        const TriRec* tr = s.tris + first + k;
+        const float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
+        float tt, b1, b2;
+        if (watertight(t.r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), tt, b1, b2) && tt >= t.tmin &&
+            tt <= t.tmax) {
+            if (t.opaque) {
+                t.throughput = 0.0f;
+                break;
+            }
+            // shadowray.ah.hlsl:29-34: throughput *= 1 - base colour alpha at the hit
+            if (t.alpha_map)
+                t.alpha_pass = 1.0f - sample_texture(s, t.alpha_tex, hit_uv(s, t.alpha_inst, __float_as_uint(a.w), b1, b2)).w;
+            t.throughput *= t.alpha_pass;
+            if (t.throughput < 1e-5f)
+                break;
+        }
+    }
+    if (t.throughput == 0.0f || t.throughput < 1e-5f)
+        return true;
+    t.ref = stack[--t.sp];
+    return false;
+}
+
+template <bool W4>
 static __device__ __forceinline__ float trace_shadow_inl(const DevScene& s, f3 o, f3 d, float tmin, float tmax, TraceCounters& tc)
 {
-    uint32_t n_nodes = 0, n_tris = 0;
-    ObjRay world;
-    world.o = o;
-    world.d = d;
-    setup_slab(world);
-    ObjRay r = world;
-    int stack[STACK_SIZE];
-    int sp = 0;
-    stack[sp++] = REF_DONE;
-    int ref = s.tlas_root;
-    bool in_blas = false;
-    bool opaque = true;
-    bool alpha_map = false; // transparent instance whose alpha comes from a base colour map
-    uint32_t alpha_tex = 0, alpha_inst = 0;
-    float alpha_pass = 1.0f;
-    float throughput = 1.0f;
-    if (ref == REF_EMPTY)
-        return 1.0f;
-    for (uint32_t iter = 0;; iter++) {
-        if (iter >= s.max_iterations) {
-            // A well-formed BVH never gets here; a malformed one must not hang the GPU.
-            atomicOr(s.error_word, ERR_WATCHDOG);
-            break;
-        }
-        if (ref >= 0) {
-            float e0, e1;
-            int c0, c1;
-            n_nodes++;
-            int m = node_children(s.nodes + ref, r, tmin, tmax, e0, e1, c0, c1);
-            if (m == 3) {
-                int near = c0, far = c1;
-                if (e1 < e0) {
-                    near = c1;
-                    far = c0;
-                }
-                if (sp < STACK_SIZE)
-                    stack[sp++] = far;
-                else
-                    atomicOr(s.error_word, ERR_STACK_OVERFLOW);
-                ref = near;
-            } else if (m == 1) {
-                ref = c0;
-            } else if (m == 2) {
-                ref = c1;
-            } else {
-                ref = stack[--sp];
-            }
-            continue;
-        }
-        if (ref == REF_DONE)
-            break;
-        if (ref == REF_EXIT_BLAS) {
-            r = world;
-            in_blas = false;
-            ref = stack[--sp];
-            continue;
-        }
-        uint32_t first = leaf_first(ref), count = leaf_count(ref);
-        if (!in_blas) {
-            const DevInstance* di = s.dinst + first;
-            int root = __ldg(&di->blas_root);
-            if (root == REF_EMPTY || count != 1) {
-                ref = stack[--sp];
-                continue;
-            }
-            uint32_t flags = __ldg(&di->flags);
-            opaque = (flags & 1u) != 0;
-            if (!opaque) {
-                uint32_t mi = __ldg(&s.inst_data[first].material_index);
-                alpha_map = (__float_as_uint(__ldg(&s.materials[mi].rmn.w)) & MAP_BASE_COLOUR) != 0;
-                alpha_tex = __float_as_uint(__ldg(&s.materials[mi].base_colour.x));
-                alpha_inst = first;
-                alpha_pass = 1.0f - __ldg(&s.materials[mi].base_colour.w);
-            }
-            to_object(di, o, d, r);
-            if (sp >= STACK_SIZE) {
-                atomicOr(s.error_word, ERR_STACK_OVERFLOW);
-                ref = stack[--sp];
-                continue;
-            }
-            stack[sp++] = REF_EXIT_BLAS;
-            in_blas = true;
-            ref = root;
-            continue;
-        }
-        n_tris += count;
-        for (uint32_t k = 0; k < count; k++) {
-            const TriRec* tr = s.tris + first + k;
-            float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
-            float t, b1, b2;
-            if (watertight(r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z), t, b1, b2) && t >= tmin && t <= tmax) {
-                if (opaque) {
-                    throughput = 0.0f;
-                    break;
-                }
-                // shadowray.ah.hlsl:29-34: throughput *= 1 - base colour alpha at the hit
-                if (alpha_map)
-                    alpha_pass = 1.0f - sample_texture(s, alpha_tex, hit_uv(s, alpha_inst, __float_as_uint(a.w), b1, b2)).w;
-                throughput *= alpha_pass;
-                if (throughput < 1e-5f)
-                    break;
-            }
-        }
-        if (throughput == 0.0f || throughput < 1e-5f)
-            break;
-        ref = stack[--sp];
+    ShadowTrace t;
+    TraceStack stack;
+    shadow_begin(s, o, d, tmin, tmax, t, stack);
+    while (!shadow_step<W4>(s, t, stack, tc)) {
     }
-    tc.nodes += n_nodes;
-    tc.tris += n_tris;
-    return throughput < 1e-5f ? 0.0f : throughput;
+    return shadow_result(t);
 }
 
 // Out-of-line copies for the megakernel (keeps its code size down); the
-// wavefront traversal kernels inline the traversal instead.
-static __device__ __noinline__ bool trace_closest(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
+// wavefront traversal kernels inline the traversal instead.  The node width
+// follows the scene (4-wide when s.nodes4 is present).
+template <bool W4>
+static __device__ __noinline__ bool trace_closest_out(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
 {
-    return trace_closest_inl(s, o, d, tmin, tmax, h, tc);
+    return trace_closest_inl<W4>(s, o, d, tmin, tmax, h, tc);
 }
-static __device__ __noinline__ float trace_shadow(const DevScene& s, f3 o, f3 d, float tmin, float tmax, TraceCounters& tc)
+template <bool W4>
+static __device__ __noinline__ float trace_shadow_out(const DevScene& s, f3 o, f3 d, float tmin, float tmax, TraceCounters& tc)
 {
-    return trace_shadow_inl(s, o, d, tmin, tmax, tc);
+    return trace_shadow_inl<W4>(s, o, d, tmin, tmax, tc);
+}
+static __device__ __forceinline__ bool trace_closest(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
+{
+    return s.nodes4 ? trace_closest_out<true>(s, o, d, tmin, tmax, h, tc) : trace_closest_out<false>(s, o, d, tmin, tmax, h, tc);
+}
+static __device__ __forceinline__ float trace_shadow(const DevScene& s, f3 o, f3 d, float tmin, float tmax, TraceCounters& tc)
+{
+    return s.nodes4 ? trace_shadow_out<true>(s, o, d, tmin, tmax, tc) : trace_shadow_out<false>(s, o, d, tmin, tmax, tc);
 }
 
 } // namespace pt

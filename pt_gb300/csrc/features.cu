@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(128) k_features(RenderArgs a, float4* feat_a, 
             f3 ro, rd;
             camera_ray(a, px, py, u_pixel, u_lens, ro, rd);
             Hit h;
-            if (!trace_closest_inl(a.s, ro, rd, a.near_plane, a.far_plane, h, tc))
+            if (!trace_closest(a.s, ro, rd, a.near_plane, a.far_plane, h, tc))
                 continue;
             f3 ha, hn;
             hit_features(a.s, h, rd, ha, hn);

@@ -8,6 +8,7 @@ namespace pt {
 
 struct RenderArgs;
 struct BvhNode;
+struct Bvh4Node;
 struct TriRec;
 struct DevInstance;
 struct DevInstanceData;
@@ -61,11 +62,12 @@ struct BatchWave {
 };
 // `path_share` holds n_paths_max u32; `waves` is host memory (the launch
 // sequence is fixed by it, so the whole call can be captured in a graph).
+// w4: every job's scene has 4-wide nodes (the 4-wide traversal kernels run).
 // Occupancy queries of the batched kernels; call before capturing a batch.
 cudaError_t wave_batch_prepare();
 cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shares, const BatchWave* waves, uint32_t wave_count,
                                    uint32_t* path_share, unsigned long long* counters, void* state, size_t state_bytes,
-                                   uint32_t n_paths_max, int sm_count, uint32_t* launches, cudaStream_t stream);
+                                   uint32_t n_paths_max, bool w4, int sm_count, uint32_t* launches, cudaStream_t stream);
 cudaError_t features_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
 
 // Denoiser features and packing (features.cu).
@@ -108,6 +110,11 @@ struct BvhBuildOutput {
     int* mesh_root;      // mesh_count
     int tlas_root;       // host value after the build
 };
+
+// 4-wide nodes derived from the n BVH2 nodes (same indices), and whether the
+// tracer uses them (PT_BVH_WIDTH=2 keeps the BVH2 traversal).
+cudaError_t build_bvh4(const BvhNode* nodes, uint32_t n, Bvh4Node* out, cudaStream_t stream);
+bool use_bvh4();
 
 // Scratch sizing for bvh_build (bytes).
 size_t bvh_scratch_bytes(uint32_t mesh_count, uint32_t tri_count, uint32_t instance_count);

@@ -26,6 +26,7 @@
 // (`OneJob`: path id -> sample and pixel of the call's camera) or a batch
 // (`ManyJobs`: a wave holds shares of several jobs, each with its own scene,
 // camera, size and sample range; raygen records each path's share).
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -207,12 +208,15 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs<Src> a)
     }
 }
 
+// Closest-hit traversal of a launch: over the 4-wide nodes, the BVH2 one
+// node-or-leaf step per iteration, or the BVH2 while-while with speculative
+// leaves.
+enum Traversal : int { TRAV_BVH4 = 0, TRAV_BVH2 = 1, TRAV_BVH2_WW = 2 };
+
 // Persistent traversal: warps fetch 32 queue entries at a time.
-// WW selects the while-while traversal with speculative leaves; MINB is the
-// resident-block target of the launch bounds (the register budget).
 // Only traces: k_wf_split then separates hits from misses.
-template <class Src, bool WW, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
+template <class Src, int TRAV>
+__global__ void __launch_bounds__(128) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
 {
     const uint32_t* queue = a.w.queue[qi];
     const uint32_t count = *(volatile uint32_t*)&a.w.counts[qi];
@@ -234,8 +238,10 @@ __global__ void __launch_bounds__(128, MINB) k_wf_extend(WaveArgs<Src> a, uint32
             const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
             Hit h;
-            hit = WW ? trace_closest_ww(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc)
-                     : trace_closest_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
+            if (TRAV == TRAV_BVH2_WW)
+                hit = trace_closest_ww(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
+            else
+                hit = trace_closest_inl<TRAV == TRAV_BVH4>(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, h, tc);
             a.w.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
             a.w.hit_prim[p] = hit ? h.prim : 0xFFFFFFFFu;
         }
@@ -394,8 +400,137 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_
     }
 }
 
-template <class Src, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_wf_shadow(WaveArgs<Src> a)
+// Persistent traversal with per-lane refill (the dynamic ray fetch of Aila &
+// Laine 2009): each lane keeps one ray's traversal state and advances it one
+// step per loop iteration; once at least `refill` lanes of the warp are idle
+// they take the next queue entries with one warp-aggregated atomic, so lanes
+// whose ray finished early do not wait for the warp's longest ray.  Every ray
+// is traversed exactly as by trace_closest_inl (same steps, same result).
+template <class Src, bool W4>
+__global__ void __launch_bounds__(128) k_wf_extend_refill(WaveArgs<Src> a, uint32_t qi, uint32_t refill)
+{
+    const uint32_t* queue = a.w.queue[qi];
+    const uint32_t count = *(volatile uint32_t*)&a.w.counts[qi];
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned lower = (1u << lane) - 1u;
+    TraceCounters tc{0u, 0u};
+    ClosestTrace t;
+    TraceStack stack;
+    const DevScene* sc = nullptr;
+    uint32_t p = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && (uint32_t)__popc(idle) >= refill) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader)
+                base = atomicAdd(&a.w.counts[3], (uint32_t)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            exhausted = base + (uint32_t)__popc(idle) >= count;
+            if (!active) {
+                const uint32_t i = base + (uint32_t)__popc(idle & lower);
+                if (i < count) {
+                    p = queue[i];
+                    sc = &a.src.args(a.src.job_of(p)).s;
+                    const float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
+                    closest_begin(*sc, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, t, stack);
+                    active = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        if (active && closest_step<W4>(*sc, t, stack, tc)) {
+            a.w.hit[p] = make_float4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.inst));
+            a.w.hit_prim[p] = t.found ? t.h.prim : 0xFFFFFFFFu;
+            active = false;
+        }
+    }
+    const uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
+    const uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
+    if (lane == 0) {
+        atomicAdd(a.src.counters() + 3, (unsigned long long)nodes);
+        atomicAdd(a.src.counters() + 4, (unsigned long long)tris);
+    }
+}
+
+// Adds the light term of shadow-queue entry p with visibility vis.
+template <class Src>
+__device__ __forceinline__ void finish_shadow_entry(WaveArgs<Src>& a, uint32_t p, float vis)
+{
+    NeeRequest nee;
+    nee.add = true;
+    nee.trace = true;
+    const float4 e = a.w.nee_e[p], b = a.w.nee_b[p], t = a.w.nee_tp[p];
+    nee.emission = mk3(e.x, e.y, e.z);
+    nee.cos_i = e.w;
+    nee.brdf = mk3(b.x, b.y, b.z);
+    nee.pdf = b.w;
+    nee.w = a.w.nee_d[p].w;
+    nee.tp_before = mk3(t.x, t.y, t.z);
+    const float4 r4 = a.w.rad[p];
+    f3 rad = mk3(r4.x, r4.y, r4.z);
+    finish_nee(rad, nee, vis);
+    a.w.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+}
+
+// Shadow rays with per-lane refill, as k_wf_extend_refill.
+template <class Src, bool W4>
+__global__ void __launch_bounds__(128) k_wf_shadow_refill(WaveArgs<Src> a, uint32_t refill)
+{
+    const uint32_t count = a.w.counts[2];
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned lower = (1u << lane) - 1u;
+    TraceCounters tc{0u, 0u};
+    ShadowTrace t;
+    TraceStack stack;
+    const DevScene* sc = nullptr;
+    uint32_t p = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && (uint32_t)__popc(idle) >= refill) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader)
+                base = atomicAdd(&a.w.counts[4], (uint32_t)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            exhausted = base + (uint32_t)__popc(idle) >= count;
+            if (!active) {
+                const uint32_t i = base + (uint32_t)__popc(idle & lower);
+                if (i < count) {
+                    p = a.w.shadow_queue[i];
+                    sc = &a.src.args(a.src.job_of(p)).s;
+                    const float4 o = a.w.nee_o[p], d = a.w.nee_d[p];
+                    shadow_begin(*sc, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, o.w, t, stack);
+                    active = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        if (active && shadow_step<W4>(*sc, t, stack, tc)) {
+            finish_shadow_entry(a, p, shadow_result(t));
+            active = false;
+        }
+    }
+    const uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
+    const uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
+    if (lane == 0) {
+        atomicAdd(a.src.counters() + 3, (unsigned long long)nodes);
+        atomicAdd(a.src.counters() + 4, (unsigned long long)tris);
+    }
+}
+
+template <class Src, bool W4>
+__global__ void __launch_bounds__(128) k_wf_shadow(WaveArgs<Src> a)
 {
     const uint32_t count = a.w.counts[2];
     unsigned lane = threadIdx.x & 31;
@@ -412,7 +547,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shadow(WaveArgs<Src> a)
             uint32_t p = a.w.shadow_queue[i];
             const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.nee_o[p], d = a.w.nee_d[p];
-            float vis = trace_shadow_inl(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, o.w, tc);
+            float vis = trace_shadow_inl<W4>(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, o.w, tc);
             NeeRequest nee;
             nee.add = true;
             nee.trace = true;
@@ -543,17 +678,20 @@ static inline uint32_t capped_grid(uint64_t threads, uint32_t block, int sm_coun
     return (uint32_t)(g < cap ? (g == 0 ? 1 : g) : cap);
 }
 
-// Launch variants of the stage kernels, fixed per process: the closest-hit
-// traversal (one node-or-leaf step per iteration, or while-while with
-// speculative leaves with PT_TRAVERSAL=ww: on the mid scene the latter ran
-// 24 % slower, its extra node visits and triangle tests costing more than the
-// coherence gained) and the resident-block targets of extend, shadow and
-// shade (PT_MINB="extend,shadow,shade", e.g. "8,8,5"; default none, the
-// occupancy their natural register counts give: 7, 7 and 4 blocks).  The alternatives stay for
+// Launch variants of the stage kernels, fixed per process: the BVH2
+// closest-hit traversal when the scene has no 4-wide nodes (one
+// node-or-leaf step per iteration, or while-while with speculative leaves
+// with PT_TRAVERSAL=ww: on the mid scene the latter ran 24 % slower, its
+// extra node visits and triangle tests costing more than the coherence
+// gained), the per-lane refill of the traversal kernels (PT_REFILL = idle
+// lanes that trigger a fetch, 1-32; 0 = whole-warp fetches of 32 rays) and
+// the resident-block target of shade (PT_MINB=5 or 6; default none, the
+// occupancy its natural register count gives).  The alternatives stay for
 // A/B measurements.
 struct StageVariant {
     bool ww = false;
-    int ext = 0, sh = 0, shade = 0; // 0: no resident-block target
+    int shade = 0;       // 0: no resident-block target
+    uint32_t refill = 0; // 0: no refill; else 1..32
 };
 
 static StageVariant stage_variant()
@@ -563,14 +701,12 @@ static StageVariant stage_variant()
         const char* t = std::getenv("PT_TRAVERSAL");
         r.ww = t && std::strcmp(t, "ww") == 0;
         const char* m = std::getenv("PT_MINB");
-        int e = 0, s = 0, h = 0;
-        if (m && std::sscanf(m, "%d,%d,%d", &e, &s, &h) == 3) {
-            r.ext = (e == 8 || e == 10) ? e : 0;
-            r.sh = (s == 8 || s == 10) ? s : 0;
-            r.shade = (h == 5 || h == 6) ? h : 0;
+        const int h = m ? std::atoi(m) : 0;
+        r.shade = (h == 5 || h == 6) ? h : 0;
+        if (const char* f = std::getenv("PT_REFILL")) {
+            const int k = std::atoi(f);
+            r.refill = k <= 0 ? 0u : (uint32_t)std::min(k, 32);
         }
-        if (r.ww)
-            r.ext = 0;
         return r;
     }();
     return v;
@@ -584,35 +720,57 @@ static int resident_blocks(K kernel)
     return b < 1 ? 1 : b;
 }
 
-// Resident 128-thread blocks per SM of the persistent traversal kernels of the
-// process's variant (queried once; thread-safe initialisation).
-template <class Src>
-static int2 traversal_blocks_per_sm()
+// The extend variant for scenes with (w4) or without 4-wide nodes.
+static int traversal_of(bool w4)
 {
-    static const int2 v = [] {
-        const StageVariant sv = stage_variant();
-        int e = sv.ww ? resident_blocks(k_wf_extend<Src, true, 0>)
-                      : sv.ext == 8 ? resident_blocks(k_wf_extend<Src, false, 8>)
-                      : sv.ext == 10 ? resident_blocks(k_wf_extend<Src, false, 10>)
-                                     : resident_blocks(k_wf_extend<Src, false, 0>);
-        int s = sv.sh == 8 ? resident_blocks(k_wf_shadow<Src, 8>)
-              : sv.sh == 10 ? resident_blocks(k_wf_shadow<Src, 10>)
-                            : resident_blocks(k_wf_shadow<Src, 0>);
-        return make_int2(e, s);
+    return w4 ? TRAV_BVH4 : stage_variant().ww ? TRAV_BVH2_WW : TRAV_BVH2;
+}
+
+// Whether the process's extend and shadow launches are the refill kernels
+// (the while-while BVH2 traversal has no refill form).
+static bool refill_for(bool w4)
+{
+    return stage_variant().refill != 0 && traversal_of(w4) != TRAV_BVH2_WW;
+}
+
+// Resident 128-thread blocks per SM of the persistent traversal kernels
+// (extend, shadow) the process launches for both node widths (queried once;
+// thread-safe initialisation).
+template <class Src>
+static int2 traversal_blocks_per_sm(bool w4)
+{
+    static const int4 v = [] {
+        int4 r;
+        if (refill_for(true)) {
+            r.x = resident_blocks(k_wf_extend_refill<Src, true>);
+            r.y = resident_blocks(k_wf_shadow_refill<Src, true>);
+        } else {
+            r.x = resident_blocks(k_wf_extend<Src, TRAV_BVH4>);
+            r.y = resident_blocks(k_wf_shadow<Src, true>);
+        }
+        if (refill_for(false)) {
+            r.z = resident_blocks(k_wf_extend_refill<Src, false>);
+            r.w = resident_blocks(k_wf_shadow_refill<Src, false>);
+        } else {
+            r.z = traversal_of(false) == TRAV_BVH2_WW ? resident_blocks(k_wf_extend<Src, TRAV_BVH2_WW>)
+                                                      : resident_blocks(k_wf_extend<Src, TRAV_BVH2>);
+            r.w = resident_blocks(k_wf_shadow<Src, false>);
+        }
+        return r;
     }();
-    return v;
+    return w4 ? make_int2(v.x, v.y) : make_int2(v.z, v.w);
 }
 
 cudaError_t wave_batch_prepare()
 {
-    traversal_blocks_per_sm<ManyJobs>();
+    traversal_blocks_per_sm<ManyJobs>(true);
     return cudaGetLastError();
 }
 
 // One wave: raygen, (extend, shade, shadow, reset) per segment, accumulate.
 template <class Src>
-static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32_t accum_threads, int sm_count, cudaStream_t st,
-                            StageTimer* tm = nullptr)
+static uint32_t launch_wave(const WaveArgs<Src>& a, bool w4, uint32_t max_bounces, uint32_t accum_threads, int sm_count,
+                            cudaStream_t st, StageTimer* tm = nullptr)
 {
     auto mark = [&](uint8_t s) {
         if (tm)
@@ -620,7 +778,9 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32
     };
     // persistent traversal grids: exactly the resident blocks of every SM
     const StageVariant sv = stage_variant();
-    const int2 per_sm = traversal_blocks_per_sm<Src>();
+    const int trav = traversal_of(w4);
+    const bool refill = refill_for(w4);
+    const int2 per_sm = traversal_blocks_per_sm<Src>(w4);
     const int trace_blocks = sm_count * per_sm.x;
     const int shadow_blocks = sm_count * per_sm.y;
     uint32_t nl = 0;
@@ -631,14 +791,16 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32
     const uint32_t sgrid = capped_grid(a.src.n_paths, 128, sm_count);
     for (uint32_t sg = 0; sg <= max_bounces; sg++) {
         mark(1);
-        if (sv.ww)
-            k_wf_extend<Src, true, 0><<<trace_blocks, 128, 0, st>>>(a, qi);
-        else if (sv.ext == 8)
-            k_wf_extend<Src, false, 8><<<trace_blocks, 128, 0, st>>>(a, qi);
-        else if (sv.ext == 10)
-            k_wf_extend<Src, false, 10><<<trace_blocks, 128, 0, st>>>(a, qi);
+        if (refill && w4)
+            k_wf_extend_refill<Src, true><<<trace_blocks, 128, 0, st>>>(a, qi, sv.refill);
+        else if (refill)
+            k_wf_extend_refill<Src, false><<<trace_blocks, 128, 0, st>>>(a, qi, sv.refill);
+        else if (trav == TRAV_BVH4)
+            k_wf_extend<Src, TRAV_BVH4><<<trace_blocks, 128, 0, st>>>(a, qi);
+        else if (trav == TRAV_BVH2_WW)
+            k_wf_extend<Src, TRAV_BVH2_WW><<<trace_blocks, 128, 0, st>>>(a, qi);
         else
-            k_wf_extend<Src, false, 0><<<trace_blocks, 128, 0, st>>>(a, qi);
+            k_wf_extend<Src, TRAV_BVH2><<<trace_blocks, 128, 0, st>>>(a, qi);
         mark(2);
         k_wf_split<Src><<<capped_grid(a.src.n_paths, 256, sm_count), 256, 0, st>>>(a, qi);
         if (sv.shade == 5)
@@ -648,12 +810,14 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, uint32_t max_bounces, uint32
         else
             k_wf_shade<Src, 0><<<sgrid, 128, 0, st>>>(a, qi);
         mark(3);
-        if (sv.sh == 8)
-            k_wf_shadow<Src, 8><<<shadow_blocks, 128, 0, st>>>(a);
-        else if (sv.sh == 10)
-            k_wf_shadow<Src, 10><<<shadow_blocks, 128, 0, st>>>(a);
+        if (refill && w4)
+            k_wf_shadow_refill<Src, true><<<shadow_blocks, 128, 0, st>>>(a, sv.refill);
+        else if (refill)
+            k_wf_shadow_refill<Src, false><<<shadow_blocks, 128, 0, st>>>(a, sv.refill);
+        else if (w4)
+            k_wf_shadow<Src, true><<<shadow_blocks, 128, 0, st>>>(a);
         else
-            k_wf_shadow<Src, 0><<<shadow_blocks, 128, 0, st>>>(a);
+            k_wf_shadow<Src, false><<<shadow_blocks, 128, 0, st>>>(a);
         mark(4);
         k_wf_reset<<<1, 1, 0, st>>>(a.w.counts, qi);
         nl += 5;
@@ -682,7 +846,7 @@ cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_byte
         a.src.samples = r.samples - done < k_max ? r.samples - done : k_max;
         a.src.first_sample = r.sample_index + done;
         a.src.n_paths = a.src.samples * a.src.pixels;
-        nl += launch_wave(a, r.max_bounces, a.src.pixels, sm_count, st, timer);
+        nl += launch_wave(a, r.s.nodes4 != nullptr, r.max_bounces, a.src.pixels, sm_count, st, timer);
         done += a.src.samples;
     }
     if (launches)
@@ -692,7 +856,7 @@ cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_byte
 
 cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shares, const BatchWave* waves, uint32_t wave_count,
                                    uint32_t* path_share, unsigned long long* counters, void* state, size_t state_bytes,
-                                   uint32_t n_paths_max, int sm_count, uint32_t* launches, cudaStream_t st)
+                                   uint32_t n_paths_max, bool w4, int sm_count, uint32_t* launches, cudaStream_t st)
 {
     WaveArgs<ManyJobs> a;
     if (!carve_state(a.w, state, state_bytes, n_paths_max))
@@ -709,7 +873,7 @@ cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shar
         a.src.share_count = bw.share_count;
         a.src.n_paths = bw.n_paths;
         a.src.n_pixels = bw.n_pixels;
-        nl += launch_wave(a, bw.max_bounces, bw.n_pixels, sm_count, st);
+        nl += launch_wave(a, w4, bw.max_bounces, bw.n_pixels, sm_count, st);
     }
     if (launches)
         *launches = nl;
