@@ -304,6 +304,15 @@ void pt_destroy(pt_ctx* c)
     c->mse_ref.release();
     c->mse_partial.release();
     c->wave_state.release();
+    c->wave_state2.release();
+    for (cudaEvent_t& ev : c->dual_ev)
+        if (ev) {
+            cudaEventDestroy(ev);
+            ev = nullptr;
+        }
+    if (c->side)
+        cudaStreamDestroy(c->side);
+    c->side = nullptr;
     c->texels.release();
     c->textures.release();
     c->feat_a.release();
@@ -677,6 +686,8 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     uint64_t pixels = (uint64_t)p->width * p->height;
     uint32_t kernel = p->kernel == PT_KERNEL_MEGA ? PT_KERNEL_MEGA : PT_KERNEL_WAVEFRONT;
     uint32_t launches = 0;
+    bool dual = false;
+    uint64_t wave_k = 1; // samples per wave
     if (kernel == PT_KERNEL_WAVEFRONT) {
         // Waves of k samples, k * pixels paths (at least one sample), at most
         // 2^n paths, n = PT_WAVE_PATHS_LOG2 (20..27, default 26: up to 15.6 GB
@@ -691,21 +702,53 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
             const int v = e ? std::atoi(e) : 26;
             return v < 20 ? 20 : (v > 27 ? 27 : v);
         }();
+        // Two sub-waves in flight (PT_DUAL_WAVES, default on): the samples
+        // are split over two path states, each at most an eighth of the free
+        // memory, and run on two streams.  Not with stage timing (one stream
+        // of events), nor with FP16 features: their running means are stored
+        // rounded after every wave, and one wave keeps them the FP32 means
+        // rounded once.
+        static const bool dual_env = [] {
+            const char* e = std::getenv("PT_DUAL_WAVES");
+            return !(e && e[0] == '0');
+        }();
+        dual = dual_env && !timing && !(p->flags & PT_RENDER_FEATURES_FP16) && p->samples >= 2;
         uint64_t cap = 1ull << wave_log2;
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
             const uint64_t per_path = wave_state_bytes(1u << 20) >> 20;
-            const uint64_t avail = (uint64_t)free_b + (uint64_t)c->wave_state.n;
-            cap = std::min<uint64_t>(cap, std::max<uint64_t>(avail / 4 / per_path, 1));
+            const uint64_t avail = (uint64_t)free_b + (uint64_t)c->wave_state.n + (uint64_t)c->wave_state2.n;
+            cap = std::min<uint64_t>(cap, std::max<uint64_t>(avail / (dual ? 8 : 4) / per_path, 1));
         }
-        uint64_t k = std::max<uint64_t>(1, std::min<uint64_t>(p->samples, cap / pixels));
+        const uint64_t per_state = dual ? (p->samples + 1) / 2 : p->samples;
+        uint64_t k = std::max<uint64_t>(1, std::min<uint64_t>(per_state, cap / pixels));
         uint64_t n = k * pixels;
         if (c->wave_paths < n) {
+            c->wave_state.release();
             cudaError_t e = c->wave_state.alloc(wave_state_bytes((uint32_t)n));
-            if (e != cudaSuccess)
+            if (e != cudaSuccess) {
+                c->wave_paths = 0;
                 return c->cuda_fail(e, "wavefront state allocation");
+            }
             c->wave_paths = (uint32_t)n;
         }
+        if (dual && c->wave_paths2 < n) {
+            c->wave_state2.release();
+            cudaError_t e = c->wave_state2.alloc(wave_state_bytes((uint32_t)n));
+            if (e != cudaSuccess) {
+                c->wave_paths2 = 0;
+                return c->cuda_fail(e, "wavefront state allocation");
+            }
+            c->wave_paths2 = (uint32_t)n;
+        }
+        if (dual && !c->side) {
+            cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+            for (int i = 0; i < 4 && e == cudaSuccess; i++)
+                e = cudaEventCreateWithFlags(&c->dual_ev[i], cudaEventDisableTiming);
+            if (e != cudaSuccess)
+                return c->cuda_fail(e, "second wave stream");
+        }
+        wave_k = k;
     }
     cudaEventRecord(c->ev0, c->stream);
     if (kernel == PT_KERNEL_MEGA) {
@@ -722,7 +765,7 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     } else {
         a.sample_index = p->sample_index;
         a.samples = p->samples;
-        uint32_t n_paths = (uint32_t)(std::min<uint64_t>(c->wave_paths / pixels, p->samples) * pixels);
+        uint32_t n_paths = (uint32_t)(wave_k * pixels);
         StageTimer timer;
         if (timing) {
             // waves x ((bounces + 1) x 4 + 2) launches, one event before each and one at the end
@@ -742,8 +785,9 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
             timer.stage = c->stage_of.data();
             timer.capacity = (uint32_t)c->stage_events.size();
         }
+        WaveDual wd{c->wave_state2.p, c->wave_state2.n, c->side, c->dual_ev[0], c->dual_ev[1], {c->dual_ev[2], c->dual_ev[3]}};
         cudaError_t e = launch_wavefront(a, c->wave_state.p, c->wave_state.n, n_paths, c->sm_count, &launches, c->stream,
-                                         timing ? &timer : nullptr);
+                                         timing ? &timer : nullptr, dual ? &wd : nullptr);
         if (e != cudaSuccess)
             return c->cuda_fail(e, "wavefront launch");
         stage_marks = timer.count;

@@ -93,6 +93,10 @@ struct pt_ctx {
     DevBuf<unsigned long long> counters;
     DevBuf<uint32_t> error_word;
     DevBuf<char> wave_state;    // wavefront path state
+    DevBuf<char> wave_state2;   // second sub-wave's path state (two waves in flight)
+    uint32_t wave_paths2 = 0;
+    cudaStream_t side = nullptr; // second sub-wave's stream, created on first use
+    cudaEvent_t dual_ev[4] = {}; // fork, join, accumulation order (2)
     uint32_t wave_paths = 0;    // paths the wave state holds
     int sm_count = 0;
     pt_render_params camera{};  // pt_set_camera state

@@ -768,9 +768,12 @@ cudaError_t wave_batch_prepare()
 }
 
 // One wave: raygen, (extend, shade, shadow, reset) per segment, accumulate.
+// acc_wait / acc_done (optional) order the accumulation after an earlier
+// wave's on another stream and mark its completion.
 template <class Src>
 static uint32_t launch_wave(const WaveArgs<Src>& a, bool w4, uint32_t max_bounces, uint32_t accum_threads, int sm_count,
-                            cudaStream_t st, StageTimer* tm = nullptr)
+                            cudaStream_t st, StageTimer* tm = nullptr, cudaEvent_t acc_wait = nullptr,
+                            cudaEvent_t acc_done = nullptr)
 {
     auto mark = [&](uint8_t s) {
         if (tm)
@@ -824,30 +827,52 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, bool w4, uint32_t max_bounce
         qi ^= 1;
     }
     mark(5);
+    if (acc_wait)
+        cudaStreamWaitEvent(st, acc_wait, 0);
     k_wf_accumulate<Src><<<capped_grid(accum_threads, 256, sm_count), 256, 0, st>>>(a);
+    if (acc_done)
+        cudaEventRecord(acc_done, st);
     nl++;
     mark(6);
     return nl;
 }
 
 cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
-                             uint32_t* launches, cudaStream_t st, StageTimer* timer)
+                             uint32_t* launches, cudaStream_t st, StageTimer* timer, const WaveDual* dual)
 {
-    WaveArgs<OneJob> a;
-    a.src.r = r;
-    if (!carve_state(a.w, state, state_bytes, n_paths_max))
+    WaveArgs<OneJob> a[2];
+    a[0].src.r = r;
+    if (!carve_state(a[0].w, state, state_bytes, n_paths_max))
         return cudaErrorInvalidValue;
-    a.src.pixels = r.width * r.height;
-    uint32_t k_max = n_paths_max / a.src.pixels;
+    a[0].src.pixels = r.width * r.height;
+    const uint32_t k_max = n_paths_max / a[0].src.pixels;
     if (k_max == 0)
         return cudaErrorInvalidValue;
-    uint32_t nl = 0;
-    for (uint32_t done = 0; done < r.samples;) {
-        a.src.samples = r.samples - done < k_max ? r.samples - done : k_max;
-        a.src.first_sample = r.sample_index + done;
-        a.src.n_paths = a.src.samples * a.src.pixels;
-        nl += launch_wave(a, r.s.nodes4 != nullptr, r.max_bounces, a.src.pixels, sm_count, st, timer);
-        done += a.src.samples;
+    const bool two = dual != nullptr && timer == nullptr && r.samples > k_max;
+    if (two) {
+        a[1] = a[0];
+        if (!carve_state(a[1].w, dual->state2, dual->state2_bytes, n_paths_max))
+            return cudaErrorInvalidValue;
+        cudaEventRecord(dual->fork, st);
+        cudaStreamWaitEvent(dual->side, dual->fork, 0);
+    }
+    const bool w4 = r.s.nodes4 != nullptr;
+    uint32_t nl = 0, w = 0;
+    for (uint32_t done = 0; done < r.samples; w++) {
+        WaveArgs<OneJob>& x = a[two ? (w & 1) : 0];
+        x.src.samples = r.samples - done < k_max ? r.samples - done : k_max;
+        x.src.first_sample = r.sample_index + done;
+        x.src.n_paths = x.src.samples * x.src.pixels;
+        if (two)
+            nl += launch_wave(x, w4, r.max_bounces, x.src.pixels, sm_count, (w & 1) ? dual->side : st, nullptr,
+                              w ? dual->acc[(w - 1) & 1] : nullptr, dual->acc[w & 1]);
+        else
+            nl += launch_wave(x, w4, r.max_bounces, x.src.pixels, sm_count, st, timer);
+        done += x.src.samples;
+    }
+    if (two) {
+        cudaEventRecord(dual->join, dual->side);
+        cudaStreamWaitEvent(st, dual->join, 0);
     }
     if (launches)
         *launches = nl;
