@@ -304,15 +304,17 @@ void pt_destroy(pt_ctx* c)
     c->mse_ref.release();
     c->mse_partial.release();
     c->wave_state.release();
-    c->wave_state2.release();
-    for (cudaEvent_t& ev : c->dual_ev)
-        if (ev) {
-            cudaEventDestroy(ev);
-            ev = nullptr;
-        }
-    if (c->side)
-        cudaStreamDestroy(c->side);
-    c->side = nullptr;
+    for (int k = 0; k < pt::MAX_WAVE_WAYS; k++) {
+        c->wave_state_x[k].release();
+        if (c->side[k])
+            cudaStreamDestroy(c->side[k]);
+        if (c->wave_join[k])
+            cudaEventDestroy(c->wave_join[k]);
+        if (c->wave_acc[k])
+            cudaEventDestroy(c->wave_acc[k]);
+    }
+    if (c->wave_fork)
+        cudaEventDestroy(c->wave_fork);
     c->texels.release();
     c->textures.release();
     c->feat_a.release();
@@ -686,7 +688,7 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     uint64_t pixels = (uint64_t)p->width * p->height;
     uint32_t kernel = p->kernel == PT_KERNEL_MEGA ? PT_KERNEL_MEGA : PT_KERNEL_WAVEFRONT;
     uint32_t launches = 0;
-    bool dual = false;
+    int ways = 1;        // sub-waves in flight
     uint64_t wave_k = 1; // samples per wave
     if (kernel == PT_KERNEL_WAVEFRONT) {
         // Waves of k samples, k * pixels paths (at least one sample), at most
@@ -702,25 +704,28 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
             const int v = e ? std::atoi(e) : 26;
             return v < 20 ? 20 : (v > 27 ? 27 : v);
         }();
-        // Two sub-waves in flight (PT_DUAL_WAVES, default on): the samples
-        // are split over two path states, each at most an eighth of the free
-        // memory, and run on two streams.  Not with stage timing (one stream
-        // of events), nor with FP16 features: their running means are stored
-        // rounded after every wave, and one wave keeps them the FP32 means
-        // rounded once.
-        static const bool dual_env = [] {
-            const char* e = std::getenv("PT_DUAL_WAVES");
-            return !(e && e[0] == '0');
+        // Sub-waves in flight (PT_WAVE_STREAMS, 1-4, default 2): the samples
+        // are split over that many path states, each at most 1/(4 x ways) of
+        // the free memory, run on as many streams.  Not with stage timing
+        // (one stream of events), nor with FP16 features: their running means
+        // are stored rounded after every wave, and one wave keeps them the
+        // FP32 means rounded once.
+        static const int ways_env = [] {
+            const char* e = std::getenv("PT_WAVE_STREAMS");
+            const int v = e ? std::atoi(e) : 2;
+            return v < 1 ? 1 : (v > pt::MAX_WAVE_WAYS ? pt::MAX_WAVE_WAYS : v);
         }();
-        dual = dual_env && !timing && !(p->flags & PT_RENDER_FEATURES_FP16) && p->samples >= 2;
+        ways = (timing || (p->flags & PT_RENDER_FEATURES_FP16)) ? 1 : (int)std::min<uint64_t>(ways_env, p->samples);
         uint64_t cap = 1ull << wave_log2;
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
             const uint64_t per_path = wave_state_bytes(1u << 20) >> 20;
-            const uint64_t avail = (uint64_t)free_b + (uint64_t)c->wave_state.n + (uint64_t)c->wave_state2.n;
-            cap = std::min<uint64_t>(cap, std::max<uint64_t>(avail / (dual ? 8 : 4) / per_path, 1));
+            uint64_t avail = (uint64_t)free_b + (uint64_t)c->wave_state.n;
+            for (int k = 1; k < pt::MAX_WAVE_WAYS; k++)
+                avail += (uint64_t)c->wave_state_x[k].n;
+            cap = std::min<uint64_t>(cap, std::max<uint64_t>(avail / (4 * (uint64_t)ways) / per_path, 1));
         }
-        const uint64_t per_state = dual ? (p->samples + 1) / 2 : p->samples;
+        const uint64_t per_state = (p->samples + ways - 1) / ways;
         uint64_t k = std::max<uint64_t>(1, std::min<uint64_t>(per_state, cap / pixels));
         uint64_t n = k * pixels;
         if (c->wave_paths < n) {
@@ -732,21 +737,33 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
             }
             c->wave_paths = (uint32_t)n;
         }
-        if (dual && c->wave_paths2 < n) {
-            c->wave_state2.release();
-            cudaError_t e = c->wave_state2.alloc(wave_state_bytes((uint32_t)n));
-            if (e != cudaSuccess) {
-                c->wave_paths2 = 0;
-                return c->cuda_fail(e, "wavefront state allocation");
+        for (int k = 1; k < ways; k++) {
+            if (c->wave_paths_x[k] < n) {
+                c->wave_state_x[k].release();
+                cudaError_t e = c->wave_state_x[k].alloc(wave_state_bytes((uint32_t)n));
+                if (e != cudaSuccess) {
+                    c->wave_paths_x[k] = 0;
+                    return c->cuda_fail(e, "wavefront state allocation");
+                }
+                c->wave_paths_x[k] = (uint32_t)n;
             }
-            c->wave_paths2 = (uint32_t)n;
-        }
-        if (dual && !c->side) {
-            cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
-            for (int i = 0; i < 4 && e == cudaSuccess; i++)
-                e = cudaEventCreateWithFlags(&c->dual_ev[i], cudaEventDisableTiming);
+            cudaError_t e = cudaSuccess;
+            if (!c->side[k])
+                e = cudaStreamCreateWithFlags(&c->side[k], cudaStreamNonBlocking);
+            if (e == cudaSuccess && !c->wave_join[k])
+                e = cudaEventCreateWithFlags(&c->wave_join[k], cudaEventDisableTiming);
             if (e != cudaSuccess)
-                return c->cuda_fail(e, "second wave stream");
+                return c->cuda_fail(e, "sub-wave stream");
+        }
+        if (ways > 1) {
+            cudaError_t e = cudaSuccess;
+            if (!c->wave_fork)
+                e = cudaEventCreateWithFlags(&c->wave_fork, cudaEventDisableTiming);
+            for (int k = 0; k < ways && e == cudaSuccess; k++)
+                if (!c->wave_acc[k])
+                    e = cudaEventCreateWithFlags(&c->wave_acc[k], cudaEventDisableTiming);
+            if (e != cudaSuccess)
+                return c->cuda_fail(e, "sub-wave events");
         }
         wave_k = k;
     }
@@ -785,9 +802,18 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
             timer.stage = c->stage_of.data();
             timer.capacity = (uint32_t)c->stage_events.size();
         }
-        WaveDual wd{c->wave_state2.p, c->wave_state2.n, c->side, c->dual_ev[0], c->dual_ev[1], {c->dual_ev[2], c->dual_ev[3]}};
+        WaveMulti wm{};
+        wm.ways = ways;
+        wm.fork = c->wave_fork;
+        for (int k = 0; k < ways; k++) {
+            wm.state[k] = k ? c->wave_state_x[k].p : c->wave_state.p;
+            wm.state_bytes[k] = k ? c->wave_state_x[k].n : c->wave_state.n;
+            wm.stream[k] = k ? c->side[k] : c->stream;
+            wm.join[k] = c->wave_join[k];
+            wm.acc[k] = c->wave_acc[k];
+        }
         cudaError_t e = launch_wavefront(a, c->wave_state.p, c->wave_state.n, n_paths, c->sm_count, &launches, c->stream,
-                                         timing ? &timer : nullptr, dual ? &wd : nullptr);
+                                         timing ? &timer : nullptr, ways > 1 ? &wm : nullptr);
         if (e != cudaSuccess)
             return c->cuda_fail(e, "wavefront launch");
         stage_marks = timer.count;

@@ -11,6 +11,7 @@
 
 #include "../../include/pt_gpu.h"
 #include "device/render.cuh"
+#include "kernels.h"
 
 namespace pt {
 struct BatchState; // batch.cu
@@ -93,10 +94,12 @@ struct pt_ctx {
     DevBuf<unsigned long long> counters;
     DevBuf<uint32_t> error_word;
     DevBuf<char> wave_state;    // wavefront path state
-    DevBuf<char> wave_state2;   // second sub-wave's path state (two waves in flight)
-    uint32_t wave_paths2 = 0;
-    cudaStream_t side = nullptr; // second sub-wave's stream, created on first use
-    cudaEvent_t dual_ev[4] = {}; // fork, join, accumulation order (2)
+    // further sub-waves in flight (index 0 unused: wave_state and stream);
+    // streams and events are created on first use
+    DevBuf<char> wave_state_x[pt::MAX_WAVE_WAYS];
+    uint32_t wave_paths_x[pt::MAX_WAVE_WAYS] = {};
+    cudaStream_t side[pt::MAX_WAVE_WAYS] = {};
+    cudaEvent_t wave_fork = nullptr, wave_join[pt::MAX_WAVE_WAYS] = {}, wave_acc[pt::MAX_WAVE_WAYS] = {};
     uint32_t wave_paths = 0;    // paths the wave state holds
     int sm_count = 0;
     pt_render_params camera{};  // pt_set_camera state

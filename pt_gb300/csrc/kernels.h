@@ -42,21 +42,24 @@ constexpr int STAGE_COUNT = 6;
 // bytes of path state for up to n_paths_max paths (a multiple of the pixel
 // count); r.samples samples are rendered in waves of n_paths_max / pixels.
 size_t wave_state_bytes(uint32_t n_paths_max);
-// Two sub-waves in flight: a second path state of the same size and a second
-// stream.  Waves alternate between (stream, state) and (side, state2), so the
-// ragged end of one wave's launches overlaps the other wave's work; the
-// accumulation kernels run in wave order (events acc[0..1]), which keeps the
-// running mean, FP64 sums, feature means and snapshot exactly those of one
-// stream.  fork/join tie `side` to `stream` before and after.
-struct WaveDual {
-    void* state2;
-    size_t state2_bytes;
-    cudaStream_t side;
-    cudaEvent_t fork, join, acc[2];
+// Several sub-waves in flight: `ways` path states of the same size, each
+// with its own stream (state[0] / stream[0] are the launch's own).  Waves go
+// round-robin over them, so the ragged end of one wave's launches overlaps
+// the others' work; the accumulation kernels run in wave order (events
+// acc[]), which keeps the running mean, FP64 sums, feature means and
+// snapshot exactly those of one stream.  fork / join[] tie the extra streams
+// to the launch's stream before and after.
+constexpr int MAX_WAVE_WAYS = 4;
+struct WaveMulti {
+    int ways;
+    void* state[MAX_WAVE_WAYS];
+    size_t state_bytes[MAX_WAVE_WAYS];
+    cudaStream_t stream[MAX_WAVE_WAYS];
+    cudaEvent_t fork, join[MAX_WAVE_WAYS], acc[MAX_WAVE_WAYS];
 };
 cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
                              uint32_t* launches, cudaStream_t stream, StageTimer* timer = nullptr,
-                             const WaveDual* dual = nullptr);
+                             const WaveMulti* multi = nullptr);
 cudaError_t wave_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
 
 // Batched wavefront: waves hold shares of several jobs (RenderArgs in device

@@ -838,9 +838,9 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, bool w4, uint32_t max_bounce
 }
 
 cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_bytes, uint32_t n_paths_max, int sm_count,
-                             uint32_t* launches, cudaStream_t st, StageTimer* timer, const WaveDual* dual)
+                             uint32_t* launches, cudaStream_t st, StageTimer* timer, const WaveMulti* multi)
 {
-    WaveArgs<OneJob> a[2];
+    WaveArgs<OneJob> a[MAX_WAVE_WAYS];
     a[0].src.r = r;
     if (!carve_state(a[0].w, state, state_bytes, n_paths_max))
         return cudaErrorInvalidValue;
@@ -848,31 +848,41 @@ cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_byte
     const uint32_t k_max = n_paths_max / a[0].src.pixels;
     if (k_max == 0)
         return cudaErrorInvalidValue;
-    const bool two = dual != nullptr && timer == nullptr && r.samples > k_max;
-    if (two) {
-        a[1] = a[0];
-        if (!carve_state(a[1].w, dual->state2, dual->state2_bytes, n_paths_max))
+    // ways in use: no more than the waves the render needs
+    const uint32_t waves = (r.samples + k_max - 1) / k_max;
+    int ways = 1;
+    if (multi != nullptr && timer == nullptr && multi->ways > 1 && multi->ways <= MAX_WAVE_WAYS)
+        ways = (int)(waves < (uint32_t)multi->ways ? waves : (uint32_t)multi->ways);
+    for (int k = 1; k < ways; k++) {
+        a[k] = a[0];
+        if (!carve_state(a[k].w, multi->state[k], multi->state_bytes[k], n_paths_max))
             return cudaErrorInvalidValue;
-        cudaEventRecord(dual->fork, st);
-        cudaStreamWaitEvent(dual->side, dual->fork, 0);
+    }
+    if (ways > 1) {
+        cudaEventRecord(multi->fork, st);
+        for (int k = 1; k < ways; k++)
+            cudaStreamWaitEvent(multi->stream[k], multi->fork, 0);
     }
     const bool w4 = r.s.nodes4 != nullptr;
     uint32_t nl = 0, w = 0;
     for (uint32_t done = 0; done < r.samples; w++) {
-        WaveArgs<OneJob>& x = a[two ? (w & 1) : 0];
+        const int k = (int)(w % (uint32_t)ways);
+        WaveArgs<OneJob>& x = a[k];
         x.src.samples = r.samples - done < k_max ? r.samples - done : k_max;
         x.src.first_sample = r.sample_index + done;
         x.src.n_paths = x.src.samples * x.src.pixels;
-        if (two)
-            nl += launch_wave(x, w4, r.max_bounces, x.src.pixels, sm_count, (w & 1) ? dual->side : st, nullptr,
-                              w ? dual->acc[(w - 1) & 1] : nullptr, dual->acc[w & 1]);
+        if (ways > 1)
+            nl += launch_wave(x, w4, r.max_bounces, x.src.pixels, sm_count, k ? multi->stream[k] : st, nullptr,
+                              w ? multi->acc[(w - 1) % (uint32_t)ways] : nullptr, multi->acc[k]);
         else
             nl += launch_wave(x, w4, r.max_bounces, x.src.pixels, sm_count, st, timer);
         done += x.src.samples;
     }
-    if (two) {
-        cudaEventRecord(dual->join, dual->side);
-        cudaStreamWaitEvent(st, dual->join, 0);
+    if (ways > 1) {
+        for (int k = 1; k < ways; k++) {
+            cudaEventRecord(multi->join[k], multi->stream[k]);
+            cudaStreamWaitEvent(st, multi->join[k], 0);
+        }
     }
     if (launches)
         *launches = nl;
