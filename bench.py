@@ -555,6 +555,8 @@ def run_ours(args) -> None:
                 "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB write, outside the event pairs)",
                            "parallelism": f"replicas x{world} (disjoint sample ranges)",
                            "kernel": {1: "megakernel", 2: "wavefront"}.get(st.kernel_used, str(st.kernel_used)),
+                           "wave_streams": "timed steps: 1 (per-launch stage events need one stream); e2e and "
+                                           "time_to_mse: the library default (PT_WAVE_STREAMS, 2)",
                            "segments_per_step": int(segs_per_step), "accel_build_ms": info.build_ms,
                            "image": f"{WIDTH}x{HEIGHT}", "spp": SPP,
                            "node_visits_per_ray": st.node_visits / max(1, st.segments + st.shadow_rays),
