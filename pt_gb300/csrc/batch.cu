@@ -49,6 +49,12 @@ struct BatchState {
     DevBuf<uint32_t> path_share;
     DevBuf<char> state;
     uint32_t state_paths = 0;
+    // the second wave state in flight (plans of two or more waves), on wave_side
+    DevBuf<char> state2;
+    DevBuf<uint32_t> path_share2;
+    uint32_t state2_paths = 0;
+    cudaStream_t wave_side = nullptr;
+    cudaEvent_t wfork = nullptr, wjoin = nullptr, wacc[2] = {nullptr, nullptr};
     bool w4 = true; // every job's scene has 4-wide nodes (else the BVH2 kernels run)
     DevBuf<unsigned long long> counters;
     DevBuf<uint32_t> error_word;
@@ -71,13 +77,17 @@ void batch_free(BatchState* b)
     b->shares.release();
     b->path_share.release();
     b->state.release();
+    b->state2.release();
+    b->path_share2.release();
     b->counters.release();
     b->error_word.release();
     if (b->exec)
         cudaGraphExecDestroy(b->exec);
     if (b->side)
         cudaStreamDestroy(b->side);
-    for (cudaEvent_t e : {b->fork, b->join, b->ev0, b->ev1})
+    if (b->wave_side)
+        cudaStreamDestroy(b->wave_side);
+    for (cudaEvent_t e : {b->fork, b->join, b->ev0, b->ev1, b->wfork, b->wjoin, b->wacc[0], b->wacc[1]})
         if (e)
             cudaEventDestroy(e);
     delete b;
@@ -245,6 +255,15 @@ int prepare(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vecto
             e = b->path_share.alloc(capacity);
         b->state_paths = e == cudaSuccess ? capacity : 0;
     }
+    // a second state for plans of two or more waves (they alternate over two streams)
+    if (e == cudaSuccess && plan.waves.size() >= 2 && b->state2_paths != capacity) {
+        b->state2.release();
+        b->path_share2.release();
+        e = b->state2.alloc(wave_state_bytes(capacity));
+        if (e == cudaSuccess)
+            e = b->path_share2.alloc(capacity);
+        b->state2_paths = e == cudaSuccess ? capacity : 0;
+    }
     if (e != cudaSuccess)
         return c->cuda_fail(e, "batch allocation");
     e = cudaMemcpyAsync(b->jobs.p, args.data(), args.size() * sizeof(RenderArgs), cudaMemcpyHostToDevice, c->stream);
@@ -298,8 +317,21 @@ cudaError_t issue(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std:
     }
     if (!plan.waves.empty()) {
         uint32_t wl = 0;
+        WaveMulti wm{};
+        const bool two = plan.waves.size() >= 2 && b->state2_paths == b->state_paths;
+        if (two) {
+            wm.ways = 2;
+            wm.state[1] = b->state2.p;
+            wm.state_bytes[1] = b->state2.n;
+            wm.stream[1] = b->wave_side;
+            wm.fork = b->wfork;
+            wm.join[1] = b->wjoin;
+            wm.acc[0] = b->wacc[0];
+            wm.acc[1] = b->wacc[1];
+        }
         e = launch_wavefront_batch(b->jobs.p, b->shares.p, plan.waves.data(), (uint32_t)plan.waves.size(), b->path_share.p,
-                                   b->counters.p, b->state.p, b->state.n, b->state_paths, b->w4, c->sm_count, &wl, st);
+                                   b->counters.p, b->state.p, b->state.n, b->state_paths, b->w4, c->sm_count, &wl, st,
+                                   two ? &wm : nullptr, two ? b->path_share2.p : nullptr);
         if (e != cudaSuccess)
             return e;
         nl += wl;
@@ -347,11 +379,11 @@ int tune(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vector<p
         max_px = std::max<uint64_t>(max_px, (uint64_t)q.width * q.height);
     float best_ms = 0.0f;
     bool have = false;
-    // capacities whose path state would take more than a quarter of the free memory are skipped
+    // capacities whose two path states would take more than a quarter of the free memory are skipped
     size_t free_b = 0, total_b = 0;
     uint64_t mem_paths = ~0ull;
     if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
-        mem_paths = ((uint64_t)free_b + (uint64_t)b->state.n) / 4 / (wave_state_bytes(1u << 20) >> 20);
+        mem_paths = ((uint64_t)free_b + (uint64_t)b->state.n + (uint64_t)b->state2.n) / 8 / (wave_state_bytes(1u << 20) >> 20);
     auto consider = [&](const BatchChoice& ch) -> int {
         if (max_px > ch.capacity)
             return PT_OK; // the largest job would not fit a wave
@@ -440,7 +472,9 @@ int pt_render_batch(pt_ctx* c, const pt_batch_job* jobs, uint32_t count, uint32_
         if (!b)
             return c->fail(PT_ERR_OOM, "batch state");
         cudaError_t e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
-        for (cudaEvent_t* ev : {&b->fork, &b->join})
+        if (e == cudaSuccess)
+            e = cudaStreamCreateWithFlags(&b->wave_side, cudaStreamNonBlocking);
+        for (cudaEvent_t* ev : {&b->fork, &b->join, &b->wfork, &b->wjoin, &b->wacc[0], &b->wacc[1]})
             if (e == cudaSuccess)
                 e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
         for (cudaEvent_t* ev : {&b->ev0, &b->ev1})

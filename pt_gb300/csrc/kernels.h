@@ -79,11 +79,15 @@ struct BatchWave {
 // `path_share` holds n_paths_max u32; `waves` is host memory (the launch
 // sequence is fixed by it, so the whole call can be captured in a graph).
 // w4: every job's scene has 4-wide nodes (the 4-wide traversal kernels run).
+// multi (optional, ways <= 2 used): a second path state with its own
+// path_share2 array and stream; waves alternate over the two as in
+// launch_wavefront, accumulation in wave order.
 // Occupancy queries of the batched kernels; call before capturing a batch.
 cudaError_t wave_batch_prepare();
 cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shares, const BatchWave* waves, uint32_t wave_count,
                                    uint32_t* path_share, unsigned long long* counters, void* state, size_t state_bytes,
-                                   uint32_t n_paths_max, bool w4, int sm_count, uint32_t* launches, cudaStream_t stream);
+                                   uint32_t n_paths_max, bool w4, int sm_count, uint32_t* launches, cudaStream_t stream,
+                                   const WaveMulti* multi = nullptr, uint32_t* path_share2 = nullptr);
 cudaError_t features_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
 
 // Denoiser features and packing (features.cu).

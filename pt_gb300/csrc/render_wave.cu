@@ -891,24 +891,43 @@ cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_byte
 
 cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shares, const BatchWave* waves, uint32_t wave_count,
                                    uint32_t* path_share, unsigned long long* counters, void* state, size_t state_bytes,
-                                   uint32_t n_paths_max, bool w4, int sm_count, uint32_t* launches, cudaStream_t st)
+                                   uint32_t n_paths_max, bool w4, int sm_count, uint32_t* launches, cudaStream_t st,
+                                   const WaveMulti* multi, uint32_t* path_share2)
 {
-    WaveArgs<ManyJobs> a;
-    if (!carve_state(a.w, state, state_bytes, n_paths_max))
+    WaveArgs<ManyJobs> a[2];
+    if (!carve_state(a[0].w, state, state_bytes, n_paths_max))
         return cudaErrorInvalidValue;
-    a.src.jobs = jobs;
-    a.src.path_share = path_share;
-    a.src.ctr = counters;
+    a[0].src.jobs = jobs;
+    a[0].src.path_share = path_share;
+    a[0].src.ctr = counters;
+    const int ways = (multi != nullptr && multi->ways >= 2 && path_share2 != nullptr && wave_count >= 2) ? 2 : 1;
+    if (ways == 2) {
+        a[1] = a[0];
+        a[1].src.path_share = path_share2;
+        if (!carve_state(a[1].w, multi->state[1], multi->state_bytes[1], n_paths_max))
+            return cudaErrorInvalidValue;
+        cudaEventRecord(multi->fork, st);
+        cudaStreamWaitEvent(multi->stream[1], multi->fork, 0);
+    }
     uint32_t nl = 0;
     for (uint32_t i = 0; i < wave_count; i++) {
         const BatchWave& bw = waves[i];
         if (bw.n_paths > n_paths_max || bw.share_count == 0)
             return cudaErrorInvalidValue;
-        a.src.shares = shares + bw.share_offset;
-        a.src.share_count = bw.share_count;
-        a.src.n_paths = bw.n_paths;
-        a.src.n_pixels = bw.n_pixels;
-        nl += launch_wave(a, w4, bw.max_bounces, bw.n_pixels, sm_count, st);
+        WaveArgs<ManyJobs>& x = a[ways == 2 ? (i & 1) : 0];
+        x.src.shares = shares + bw.share_offset;
+        x.src.share_count = bw.share_count;
+        x.src.n_paths = bw.n_paths;
+        x.src.n_pixels = bw.n_pixels;
+        if (ways == 2)
+            nl += launch_wave(x, w4, bw.max_bounces, bw.n_pixels, sm_count, (i & 1) ? multi->stream[1] : st, nullptr,
+                              i ? multi->acc[(i - 1) & 1] : nullptr, multi->acc[i & 1]);
+        else
+            nl += launch_wave(x, w4, bw.max_bounces, bw.n_pixels, sm_count, st);
+    }
+    if (ways == 2) {
+        cudaEventRecord(multi->join[1], multi->stream[1]);
+        cudaStreamWaitEvent(st, multi->join[1], 0);
     }
     if (launches)
         *launches = nl;
