@@ -329,6 +329,46 @@ def test_wavefront_many_waves(ctx, small, tmp_path):
     assert np.array_equal(gpu.view(np.uint32), mega.view(np.uint32))
 
 
+_VARIANT = """
+import sys, numpy as np, pathlib
+import pt_gb300 as P
+from pt_gb300 import abi, scenes
+hs = P.HostScene.load(scenes.mid_scene(pathlib.Path(sys.argv[1]), seed=1))
+ctx = P.Context(0)
+ctx.upload(hs.pack())
+ctx.build_accel()
+st = ctx.render(hs.render_params(256, 192, 6, 8, accum_mode=abi.PT_ACCUM_FP32_FP64))
+assert st.error_word == 0
+np.save(sys.argv[2], ctx.read_image())
+np.save(sys.argv[3], ctx.read_image(fp64=True))
+"""
+
+
+@pytest.mark.parametrize("env", [{"PT_WAVE_STREAMS": "1"}, {"PT_WAVE_STREAMS": "3"}, {"PT_BVH_WIDTH": "2"},
+                                 {"PT_REFILL": "16"}, {"PT_BVH_WIDTH": "2", "PT_TRAVERSAL": "ww"},
+                                 {"PT_WAVE_PATHS_LOG2": "20"}],
+                         ids=["one_stream", "three_streams", "bvh2", "refill", "bvh2_while_while", "small_waves"])
+def test_execution_variants_agree(ctx, mid, tmp_path, env):
+    """Every execution variant (sub-wave streams, node width, traversal
+    order, lane refill, wave size; each read once per process, so set in a
+    child) renders the same image and FP64 sums bit for bit as the default."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    a, b = tmp_path / "img.npy", tmp_path / "sums.npy"
+    r = subprocess.run([sys.executable, "-c", _VARIANT, str(tmp_path / "scene"), str(a), str(b)],
+                       env=dict(os.environ, **env), cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    hs, view = mid
+    ctx.upload(view)
+    ctx.build_accel()
+    ctx.render(hs.render_params(256, 192, 6, 8, accum_mode=abi.PT_ACCUM_FP32_FP64))
+    assert np.array_equal(np.load(a).view(np.uint32), ctx.read_image().view(np.uint32))
+    assert np.array_equal(np.load(b), ctx.read_image(fp64=True))
+
+
 def test_kernels_agree_on_counts(ctx, mid):
     hs, view = mid
     ctx.upload(view)
