@@ -115,9 +115,8 @@ __device__ __forceinline__ float pt_cos(float x)
 // ---------------------------------------------------------------- sampler
 // Owen-scrambled Sobol' sampler of shaders/pathtrace/sample.hlsli:94-166
 // (Burley 2020 with the Laine-Karras permutation).  The 4x32 direction
-// numbers live in constant memory (one copy per translation unit), filled
-// by the host from Joe & Kuo's primitive polynomials.
-static __constant__ uint32_t c_sobol[4][32];
+// numbers come from the host (Joe & Kuo's primitive polynomials) as byte
+// tables (g_sobol_bytes below, one copy per translation unit).
 
 __device__ __forceinline__ uint32_t hash_combine(uint32_t seed, uint32_t x) { return seed ^ (x + (seed << 6) + (seed >> 2)); }
 __device__ __forceinline__ uint32_t hash32(uint32_t x)
@@ -139,18 +138,33 @@ __device__ __forceinline__ uint32_t lk_permutation(uint32_t x, uint32_t seed)
     return x;
 }
 __device__ __forceinline__ uint32_t scramble(uint32_t x, uint32_t seed) { return __brev(lk_permutation(__brev(x), seed)); }
+// The Sobol' point of dimension `dim` (< 4) is the XOR of the direction
+// numbers dir[dim][b] over the set bits b of the index.  XOR is
+// associative, so it is taken a byte at a time from tables holding, for each
+// byte position k and byte value v, the XOR over v's set bits j of
+// dir[dim][8k + j]: four L1-resident loads instead of a 32-step loop over
+// the (scrambled, so full-width) index.  Filled per translation unit from the
+// same direction numbers (sobol_byte_tables).
+static __device__ uint32_t g_sobol_bytes[4][4][256];
+
+__host__ inline void sobol_byte_tables(const uint32_t* table128, uint32_t (*out)[4][256])
+{
+    for (int d = 0; d < 4; d++)
+        for (int k = 0; k < 4; k++)
+            for (int v = 0; v < 256; v++) {
+                uint32_t x = 0;
+                for (int j = 0; j < 8; j++)
+                    if (v & (1 << j))
+                        x ^= table128[d * 32 + 8 * k + j];
+                out[d][k][v] = x;
+            }
+}
+
 __device__ __forceinline__ uint32_t sobol(uint32_t index, uint32_t dim)
 {
-    uint32_t x = 0;
-#pragma unroll 4
-    for (int b = 0; b < 32; b++) {
-        if (index == 0)
-            break;
-        if (index & 1u)
-            x ^= c_sobol[dim][b];
-        index >>= 1;
-    }
-    return x;
+    const uint32_t* t = &g_sobol_bytes[dim][0][0];
+    return (__ldg(t + (index & 255u)) ^ __ldg(t + 256u + ((index >> 8) & 255u))) ^
+           (__ldg(t + 512u + ((index >> 16) & 255u)) ^ __ldg(t + 768u + (index >> 24)));
 }
 
 struct Sampler {

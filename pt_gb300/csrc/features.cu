@@ -99,7 +99,9 @@ unsigned grid_for(uint32_t n, int threads)
 // This unit's copies of the sampler's direction numbers and the sRGB table.
 cudaError_t features_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream)
 {
-    cudaError_t e = cudaMemcpyToSymbolAsync(c_sobol, table128, sizeof(uint32_t) * 128, 0, cudaMemcpyHostToDevice, stream);
+    uint32_t bytes[4][4][256];
+    sobol_byte_tables(table128, bytes);
+    cudaError_t e = cudaMemcpyToSymbol(g_sobol_bytes, bytes, sizeof(bytes)); // synchronous: `bytes` is local
     if (e == cudaSuccess)
         e = cudaMemcpyToSymbolAsync(c_srgb, srgb256, sizeof(float) * 256, 0, cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess)
