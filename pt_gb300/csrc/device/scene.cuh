@@ -312,9 +312,11 @@ __device__ __forceinline__ int node4_children(const Bvh4Node* node, const ObjRay
 }
 
 // One interior step of a 4-wide traversal: the nearest hit child becomes
-// `ref`, the others are pushed far to near; nothing hit pops the stack.  A
-// push that would overflow sets ERR_STACK_OVERFLOW and drops those children.
-template <int N>
+// `ref`, the others are pushed far to near (SORT; else in slot order, for
+// any-hit queries whose result does not depend on the order); nothing hit
+// pops the stack.  A push that would overflow sets ERR_STACK_OVERFLOW and
+// drops those children.
+template <int N, bool SORT = true>
 __device__ __forceinline__ void step4(const DevScene& s, const ObjRay& r, float tmin, float tmax, int& ref, int (&stack)[N], int& sp)
 {
     float e[4];
@@ -327,6 +329,21 @@ __device__ __forceinline__ void step4(const DevScene& s, const ObjRay& r, float 
     }
     if (cnt == 1) {
         ref = c[__ffs(m) - 1];
+        return;
+    }
+    if (!SORT) {
+        if (sp + cnt - 1 > N) {
+            atomicOr(s.error_word, ERR_STACK_OVERFLOW);
+            ref = c[__ffs(m) - 1];
+            return;
+        }
+        int rest = m;
+        ref = c[__ffs(rest) - 1];
+        rest &= rest - 1;
+        while (rest) {
+            stack[sp++] = c[__ffs(rest) - 1];
+            rest &= rest - 1;
+        }
         return;
     }
     // sort (entry, child) ascending with misses keyed +inf: a five-exchange network
@@ -745,7 +762,7 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
     if (ref >= 0) {
         tc.nodes++;
         if (W4)
-            step4(s, t.r, t.tmin, t.tmax, t.ref, stack, t.sp);
+            step4<STACK_SIZE, false>(s, t.r, t.tmin, t.tmax, t.ref, stack, t.sp);
         else
             step2(s, t.r, t.tmin, t.tmax, t.ref, stack, t.sp);
         return false;
