@@ -216,7 +216,7 @@ enum Traversal : int { TRAV_BVH4 = 0, TRAV_BVH2 = 1, TRAV_BVH2_WW = 2 };
 // Persistent traversal: warps fetch 32 queue entries at a time.
 // Only traces: k_wf_split then separates hits from misses.
 template <class Src, int TRAV>
-__global__ void __launch_bounds__(128) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
+__global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 7 : 1) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
 {
     const uint32_t* queue = a.w.queue[qi];
     const uint32_t count = *(volatile uint32_t*)&a.w.counts[qi];
@@ -530,7 +530,7 @@ __global__ void __launch_bounds__(128) k_wf_shadow_refill(WaveArgs<Src> a, uint3
 }
 
 template <class Src, bool W4>
-__global__ void __launch_bounds__(128) k_wf_shadow(WaveArgs<Src> a)
+__global__ void __launch_bounds__(128, W4 ? 7 : 1) k_wf_shadow(WaveArgs<Src> a)
 {
     const uint32_t count = a.w.counts[2];
     unsigned lane = threadIdx.x & 31;
