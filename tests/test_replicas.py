@@ -1,7 +1,7 @@
-"""Replicas across processes (the multi-GPU path of this build, SURVEY
-section 8e): disjoint sample ranges per rank, FP64 sums merged with an
-all-reduce.  Run on CPU with world size 2 and 3 over gloo; each rank's
-partial sums come from the oracle (the GPU renders the same per-sample values
+"""Replicas across processes (the multi-GPU path of this library):
+disjoint sample ranges per rank, FP64 sums merged with an all-reduce.  Run
+on CPU with world size 2 and 3 over gloo; each rank's partial sums come
+from the oracle (the GPU renders the same per-sample values
 bit for bit, tests/test_gpu_parity.py), so what is tested here is the split,
 the merge and the mean."""
 import os
