@@ -289,6 +289,16 @@ int pt_render_next(pt_ctx* ctx, uint32_t samples, pt_render_stats* stats_out);
 #define PT_IMAGE_SUMS64 3
 int pt_read_image(pt_ctx* ctx, void* rgba, size_t pitch_bytes, int fp64);
 
+/* Fault injection for the bounds-checked build (libptgpu_checked.so, built
+ * with -DPT_CHECKED: every node, triangle, instance, vertex-index and queue
+ * index is compared with its array's length before use, and a bad one makes
+ * pt_render fail with PT_ERR_DEVICE, "index out of range").  Overwrites the
+ * first child link of the traversed root node of the context's TLAS with
+ * `value`; rebuild the acceleration structure to repair it.  Returns
+ * PT_ERR_UNSUPPORTED in the normal build (whose kernels do not check) and
+ * PT_ERR_STATE when there is no TLAS node (fewer than two instances). */
+int pt_debug_poke_tlas_link(pt_ctx* ctx, int value);
+
 /* Checkpoint / resume of long progressive renders (no reference
  * counterpart: the reference keeps its running mean only in device memory).
  * A checkpoint is pt_read_image (the FP32 running mean, and PT_IMAGE_SUMS64

@@ -7,10 +7,12 @@ native library is missing or cannot be loaded, every call raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 _HERE = Path(__file__).resolve().parent
-LIB_PATH = _HERE / "_build" / "libptgpu.so"
+# PT_CHECKED=1 selects the bounds-checked build of the same library
+LIB_PATH = _HERE / "_build" / ("libptgpu_checked.so" if os.environ.get("PT_CHECKED") == "1" else "libptgpu.so")
 ABI_VERSION = 2  # PT_ABI_VERSION of include/pt_gpu.h that these declarations follow
 
 PT_OK = 0
@@ -183,6 +185,7 @@ SIGNATURES = [
     ("pt_png_decode", C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_uint32),
                                 C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     # denoiser (include/pt_denoise.h)
+    ("pt_debug_poke_tlas_link", C.c_int, [C.c_void_p, C.c_int]),
     ("pt_unet_param_count", C.c_size_t, []),
     ("pt_unet_layer_shape", C.c_int, [C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     ("pt_unet_create", C.c_void_p, [C.c_int, C.c_uint32, C.c_uint32, C.c_uint32]),

@@ -17,6 +17,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = BUILD / "libptgpu.so"
+LIB_CHECKED = BUILD / "libptgpu_checked.so" # the same library with bounds-checked kernels (-DPT_CHECKED)
 CLI = BUILD / "pt"
 
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
@@ -69,12 +70,28 @@ def build(verbose: bool = False) -> Path:
             objs.append(obj)
         if _stale(obj, [CSRC / src] + HEADERS):
             jobs.append((src, ["g++"] + CXX_FLAGS + ["-c", str(CSRC / src), "-o", str(obj)]))
+    # the bounds-checked variant: the tracer's translation units again with -DPT_CHECKED
+    checked_objs = []
+    for src, obj in zip(CU_SOURCES, objs):
+        if src.startswith("nn/"):
+            checked_objs.append(obj)
+            continue
+        cobj = BUILD / (Path(src).stem + "_checked.o")
+        checked_objs.append(cobj)
+        if _stale(cobj, [CSRC / src] + HEADERS):
+            jobs.append((src + " (checked)", [NVCC] + NVCC_FLAGS + ["-DPT_CHECKED", "-c", str(CSRC / src), "-o", str(cobj)]))
+    checked_objs += objs[len(CU_SOURCES):]
     if jobs:
         if verbose:
             print("building:", ", ".join(n for n, _ in jobs), file=sys.stderr)
         _run_parallel(jobs)
+    links = []
     if _stale(LIB, objs):
-        _run_parallel([("link libptgpu.so", [NVCC] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs])])
+        links.append(("link libptgpu.so", [NVCC] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs]))
+    if _stale(LIB_CHECKED, checked_objs):
+        links.append(("link libptgpu_checked.so", [NVCC] + ARCH + ["-shared", "-o", str(LIB_CHECKED)] + [str(o) for o in checked_objs]))
+    if links:
+        _run_parallel(links)
     main_obj = BUILD / "main.o"
     if _stale(CLI, [main_obj, LIB]):
         _run_parallel([("link pt", ["g++", "-o", str(CLI), str(main_obj), f"-L{BUILD}", "-lptgpu", f"-Wl,-rpath,{BUILD}"])])

@@ -608,6 +608,9 @@ RenderArgs render_args(const pt_ctx* c, const pt_render_params* p, bool fp64)
     a.s.nodes = c->nodes.p;
     a.s.nodes4 = c->nodes4.p;
     a.s.tris = c->tris.p;
+    a.s.node_count = (uint32_t)c->nodes.n;
+    a.s.tri_count = c->tri_count;
+    a.s.index_count = c->index_count;
     a.s.dinst = c->dinst.p;
     a.s.tlas_root = c->tlas_root;
     a.s.env = mk3(c->env[0], c->env[1], c->env[2]);
@@ -683,6 +686,7 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
         a.snapshot_after = c->snapshot_armed;
     }
     cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
+    cudaMemsetAsync(c->error_word.p, 0, sizeof(uint32_t), c->stream); // errors belong to this render
     const bool timing = (p->flags & PT_RENDER_TIME_STAGES) != 0;
     uint32_t stage_marks = 0;
     uint64_t pixels = (uint64_t)p->width * p->height;
@@ -867,10 +871,34 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
         }
         if (ew != 0)
             return c->fail((ew & ERR_WATCHDOG) ? PT_ERR_TIMEOUT : PT_ERR_DEVICE,
-                          std::string((ew & ERR_WATCHDOG) ? "traversal iteration cap hit" : "device error") + " (error word " +
-                              std::to_string(ew) + ")");
+                          std::string((ew & ERR_WATCHDOG)      ? "traversal iteration cap hit"
+                                      : (ew & ERR_BAD_INDEX) ? "index out of range (checked build)"
+                                                              : "device error") +
+                              " (error word " + std::to_string(ew) + ")");
     }
     return PT_OK;
+}
+
+int pt_debug_poke_tlas_link(pt_ctx* c, int value)
+{
+    if (!c)
+        return PT_ERR_INVALID;
+#ifndef PT_CHECKED
+    (void)value;
+    return c->fail(PT_ERR_UNSUPPORTED, "fault injection needs the bounds-checked build (libptgpu_checked.so)");
+#else
+    if (!c->accel_ok)
+        return c->fail(PT_ERR_STATE, "no acceleration structure");
+    if (c->tlas_root < 0)
+        return c->fail(PT_ERR_STATE, "the TLAS has no node");
+    cudaSetDevice(c->device);
+    cudaError_t e;
+    if (c->nodes4.p)
+        e = cudaMemcpy(&c->nodes4.p[c->tlas_root].link.x, &value, sizeof(int), cudaMemcpyHostToDevice);
+    else
+        e = cudaMemcpy(&c->nodes.p[c->tlas_root].link.x, &value, sizeof(int), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? PT_OK : c->cuda_fail(e, "fault injection");
+#endif
 }
 
 int pt_restore_image(pt_ctx* c, const float* rgba, size_t pitch, const double* sums64, uint32_t width, uint32_t height,

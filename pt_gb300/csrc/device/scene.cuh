@@ -98,6 +98,9 @@ struct DevScene {
     const BvhNode* nodes;
     const Bvh4Node* nodes4; // null: traverse the BVH2 `nodes`
     const TriRec* tris;
+    uint32_t node_count;  // entries of nodes (and nodes4)
+    uint32_t tri_count;   // entries of tris
+    uint32_t index_count; // entries of indices
     const DevInstance* dinst;
     int tlas_root;
     f3 env;
@@ -107,6 +110,20 @@ struct DevScene {
 constexpr uint32_t ERR_STACK_OVERFLOW = 1u;
 constexpr uint32_t ERR_BAD_INDEX = 2u;
 constexpr uint32_t ERR_WATCHDOG = 4u;
+
+// Checked builds (-DPT_CHECKED, libptgpu_checked.so): every node, triangle,
+// instance, vertex-index and queue index is compared with its array's length
+// before it is used; a bad one sets ERR_BAD_INDEX and ends that ray or entry
+// instead of reading outside the array (the stand-in for a memory checker).
+#ifdef PT_CHECKED
+#define PT_CHECK_INDEX(cond, s, on_fail)          \
+    if (!(cond)) {                                \
+        atomicOr((s).error_word, ERR_BAD_INDEX); \
+        on_fail;                                  \
+    }
+#else
+#define PT_CHECK_INDEX(cond, s, on_fail)
+#endif
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 __device__ __forceinline__ int4 ldg4i(const int4* p) { return __ldg(p); }
@@ -518,6 +535,7 @@ __device__ __forceinline__ bool closest_step(const DevScene& s, ClosestTrace& t,
     t.iter++;
     const int ref = t.ref;
     if (ref >= 0) {
+        PT_CHECK_INDEX((uint32_t)ref < s.node_count, s, return true)
         tc.nodes++;
         if (W4)
             step4(s, t.r, t.tmin, t.h.t, t.ref, stack, t.sp);
@@ -536,6 +554,7 @@ __device__ __forceinline__ bool closest_step(const DevScene& s, ClosestTrace& t,
     const uint32_t first = leaf_first(ref), count = leaf_count(ref);
     if (!t.in_blas) {
         // TLAS leaf: instances [first, first + count); one per leaf here.
+        PT_CHECK_INDEX(first < s.instance_count, s, return true)
         t.cur_inst = first;
         const DevInstance* di = s.dinst + first;
         const int root = __ldg(&di->blas_root);
@@ -554,6 +573,7 @@ __device__ __forceinline__ bool closest_step(const DevScene& s, ClosestTrace& t,
         t.ref = root;
         return false;
     }
+    PT_CHECK_INDEX((uint64_t)first + count <= s.tri_count, s, return true)
     tc.tris += count;
     for (uint32_t k = 0; k < count; k++) {
         const TriRec* tr = s.tris + first + k;
@@ -760,6 +780,7 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
     t.iter++;
     const int ref = t.ref;
     if (ref >= 0) {
+        PT_CHECK_INDEX((uint32_t)ref < s.node_count, s, return true)
         tc.nodes++;
         if (W4)
             step4<STACK_SIZE, false>(s, t.r, t.tmin, t.tmax, t.ref, stack, t.sp);
@@ -777,6 +798,7 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
     }
     const uint32_t first = leaf_first(ref), count = leaf_count(ref);
     if (!t.in_blas) {
+        PT_CHECK_INDEX(first < s.instance_count, s, return true)
         const DevInstance* di = s.dinst + first;
         const int root = __ldg(&di->blas_root);
         if (root == REF_EMPTY || count != 1) {
@@ -803,6 +825,7 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
         t.ref = root;
         return false;
     }
+    PT_CHECK_INDEX((uint64_t)first + count <= s.tri_count, s, return true)
     tc.tris += count;
     for (uint32_t k = 0; k < count; k++) {
         const TriRec* tr = s.tris + first + k;

@@ -334,15 +334,29 @@ __device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 r
 {
     nee.add = false;
     nee.trace = false;
+    PT_CHECK_INDEX(h.inst < s.instance_count, s, {
+        pl.final_segment = true;
+        return;
+    })
     const DevInstanceData* id = s.inst_data + h.inst;
     const DevInstance* di = s.dinst + h.inst;
     uint32_t vbase = __ldg(&id->vertex_index);
     uint32_t ibase = __ldg(&id->index_index);
     uint32_t emitter_index = __ldg(&id->emitter_index);
     const DevMaterial* mat = s.materials + __ldg(&id->material_index);
+    PT_CHECK_INDEX((uint64_t)ibase + 3ull * h.prim + 3ull <= s.index_count, s, {
+        pl.final_segment = true;
+        return;
+    })
     uint32_t i0 = __ldg(s.indices + ibase + h.prim * 3 + 0);
     uint32_t i1 = __ldg(s.indices + ibase + h.prim * 3 + 1);
     uint32_t i2 = __ldg(s.indices + ibase + h.prim * 3 + 2);
+    PT_CHECK_INDEX((uint64_t)vbase + i0 < s.vertex_count && (uint64_t)vbase + i1 < s.vertex_count &&
+                       (uint64_t)vbase + i2 < s.vertex_count,
+                   s, {
+                       pl.final_segment = true;
+                       return;
+                   })
     VertexF va = vfetch(s, vbase + i0), vb = vfetch(s, vbase + i1), vc = vfetch(s, vbase + i2);
 
     float ba = (1.0f - h.b1) - h.b2;

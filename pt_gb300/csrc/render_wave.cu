@@ -208,6 +208,19 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs<Src> a)
     }
 }
 
+// Checked builds: a queue entry must name a path of the wave; a bad one sets
+// ERR_BAD_INDEX and the entry is dropped (`valid` cleared) instead of used.
+#ifdef PT_CHECKED
+#define PT_CHECK_ENTRY(valid, p, a)                                      \
+    if ((valid) && (p) >= (a).src.n_paths) {                             \
+        atomicOr((a).src.args(0u).s.error_word, ERR_BAD_INDEX);         \
+        (valid) = false;                                                 \
+        (p) = 0u;                                                        \
+    }
+#else
+#define PT_CHECK_ENTRY(valid, p, a)
+#endif
+
 // Closest-hit traversal of a launch: over the 4-wide nodes, the BVH2 one
 // node-or-leaf step per iteration, or the BVH2 while-while with speculative
 // leaves.
@@ -233,8 +246,12 @@ __global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 7 : 1) k_wf_extend(Wa
         uint32_t i = base + lane;
         uint32_t p = 0;
         bool hit = false;
-        if (i < count) {
+        bool ok = i < count;
+        if (ok) {
             p = queue[i];
+            PT_CHECK_ENTRY(ok, p, a)
+        }
+        if (ok) {
             const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
             Hit h;
@@ -272,8 +289,9 @@ __global__ void __launch_bounds__(256) k_wf_split(WaveArgs<Src> a, uint32_t qi)
     // the loop bound is the same for the whole block, so the barriers below are uniform
     for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
-        const bool valid = i < count;
-        const uint32_t p = valid ? queue[i] : 0u;
+        bool valid = i < count;
+        uint32_t p = valid ? queue[i] : 0u;
+        PT_CHECK_ENTRY(valid, p, a)
         const bool hit = valid && a.w.hit_prim[p] != 0xFFFFFFFFu;
         if (valid && !hit) {
             const RenderArgs& R = a.src.args(a.src.job_of(p));
@@ -326,6 +344,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_
         bool active = i < count;
         bool cont = false, trace = false;
         uint32_t p = active ? qin[i] : 0;
+        PT_CHECK_ENTRY(active, p, a)
         if (active) {
             segments++;
             uint32_t sg = a.w.seg[p];
@@ -543,8 +562,10 @@ __global__ void __launch_bounds__(128, W4 ? 7 : 1) k_wf_shadow(WaveArgs<Src> a)
         if (base >= count)
             break;
         uint32_t i = base + lane;
-        if (i < count) {
-            uint32_t p = a.w.shadow_queue[i];
+        bool ok = i < count;
+        uint32_t p = ok ? a.w.shadow_queue[i] : 0u;
+        PT_CHECK_ENTRY(ok, p, a)
+        if (ok) {
             const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.nee_o[p], d = a.w.nee_d[p];
             float vis = trace_shadow_inl<W4>(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, o.w, tc);
@@ -723,14 +744,23 @@ static int resident_blocks(K kernel)
 // The extend variant for scenes with (w4) or without 4-wide nodes.
 static int traversal_of(bool w4)
 {
+#ifdef PT_CHECKED
+    return w4 ? TRAV_BVH4 : TRAV_BVH2; // the while-while traversal has no checked form
+#else
     return w4 ? TRAV_BVH4 : stage_variant().ww ? TRAV_BVH2_WW : TRAV_BVH2;
+#endif
 }
 
 // Whether the process's extend and shadow launches are the refill kernels
 // (the while-while BVH2 traversal has no refill form).
 static bool refill_for(bool w4)
 {
+#ifdef PT_CHECKED
+    (void)w4;
+    return false; // the refill kernels have no checked form
+#else
     return stage_variant().refill != 0 && traversal_of(w4) != TRAV_BVH2_WW;
+#endif
 }
 
 // Resident 128-thread blocks per SM of the persistent traversal kernels

@@ -36,6 +36,17 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
+def test_checked_library_exports_the_same_symbols():
+    """libptgpu_checked.so (bounds-checked kernels) is a drop-in for libptgpu.so."""
+    path = abi.LIB_PATH.with_name("libptgpu_checked.so")
+    assert path.exists(), path
+    lib = C.CDLL(str(path))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    lib.pt_abi_version.restype = C.c_int
+    assert lib.pt_abi_version() == abi.ABI_VERSION
+
+
 def test_ctypes_signatures_cover_declarations():
     assert {n for n, _, _ in abi.SIGNATURES} == declared_functions()
 

@@ -101,6 +101,52 @@ def test_empty_and_zero_triangle_scenes_render(ctx):
     assert np.allclose(img[..., :3], np.asarray(raw["environment_colour"], np.float32))
 
 
+_CHECKED = """
+import sys, numpy as np
+import pt_gb300 as P
+from pt_gb300 import abi, scenes
+assert abi.LIB_PATH.name == "libptgpu_checked.so"
+hs = P.HostScene.load(scenes.small_scene(__import__("pathlib").Path(sys.argv[1]), seed=0))
+ctx = P.Context(0)
+ctx.upload(hs.pack())
+ctx.build_accel()
+p = hs.render_params(64, 48, 3, 6)
+st = ctx.render(p)
+assert st.error_word == 0
+np.save(sys.argv[2], ctx.read_image())
+# an out-of-range child link in the traversed TLAS root: caught before any access
+assert abi.lib().pt_debug_poke_tlas_link(ctx._h, 0x7FFF0000) == abi.PT_OK
+try:
+    ctx.render(p)
+    print("no error")
+except P.PtError as e:
+    print("status", e.status, str(e))
+ctx.build_accel()  # repaired by a rebuild
+ctx.render(p)
+np.save(sys.argv[3], ctx.read_image())
+"""
+
+
+def test_checked_build_matches_and_catches_bad_indices(ctx, tmp_path):
+    """The bounds-checked library (PT_CHECKED=1 selects it; set in a child)
+    renders the same image as the normal one, and a corrupted BVH link is
+    reported as PT_ERR_DEVICE "index out of range" instead of being followed;
+    the normal build refuses the fault injection."""
+    a, b = tmp_path / "a.npy", tmp_path / "b.npy"
+    r = subprocess.run([sys.executable, "-c", _CHECKED, str(tmp_path / "scene"), str(a), str(b)],
+                       env=dict(os.environ, PT_CHECKED="1"), cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert f"status {abi.PT_ERR_DEVICE}" in r.stdout and "index out of range" in r.stdout, r.stdout
+    hs = P.HostScene.load(scenes.small_scene(tmp_path / "scene2", seed=0))
+    ctx.upload(hs.pack())
+    ctx.build_accel()
+    ctx.render(hs.render_params(64, 48, 3, 6))
+    want = ctx.read_image()
+    assert np.array_equal(np.load(a).view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(np.load(b).view(np.uint32), want.view(np.uint32))
+    assert abi.lib().pt_debug_poke_tlas_link(ctx._h, 0x7FFF0000) == abi.PT_ERR_UNSUPPORTED
+
+
 _CAPPED = """
 import pt_gb300 as P
 from pt_gb300 import abi, scenes
