@@ -126,6 +126,34 @@ def test_same_scene_several_cameras(batch):
         assert _same(ctx.read_batch_image(j), ref[j])
 
 
+def test_refractive_and_textured_jobs_in_a_batch(batch):
+    """Jobs whose scenes use the refractive dielectric and every texture map
+    kind, packed with the others into multi-wave batches on two wave states,
+    equal their single renders and the oracle."""
+    ctx, jobs, _ = batch
+    extra, keep = [], []
+    for raw, cam in (scenes.glass_raw("glass"), scenes.textured_raw()):
+        hs = P.HostScene.from_raw(raw, cam)
+        view = hs.pack()
+        c = P.Context(0)
+        c.upload(view)
+        c.build_accel()
+        keep.append((hs, view, c))
+        extra.append((c, hs.render_params(48, 40, 4, 8)))
+    mixed = extra + jobs[:3]
+    ref = _single(mixed)
+    for flags in (abi.PT_BATCH_NO_TUNE | abi.PT_BATCH_CAPACITY_LOG2(12), abi.PT_BATCH_NO_TUNE):
+        st = ctx.render_batch(mixed, flags)
+        assert st.error_word == 0
+        for j in range(len(mixed)):
+            assert _same(ctx.read_batch_image(j), ref[j]), (flags, j)
+    for k, (_, view, _) in enumerate(keep):  # the first jobs of `mixed` are the extra ones
+        want, _ = oracle.OracleScene(view).render(extra[k][1])
+        assert _same(ref[k], want), k
+    for _, _, c in keep:
+        c.close()
+
+
 def test_invalid_batches(batch):
     ctx, jobs, _ = batch
     c, p = jobs[0]
