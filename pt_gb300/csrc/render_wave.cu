@@ -629,15 +629,19 @@ __global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs<Src> a)
             feat_store(R.feat_a, pix, fa, R.fp16_features);
             feat_store(R.feat_n, pix, fn, R.fp16_features);
         }
+        // FP64 sums only when the render keeps them: FP64 adds are slow on this GPU
+        const bool want64 = R.sum64 != nullptr;
         for (uint32_t j = 0; j < E.samples; j++) {
             float4 r4 = a.w.rad[E.path_base + (size_t)j * E.pixels + pix];
             f3 r = correct_radiance(mk3(r4.x, r4.y, r4.z) * R.exposure);
             accumulate(acc, r, E.first_sample + j);
             if (R.snapshot && E.first_sample + j + 1 == R.snapshot_after)
                 feat_store(R.snapshot, pix, acc, R.fp16_features);
-            s64[0] += (double)r.x;
-            s64[1] += (double)r.y;
-            s64[2] += (double)r.z;
+            if (want64) {
+                s64[0] += (double)r.x;
+                s64[1] += (double)r.y;
+                s64[2] += (double)r.z;
+            }
         }
         R.image[pix] = acc;
         if (R.sum64) {
