@@ -289,16 +289,6 @@ int pt_render_next(pt_ctx* ctx, uint32_t samples, pt_render_stats* stats_out);
 #define PT_IMAGE_SUMS64 3
 int pt_read_image(pt_ctx* ctx, void* rgba, size_t pitch_bytes, int fp64);
 
-/* Fault injection for the bounds-checked build (libptgpu_checked.so, built
- * with -DPT_CHECKED: every node, triangle, instance, vertex-index and queue
- * index is compared with its array's length before use, and a bad one makes
- * pt_render fail with PT_ERR_DEVICE, "index out of range").  Overwrites the
- * first child link of the traversed root node of the context's TLAS with
- * `value`; rebuild the acceleration structure to repair it.  Returns
- * PT_ERR_UNSUPPORTED in the normal build (whose kernels do not check) and
- * PT_ERR_STATE when there is no TLAS node (fewer than two instances). */
-int pt_debug_poke_tlas_link(pt_ctx* ctx, int value);
-
 /* Checkpoint / resume of long progressive renders (no reference
  * counterpart: the reference keeps its running mean only in device memory).
  * A checkpoint is pt_read_image (the FP32 running mean, and PT_IMAGE_SUMS64
@@ -323,12 +313,11 @@ int pt_tonemap(pt_ctx* ctx);
  * (meansq.cpp:34-43): SSE over RGB / (w*h*3 - 1), reduced in FP64. */
 int pt_mse_host(pt_ctx* ctx, const float* reference_rgba, double* mse_out);
 
-/* Mean squared error for callers that cannot allocate device memory: code
- * recording a CUDA stream capture (cudaMalloc is not allowed while capturing),
- * host applications that own all device memory and forbid allocations inside
- * plug-ins, and real-time loops that cannot risk the implicit device
- * synchronisation of cudaMalloc/cudaFree.  This entry point has no counterpart
- * in the reference.
+/* Mean squared error for callers that cannot allocate device memory: host
+ * applications that reserve the GPU's memory for their own pool and forbid
+ * allocations inside plug-ins, processes under a hard device-memory cap, and
+ * real-time loops that cannot risk the implicit device synchronisation of
+ * cudaMalloc/cudaFree.  This entry point has no counterpart in the reference.
  *
  * Same value as pt_mse_host (util/meansq semantics) for two caller-owned
  * device images (RGBA float rows, 16-byte aligned, width * height pixels);
@@ -340,7 +329,8 @@ int pt_mse_host(pt_ctx* ctx, const float* reference_rgba, double* mse_out);
  * that device current) looks up the array's address; make that first call
  * before any stream capture.  All calls share the array: calls that overlap on
  * the GPU race.  Images above PT_MSE_NOALLOC_MAX_PIXELS pixels are rejected
- * with PT_ERR_UNSUPPORTED; null or misaligned pointers with PT_ERR_INVALID. */
+ * with PT_ERR_UNSUPPORTED; null pointers, images not 16-byte aligned and an
+ * output not 8-byte aligned with PT_ERR_INVALID. */
 #define PT_MSE_NOALLOC_SCRATCH_BYTES 9728u
 #define PT_MSE_NOALLOC_MAX_PIXELS 2147483648ull
 int pt_mse_noalloc(const float* image_rgba, const float* reference_rgba, uint32_t width, uint32_t height, double* mse_out,

@@ -9,6 +9,7 @@ reference functions it restates and how each is pinned.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -18,16 +19,30 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libptref.so"
 REF_MEANSQ = HERE / "_ref" / "meansq"
-REFERENCE_TREE = Path("/root/reference")
+# Where the reference's source tree is read from (its CPU sources for
+# oracle/_ref, one shader table as text for the golden fixtures): the one
+# setting of that location, PT_REFERENCE_TREE, with the tree's usual place as
+# the default.  Where no tree exists (the GPU machine) everything that needs
+# it is skipped.
+_DEFAULT_REFERENCE_TREE = "/root/reference"
+
+
+def reference_tree() -> Path | None:
+    """The reference's source tree, or None where it does not exist."""
+    p = Path(os.environ.get("PT_REFERENCE_TREE", _DEFAULT_REFERENCE_TREE))
+    return p if (p / "src").is_dir() else None
 
 
 def build(reference: bool | None = None) -> None:
     """Compile the oracle (and the reference shim when the reference tree exists)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], check=True)
+    tree = reference_tree()
     if reference is None:
-        reference = REFERENCE_TREE.exists()
+        reference = tree is not None
     if reference:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+        if tree is None:
+            raise FileNotFoundError("no reference tree (set PT_REFERENCE_TREE)")
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={tree}"], check=True)
 
 
 _lib = None

@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/pt_checked.h"
 #include "../../include/pt_denoise.h"
 #include "../../include/pt_gpu.h"
 #include "ctx.h"
@@ -653,6 +654,12 @@ int pt_render(pt_ctx* c, const pt_render_params* p, pt_render_stats* stats)
     if (p->flags & ~(PT_RENDER_FEATURES | PT_RENDER_TIME_STAGES | PT_RENDER_FEATURES_FP16 | PT_RENDER_RESTART))
         return c->fail(PT_ERR_INVALID, "unknown render flags");
     const bool restart = p->sample_index == 0 || (p->flags & PT_RENDER_RESTART) != 0;
+    // FP64 sums that continue a progression must hold every earlier sample:
+    // after an FP32-only chunk (or a restore without sums) they do not.
+    const bool continues = !restart && c->image.p && c->width == p->width && c->height == p->height;
+    if (fp64 && continues && !c->have_fp64)
+        return c->fail(PT_ERR_STATE, "FP64 sums requested for a continued render whose earlier samples have none "
+                                     "(restart it, or keep FP64 sums from its first sample)");
     int rc = ensure_image(c, p->width, p->height, fp64, restart);
     if (rc != PT_OK)
         return rc;

@@ -1,22 +1,21 @@
 // noalloc.cu — pt_mse_noalloc: the meansq reduction without any allocation.
 //
-// Some callers must not allocate device memory: code recording into a CUDA
-// stream capture (cudaMalloc is not allowed while a stream is being captured),
-// host applications that own every byte of device memory and forbid
-// allocations inside plug-ins, and real-time loops that cannot afford the
-// implicit device synchronisation cudaMalloc/cudaFree may cause.  This entry
-// point computes the same value as pt_mse_host from caller-owned device
-// buffers, with its only scratch (the per-block partial sums) in a fixed
-// file-scope device array.
+// Some callers of this library cannot allocate device memory: host
+// applications (renderers, game engines, simulation frameworks) that reserve
+// the GPU's memory for their own pool up front and forbid allocations inside
+// plug-ins, processes started under a hard device-memory cap, and real-time
+// loops that cannot afford the implicit device synchronisation that
+// cudaMalloc/cudaFree may cause.  This entry point computes the same value as
+// pt_mse_host from caller-owned device buffers, with its only scratch (the
+// per-block partial sums) in a fixed file-scope device array.
 //
 // The array lives in every GPU that loads the library until the process
-// exits.  Its device address is looked up once per device (the first call on
-// a device, with that device current); that first call must therefore happen
-// before any stream capture that wants to record later calls.  Every call
-// shares the one array: calls that overlap on the GPU (different streams, or
-// different host threads, without ordering between them) race on it.  Each
-// block overwrites its own partial sum before the final pass reads it, so no
-// clearing is needed between calls.
+// exits.  Its device address is looked up once per device, by the first call
+// on that device (made with that device current); make that first call before
+// any stream capture.  Every call shares the one array: calls that overlap on
+// the GPU (different streams, or different host threads, without ordering
+// between them) race on it.  Each block overwrites its own partial sum before
+// the final pass reads it, so no clearing is needed between calls.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -52,7 +51,7 @@ int pt_mse_noalloc(const float* image, const float* reference, uint32_t width, u
     if ((uint64_t)width * height > PT_MSE_NOALLOC_MAX_PIXELS) {
         return PT_ERR_UNSUPPORTED;
     }
-    if (((uintptr_t)image | (uintptr_t)reference) & 15u) {
+    if ((((uintptr_t)image | (uintptr_t)reference) & 15u) || ((uintptr_t)mse_out & 7u)) {
         return PT_ERR_INVALID;
     }
     int dev = 0;

@@ -28,7 +28,9 @@ sys.path.insert(0, str(ROOT))
 import oracle  # noqa: E402
 from pt_gb300 import abi, core, scenes  # noqa: E402
 
-REF = Path("/root/reference")
+REF = oracle.reference_tree()
+if REF is None:
+    sys.exit("make_golden: no reference tree (set PT_REFERENCE_TREE)")
 
 
 def sobol_table():

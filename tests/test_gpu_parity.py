@@ -251,6 +251,26 @@ def test_checkpoint_resume_is_exact(ctx, small):
     fresh.close()
 
 
+def test_fp64_sums_refused_after_an_fp32_chunk(ctx, small):
+    """A progression that took samples without FP64 sums cannot ask for FP64
+    sums later without a restart: those sums would miss the FP32-only samples."""
+    hs, view = small
+    ctx.upload(view)
+    ctx.build_accel()
+    ctx.render(hs.render_params(24, 16, 2, 4, accum_mode=abi.PT_ACCUM_FP32_FP64))
+    ctx.render(hs.render_params(24, 16, 1, 4, sample_index=2))
+    with pytest.raises(P.PtError) as e:
+        ctx.render(hs.render_params(24, 16, 1, 4, sample_index=3, accum_mode=abi.PT_ACCUM_FP32_FP64))
+    assert e.value.status == abi.PT_ERR_STATE
+    with pytest.raises(P.PtError):
+        ctx.read_image(fp64=True)
+    # a restart may ask for them again; a continuation that kept them may too
+    ctx.render(hs.render_params(24, 16, 2, 4, accum_mode=abi.PT_ACCUM_FP32_FP64))
+    ctx.render(hs.render_params(24, 16, 1, 4, sample_index=2, accum_mode=abi.PT_ACCUM_FP32_FP64))
+    s = ctx.read_image(fp64=True)
+    assert np.isfinite(s).all()
+
+
 def test_deterministic(ctx, small):
     hs, view = small
     params = hs.render_params(64, 48, 3, 8)

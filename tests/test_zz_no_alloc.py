@@ -1,6 +1,7 @@
 """pt_mse_noalloc: the meansq reduction for callers that cannot allocate device
-memory (stream captures, host applications that own all device memory,
-real-time loops that must avoid cudaMalloc's implicit synchronisation).
+memory (host applications that own all device memory and forbid allocations in
+plug-ins, processes under a hard device-memory cap, real-time loops that must
+avoid cudaMalloc's implicit synchronisation).
 
 It must give the value of the existing entry point pt_mse_host for the same
 images, call after call, while its scratch lives in a fixed array inside the
@@ -65,5 +66,8 @@ def test_noalloc_rejects_bad_arguments():
     assert L.pt_mse_noalloc(C.c_void_p(a.data_ptr()), C.c_void_p(a.data_ptr()), 65536, 65536, C.c_void_p(out.data_ptr()),
                             None) == abi.PT_ERR_UNSUPPORTED
     assert L.pt_mse_noalloc(C.c_void_p(a.data_ptr() + 4), C.c_void_p(a.data_ptr()), 2, 2, C.c_void_p(out.data_ptr()),
+                            None) == abi.PT_ERR_INVALID
+    # an output that is not 8-byte aligned (a byte offset into a device buffer)
+    assert L.pt_mse_noalloc(C.c_void_p(a.data_ptr()), C.c_void_p(a.data_ptr()), 2, 2, C.c_void_p(out.data_ptr() + 4),
                             None) == abi.PT_ERR_INVALID
     torch.cuda.synchronize()
