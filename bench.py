@@ -156,13 +156,33 @@ def make_scene(workdir: Path):
     return hs
 
 
-def cpu_baseline(view, params_fn, seconds_target: float = 15.0) -> dict:
+def oracle_scene(workdir: Path):
+    """The same mid scene, read and packed by the oracle alone (its own .scn +
+    glTF reader and packer): nothing here loads libptgpu.so.  Returns the
+    oracle scene, the packed scene (kept alive with it) and a params factory."""
+    import oracle
+    from oracle import scn_reader
+    from pt_gb300 import abi, scenes
+    raw, cam = scn_reader.read_scn(scenes.mid_scene(workdir / "mid", seed=1))
+    rs, keep = scn_reader.raw_struct(raw)
+    packed = oracle.OraclePacked(rs)
+    osc = oracle.OracleScene(packed.view)
+    cd = scn_reader.camera_desc(cam)
+
+    def params(samples, first):
+        p = abi.RenderParams()
+        oracle.lib().or_camera_params(cd, WIDTH, HEIGHT, p)
+        p.sample_index, p.samples, p.max_bounces, p.rr_start = first, samples, BOUNCES, 1
+        return p
+
+    return osc, (packed, keep), params
+
+
+def cpu_baseline(osc, params_fn, seconds_target: float = 15.0) -> dict:
     """Oracle port on all host threads over a bounded sample of the workload:
     whole frames of consecutive samples (0, 1, 2, ...) until about
     seconds_target of wall time has been spent.  params_fn(samples, first)."""
-    import oracle
     threads = os.cpu_count() or 1
-    osc = oracle.OracleScene(view)
     segs, dt, n = 0, 0.0, 0
     while dt < seconds_target:
         t0 = time.perf_counter()
@@ -171,32 +191,41 @@ def cpu_baseline(view, params_fn, seconds_target: float = 15.0) -> dict:
         segs += st.segments
         n += 1
     return {"value": segs / dt / 1e6, "unit": "Mpath-segs/s", "cores": threads, "kind": "port",
-            "sample": f"mid scene 1024x1024, samples 0-{n - 1} of 128 ({segs} segments, {dt:.1f} s)",
+            "sample": f"mid scene {WIDTH}x{HEIGHT}, samples 0-{n - 1} of {SPP} ({segs} segments, {dt:.1f} s)",
             "segments": int(segs), "seconds": dt}
 
 
+def shared_config(world: int) -> dict:
+    """The workload, identical in both arms' lines."""
+    return {"workload": WORKLOAD, "image": f"{WIDTH}x{HEIGHT}", "spp": SPP, "max_bounces": BOUNCES,
+            "l2": "GPU arm: flushed between steps (512 MiB write, outside the event pairs); CPU arm: n/a",
+            "parallelism": f"replicas x{world} (disjoint sample ranges)"}
+
+
 def run_reference(args) -> None:
+    """The reference's CPU implementation of the path on the host cores: its
+    Vulkan tracer cannot run on this machine (no graphics stack), so the
+    oracle port is timed, each step a bounded sample (whole frames of
+    consecutive samples for about --ref-seconds).  Scene read and packed by
+    the oracle alone; libptgpu.so is never loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     with tempfile.TemporaryDirectory() as td:
-        hs = make_scene(Path(td))
-        view = hs.pack()
-        base = cpu_baseline(view, lambda n, f: hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=f), seconds_target=float(args.cpu_seconds))
-        values = []
+        osc, keep, params = oracle_scene(Path(td))
         for _ in range(args.warmup):
-            cpu_baseline(view, lambda n, f: hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=f), seconds_target=2.0)
-        for _ in range(args.steps):
-            values.append(cpu_baseline(view, lambda n, f: hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=f),
-                                       seconds_target=float(args.cpu_seconds))["value"])
-        v = statistics.median(values)
+            cpu_baseline(osc, params, seconds_target=1.0)
+        runs = [cpu_baseline(osc, params, seconds_target=float(args.ref_seconds)) for _ in range(args.steps)]
+        v = statistics.median(r["value"] for r in runs)
         line = {"metric": METRIC, "value": v, "unit": "Mpath-segs/s", "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-                "config": {"workload": WORKLOAD, "l2": "n/a (CPU)"},
-                "cpu_baseline": {"value": v, "unit": "Mpath-segs/s", "cores": base["cores"], "kind": "port",
-                                 "sample": base["sample"] + "; the reference's Vulkan tracer is unavailable on this box "
-                                                           "(no graphics stack), so its CPU restatement is timed"},
+                "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.median(r["seconds"] for r in runs),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference", "config": shared_config(world),
+                "cpu_baseline": {"value": v, "unit": "Mpath-segs/s", "cores": runs[0]["cores"], "kind": "port",
+                                 "sample": runs[0]["sample"] + " per step; the reference's Vulkan tracer is unavailable "
+                                                               "on this box (no graphics stack), so its CPU restatement "
+                                                               "(the oracle) is timed"},
                 "e2e": {"value": v, "unit": "Mpath-segs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
 
@@ -542,8 +571,11 @@ def run_ours(args) -> None:
                 "stage_ms_per_step": {k: v / args.steps for k, v in zip(abi.STAGES, stage_ms)},
                 "step": {"achieved": step_achieved, "frac": step_achieved / peaks["hbm_gbs"], "bytes_per_segment": b,
                          "note": "whole render step: B_seg x segments / step time"}}
-        base = cpu_baseline(view, lambda n, f: hs.render_params(WIDTH, HEIGHT, n, BOUNCES, sample_index=f), seconds_target=float(args.cpu_seconds)) \
-            if not args.no_cpu else None
+        base = None
+        if not args.no_cpu:
+            osc, keep_o, oparams = oracle_scene(Path(td.name) / "oracle")
+            base = cpu_baseline(osc, oparams, seconds_target=float(args.cpu_seconds))
+            del osc, keep_o
         ttm = time_to_mse(ctx, hs, args.kernel, args.ref_spp) if not args.no_mse else None
         batches = None
         if not args.no_batch:
@@ -552,9 +584,8 @@ def run_ours(args) -> None:
         line = {"metric": METRIC, "value": value, "unit": "Mpath-segs/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB write, outside the event pairs)",
-                           "parallelism": f"replicas x{world} (disjoint sample ranges)",
-                           "kernel": {1: "megakernel", 2: "wavefront"}.get(st.kernel_used, str(st.kernel_used)),
+                "config": shared_config(world),
+                "details": {"kernel": {1: "megakernel", 2: "wavefront"}.get(st.kernel_used, str(st.kernel_used)),
                            "wave_streams": "timed steps: 1 (per-launch stage events need one stream); e2e and "
                                            "time_to_mse: the library default (PT_WAVE_STREAMS, 2)",
                            "segments_per_step": int(segs_per_step), "accel_build_ms": info.build_ms,
@@ -582,7 +613,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--kernel", type=int, default=0)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample of our arm's line")
+    ap.add_argument("--ref-seconds", type=float, default=8.0, help="CPU work per step of the reference arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mse", action="store_true", help="skip the time-to-MSE measurement")
