@@ -278,7 +278,7 @@ def meansq(a, ref) -> float:
     return float(np.sum(d * d) / (d.size - 1))
 
 
-def time_to_mse(ctx, hs, kernel: int, ref_spp: int) -> dict:
+def time_to_mse(ctx, hs, kernel: int, ref_spp: int, curve: bool = True) -> dict:
     """Wall time (render + read of the converged-enough image, synchronised)
     for plain accumulation and for the denoised pipeline to reach
     MSE <= MSE_TARGET against an FP64-accumulated reference of ref_spp samples."""
@@ -338,18 +338,156 @@ def time_to_mse(ctx, hs, kernel: int, ref_spp: int) -> dict:
         return meansq(ctx.read_denoised(), ref), t
 
     denoised(4)  # warm-up
-    curve = {}
+    points = {}
     best = None
     for s in DENOISE_SPP:
         m, t = denoised(s)
-        curve[s] = {"mse": m, "seconds": t, "plain_mse": plain(s)[0]}
+        points[s] = {"mse": m, "seconds": t, "plain_mse": plain(s)[0] if curve else None}
         if m <= MSE_TARGET:
             best = {"spp": s, "seconds": t, "mse": m}
             break
     out["denoised"] = best
-    out["denoised_curve"] = curve
+    if curve:
+        out["denoised_curve"] = points
     out["speedup"] = (out["plain"]["seconds"] / best["seconds"]) if best else None
     unet.close()
+    return out
+
+
+def time_to_mse_seeds(device_index: int, kernel: int, ref_spp: int, seeds=(2, 3, 4)) -> dict:
+    """time_to_mse on mid scenes of other seeds (held out: the denoiser's
+    training scenes come from pt_gb300.trainset, not from these)."""
+    import pt_gb300 as P
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        for s in seeds:
+            from pt_gb300 import scenes
+            hs = P.HostScene.load(scenes.mid_scene(Path(td) / f"mid{s}", seed=s))
+            c = P.Context(device_index)
+            c.upload(hs.pack())
+            c.build_accel()
+            r = time_to_mse(c, hs, kernel, ref_spp, curve=False)
+            out[str(s)] = {"plain_spp": r["plain"]["spp"], "plain_s": r["plain"]["seconds"],
+                           "denoised_spp": (r["denoised"] or {}).get("spp"),
+                           "denoised_s": (r["denoised"] or {}).get("seconds"), "speedup": r.get("speedup")}
+            c.close()
+    sp = [v["speedup"] for v in out.values() if v["speedup"]]
+    return {"seeds": out, "speedup_min": min(sp) if sp else None,
+            "speedup_median": statistics.median(sp) if sp else None}
+
+
+HEAVY = {"width": 1920, "height": 1080, "bounces": 12, "rr_start": 4, "ref_spp": 16384}
+HEAVY_DENOISE_SPP = (4, 8, 16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024)
+
+
+def time_to_mse_heavy(device_index: int, ref_spp: int = HEAVY["ref_spp"]) -> dict:
+    """Time to MSE <= 1e-3 on the heavy configuration: ~2M unique triangles
+    in 64 BLASes, 10,000 instances, 256 emitters, 1920x1080, 12 bounces,
+    Russian roulette from segment 4, against a `ref_spp`-sample image
+    accumulated in FP64 on the GPU.
+
+    plain     the smallest spp whose running mean reaches the threshold,
+              found by rendering progressively (chunks sized from the 1/spp
+              decay of the error, down to 8 spp; untimed), then timed as one
+              uninterrupted render of that many samples;
+    denoised  the first spp of HEAVY_DENOISE_SPP whose denoised image
+              reaches it, then bisected between that rung and the one
+              below; timed as render (with features and the half-sample
+              snapshot) + network, synchronised."""
+    import math
+    import numpy as np
+    import pt_gb300 as P
+    from pt_gb300 import abi, scenes
+    from pt_gb300.denoise import WEIGHTS_DIR, UNet, load_params
+
+    W, H, B, RR = HEAVY["width"], HEAVY["height"], HEAVY["bounces"], HEAVY["rr_start"]
+    raw, cam = scenes.heavy_scene()
+    hs = P.HostScene.from_raw(raw, cam)
+    ctx = P.Context(device_index)
+    ctx.upload(hs.pack())
+    ctx.build_accel()
+
+    def params(n, first=0, mode=abi.PT_ACCUM_FP32):
+        return hs.render_params(W, H, n, B, sample_index=first, accum_mode=mode, rr_start=RR)
+
+    t0 = time.perf_counter()
+    st = ctx.render(params(ref_spp, mode=abi.PT_ACCUM_FP32_FP64))
+    ref = ctx.read_image(fp64=True)
+    ref_s = time.perf_counter() - t0
+    ref32 = np.ascontiguousarray(ref.astype(np.float32))
+    out = {"threshold": MSE_TARGET, "metric": "meansq over RGB (meansq.cpp)",
+           "config": f"heavy scene {W}x{H}, {B} bounces, Russian roulette from segment {RR}",
+           "reference": {"spp": ref_spp, "accumulation": "fp64 on the GPU", "seconds": round(ref_s, 3),
+                         "mpath_segs_s": st.segments / st.milliseconds / 1e3}}
+
+    # plain: progressive search (untimed), then one timed render
+    n, m = 32, None
+    ctx.render(params(32), stats=False)
+    m = ctx.mse(ref32)
+    trail = [(n, m)]
+    while m > MSE_TARGET:
+        proj = n * m / MSE_TARGET
+        step = int(min(512, max(8, round((proj - n) * 0.7))))
+        ctx.render(params(step, first=n), stats=False)
+        n += step
+        m = ctx.mse(ref32)
+        trail.append((n, m))
+    ctx.synchronize()
+    t = time.perf_counter()
+    ctx.render(params(n), stats=False)
+    ctx.synchronize()
+    plain_s = time.perf_counter() - t
+    m_check = ctx.mse(ref32)
+    out["plain"] = {"spp": n, "seconds": plain_s, "mse": m_check, "previous_step": trail[-2] if len(trail) > 1 else None}
+
+    wfile = WEIGHTS_DIR / "unet.bin"
+    if not wfile.exists():
+        out["denoised"] = None
+        ctx.close()
+        return out
+    unet = UNet(1, H, W)
+    unet.set_params(load_params(wfile))
+
+    def denoised(s):
+        p = params(s)
+        ctx.synchronize()
+        tt = time.perf_counter()
+        ctx.render_denoised(unet, p)
+        ctx.synchronize()
+        tt = time.perf_counter() - tt
+        return meansq(ctx.read_denoised(), ref), tt, ctx.mse(ref32)
+
+    denoised(4)  # warm-up
+    curve, best, below = {}, None, None
+    for s in HEAVY_DENOISE_SPP:
+        if s >= n:
+            break
+        md, td, mp = denoised(s)
+        curve[s] = {"mse": md, "seconds": td, "plain_mse": mp}
+        if md <= MSE_TARGET:
+            best = {"spp": s, "seconds": td, "mse": md}
+            break
+        below = s
+    if best is not None and below is not None:
+        lo, hi = below, best["spp"]
+        while hi - lo > max(2, lo // 16):
+            mid_s = (lo + hi) // 2
+            md, td, mp = denoised(mid_s)
+            curve[mid_s] = {"mse": md, "seconds": td, "plain_mse": mp}
+            if md <= MSE_TARGET:
+                hi, best = mid_s, {"spp": mid_s, "seconds": td, "mse": md}
+            else:
+                lo = mid_s
+    out["denoised"] = best
+    out["denoised_curve"] = dict(sorted(curve.items()))
+    out["speedup"] = plain_s / best["seconds"] if best else None
+    if best is None:
+        below_plain = [s for s in curve if s < n]
+        out["denoised_shortfall"] = (f"the denoised image did not reach MSE {MSE_TARGET} at any tried spp below "
+                                     f"plain's {n}; lowest denoised MSE "
+                                     f"{min(v['mse'] for v in curve.values()):.4g}" if below_plain else None)
+    unet.close()
+    ctx.close()
     return out
 
 
@@ -576,7 +714,13 @@ def run_ours(args) -> None:
             osc, keep_o, oparams = oracle_scene(Path(td.name) / "oracle")
             base = cpu_baseline(osc, oparams, seconds_target=float(args.cpu_seconds))
             del osc, keep_o
-        ttm = time_to_mse(ctx, hs, args.kernel, args.ref_spp) if not args.no_mse else None
+        ttm = None
+        if not args.no_mse:
+            ttm = time_to_mse(ctx, hs, args.kernel, args.ref_spp)
+            if not args.no_seeds:
+                ttm["held_out_seeds"] = time_to_mse_seeds(device_index, args.kernel, args.ref_spp)
+            if not args.no_heavy:
+                ttm["heavy"] = time_to_mse_heavy(device_index, args.heavy_ref_spp)
         batches = None
         if not args.no_batch:
             batches = {"uneven_64": batch_bench(device_index),
@@ -620,6 +764,10 @@ def main():
     ap.add_argument("--no-mse", action="store_true", help="skip the time-to-MSE measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering measurement")
     ap.add_argument("--ref-spp", type=int, default=REF_SPP)
+    ap.add_argument("--no-seeds", action="store_true", help="skip time to MSE on held-out mid-scene seeds")
+    ap.add_argument("--no-heavy", action="store_true", help="skip time to MSE on the heavy configuration")
+    ap.add_argument("--heavy-ref-spp", type=int, default=HEAVY["ref_spp"])
+    ap.add_argument("--heavy-only", action="store_true", help="only the heavy time-to-MSE leg (one JSON line)")
     ap.add_argument("--denoise-profile", type=int, default=0, help="only run the denoised pipeline at this spp (profiling)")
     ap.add_argument("--width", type=int, default=1024, help="smaller images only for profiling captures")
     ap.add_argument("--height", type=int, default=1024)
@@ -629,7 +777,9 @@ def main():
     WIDTH, HEIGHT, SPP = args.width, args.height, args.spp
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.heavy_only:
+        print(json.dumps({"time_to_mse_heavy": time_to_mse_heavy(0, args.heavy_ref_spp)}), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.denoise_profile:
         run_denoise_profile(args)

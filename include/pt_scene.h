@@ -121,7 +121,17 @@ int pt_read_hdr(const char* path, float** rgba, uint32_t* width, uint32_t* heigh
 int pt_png_decode(const uint8_t* data, size_t size, uint8_t** texels, uint32_t* width, uint32_t* height,
                   uint32_t* channels, uint32_t* file_channels);
 
-/* Release memory returned by pt_read_hdr. */
+/* Decodes a baseline (sequential Huffman, 8-bit) JPEG image as the
+ * reference's texture loader keeps it (stb_image, texturedata.cpp:30-48): 1
+ * channel for greyscale files, 4 (RGB + alpha 255) for colour files; rows from
+ * the top; release *texels with pt_host_free.  Texels may differ from
+ * stb_image's by a few units (its integer IDCT and fixed-point colour
+ * conversion round differently).  Progressive, lossless and arithmetic-coded
+ * files are refused with PT_ERR_IO. */
+int pt_jpeg_decode(const uint8_t* data, size_t size, uint8_t** texels, uint32_t* width, uint32_t* height,
+                   uint32_t* channels, uint32_t* file_channels);
+
+/* Release memory returned by pt_read_hdr, pt_png_decode and pt_jpeg_decode. */
 void pt_host_free(void* p);
 
 #ifdef __cplusplus

@@ -133,6 +133,12 @@ def ref():
         R.ref_is_emitter.argtypes = [C.POINTER(abi.Material)]
         R.ref_parse_transform.restype = C.c_int
         R.ref_parse_transform.argtypes = [C.c_char_p, C.POINTER(C.c_float)]
+        R.ref_image_decode.restype = C.c_int
+        R.ref_image_decode.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_uint8), C.c_int, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        R.ref_jpeg_encode.restype = C.c_int
+        R.ref_jpeg_encode.argtypes = [C.POINTER(C.c_uint8), C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint8),
+                                      C.c_int]
         _ref = R
     return _ref
 

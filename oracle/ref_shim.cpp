@@ -2,7 +2,8 @@
 // the oracle.  TEST INFRASTRUCTURE ONLY: compiled by oracle/Makefile together
 // with the reference's sources where they lie (src/rng.cpp, lalgebra.cpp,
 // colour.cpp, scene/camera.cpp, scene/lightsample.cpp, scene/material.cpp,
-// io/tokenstream.cpp, io/parseutil.cpp) into oracle/_ref/libptref.so.  No
+// io/tokenstream.cpp, io/parseutil.cpp, io/imagewrite.cpp for stb_image_write,
+// scene/texturedata.cpp for stb_image) into oracle/_ref/libptref.so.  No
 // reference source is copied into this repository.
 #include <cstring>
 #include <vector>
@@ -16,6 +17,9 @@
 #include "scene/camera.h"
 #include "scene/lightsample.h"
 #include "scene/scene.h"
+
+#include <stb/stb_image.h>
+#include <stb/stb_image_write.h>
 
 #include "../include/pt_scene.h"
 
@@ -180,6 +184,55 @@ int ref_parse_transform(const char* line, float out_colmajor[16])
     } catch (...) {
         return -2;
     }
+}
+
+// A texture image decoded by the reference's stb_image as TextureData loads
+// it (texturedata.cpp:64-76): the file's channel count with 3 widened to 4.
+// Returns the byte count written (or -1).
+int ref_image_decode(const uint8_t* data, int size, uint8_t* out, int cap, int* w, int* h, int* channels)
+{
+    int x, y, comp;
+    if (!stbi_info_from_memory(data, size, &x, &y, &comp))
+        return -1;
+    const int want = comp == 3 ? 4 : comp;
+    unsigned char* px = stbi_load_from_memory(data, size, &x, &y, &comp, want);
+    if (!px)
+        return -1;
+    const int n = x * y * want;
+    if (n > cap) {
+        stbi_image_free(px);
+        return -1;
+    }
+    std::memcpy(out, px, (size_t)n);
+    stbi_image_free(px);
+    *w = x;
+    *h = y;
+    *channels = want;
+    return n;
+}
+
+namespace {
+struct Sink {
+    uint8_t* out;
+    int cap, n;
+};
+void sink_write(void* ctx, void* data, int size)
+{
+    Sink* s = (Sink*)ctx;
+    if (s->n + size <= s->cap)
+        std::memcpy(s->out + s->n, data, (size_t)size);
+    s->n += size;
+}
+} // namespace
+
+// A JPEG written by the reference's vendored stb_image_write (baseline;
+// chroma subsampled 2x2 at quality <= 90).  Returns the byte count (or -1).
+int ref_jpeg_encode(const uint8_t* pixels, int w, int h, int comp, int quality, uint8_t* out, int cap)
+{
+    Sink s{out, cap, 0};
+    if (!stbi_write_jpg_to_func(sink_write, &s, w, h, comp, pixels, quality))
+        return -1;
+    return s.n <= cap ? s.n : -1;
 }
 
 } // extern "C"

@@ -184,6 +184,8 @@ SIGNATURES = [
     ("pt_host_free", None, [C.c_void_p]),
     ("pt_png_decode", C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_uint32),
                                 C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    ("pt_jpeg_decode", C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_uint32),
+                                C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     # denoiser (include/pt_denoise.h)
     ("pt_debug_poke_tlas_link", C.c_int, [C.c_void_p, C.c_int]),
     ("pt_unet_param_count", C.c_size_t, []),

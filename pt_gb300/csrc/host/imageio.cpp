@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../../include/pt_scene.h"
+#include "jpeg.h"
 #include "png.h"
 
 namespace {
@@ -277,6 +278,28 @@ int pt_read_hdr(const char* path, float** rgba, uint32_t* width, uint32_t* heigh
     *rgba = out;
     *width = (uint32_t)W;
     *height = (uint32_t)H;
+    return PT_OK;
+}
+
+int pt_jpeg_decode(const uint8_t* data, size_t size, uint8_t** texels, uint32_t* width, uint32_t* height,
+                   uint32_t* channels, uint32_t* file_channels)
+{
+    if (!data || !texels || !width || !height || !channels)
+        return PT_ERR_INVALID;
+    pt::host::JpegImage img;
+    std::string err;
+    if (!pt::host::jpeg_decode(data, size, img, err))
+        return PT_ERR_IO;
+    uint8_t* out = (uint8_t*)std::malloc(img.texels.size());
+    if (!out)
+        return PT_ERR_OOM;
+    std::memcpy(out, img.texels.data(), img.texels.size());
+    *texels = out;
+    *width = img.width;
+    *height = img.height;
+    *channels = img.channels;
+    if (file_channels)
+        *file_channels = img.file_channels;
     return PT_OK;
 }
 

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "../../../include/pt_scene.h"
+#include "jpeg.h"
 #include "json.h"
 #include "png.h"
 
@@ -58,6 +59,13 @@ Mat4 mul(const Mat4& a, const Mat4& b)
         for (int i = 0; i < 4; i++)
             r.m[j][i] = ((a.m[0][i] * b.m[j][0] + a.m[1][i] * b.m[j][1]) + a.m[2][i] * b.m[j][2]) + a.m[3][i] * b.m[j][3];
     return r;
+}
+
+// glm's mat4 * vec4 (type_mat4x4.inl): (m0*x + m1*y) + (m2*z + m3*w) per row.
+void transform_point(const Mat4& m, const float v[3], float w, float out[3])
+{
+    for (int i = 0; i < 3; i++)
+        out[i] = (m.m[0][i] * v[0] + m.m[1][i] * v[1]) + (m.m[2][i] * v[2] + m.m[3][i] * w);
 }
 
 // lalgebra.cpp:5-14
@@ -221,11 +229,22 @@ bool has_alpha_below_one(const HostTexture& t)
 
 // An encoded texture image as TextureData keeps it (texturedata.cpp:30-48:
 // the file's channel count with 3 widened to 4; sRGB only for 4 channels).
-// PNG only: JPEG and other formats are rejected.
+// PNG and baseline JPEG; other formats are rejected.
 HostTexture decode_texture(const std::vector<uint8_t>& bytes, const std::string& what, bool srgb)
 {
-    if (bytes.size() >= 3 && bytes[0] == 0xFF && bytes[1] == 0xD8 && bytes[2] == 0xFF)
-        throw std::runtime_error("Failed to read texture " + what + " (JPEG textures are not supported)");
+    if (bytes.size() >= 3 && bytes[0] == 0xFF && bytes[1] == 0xD8 && bytes[2] == 0xFF) {
+        pt::host::JpegImage jpg;
+        std::string err;
+        if (!pt::host::jpeg_decode(bytes.data(), bytes.size(), jpg, err))
+            throw std::runtime_error("Failed to read texture " + what + ": " + err);
+        HostTexture ht;
+        ht.width = jpg.width;
+        ht.height = jpg.height;
+        ht.channels = jpg.channels;
+        ht.srgb = (jpg.channels == 4 && srgb) ? 1u : 0u;
+        ht.texels = std::move(jpg.texels);
+        return ht;
+    }
     pt::host::PngImage png;
     std::string err;
     if (!pt::host::png_decode(bytes.data(), bytes.size(), png, err))
@@ -323,6 +342,44 @@ struct Accessor {
     }
 };
 
+// The binary glTF container (.glb, glTF 2.0 section 4.4): a 12-byte header
+// (magic "glTF", version 2, total length) and chunks of (length, type, data),
+// the JSON chunk first and an optional BIN chunk that buffer 0 refers to when
+// it has no uri.  Returns false when `file` is not a .glb.
+bool split_glb(const std::string& file, std::string& json, std::vector<uint8_t>& bin, bool& has_bin)
+{
+    if (file.size() < 12 || std::memcmp(file.data(), "glTF", 4) != 0)
+        return false;
+    uint32_t version, length;
+    std::memcpy(&version, file.data() + 4, 4);
+    std::memcpy(&length, file.data() + 8, 4);
+    if (version != 2)
+        throw std::runtime_error("unsupported .glb version " + std::to_string(version));
+    if (length > file.size() || length < 12)
+        throw std::runtime_error(".glb shorter than its header says");
+    has_bin = false;
+    bool has_json = false;
+    size_t off = 12;
+    while (off + 8 <= length) {
+        uint32_t clen, ctype;
+        std::memcpy(&clen, file.data() + off, 4);
+        std::memcpy(&ctype, file.data() + off + 4, 4);
+        if ((uint64_t)off + 8 + clen > length)
+            throw std::runtime_error(".glb chunk runs past the end of the file");
+        if (ctype == 0x4E4F534Au && !has_json) {
+            json.assign(file.data() + off + 8, clen);
+            has_json = true;
+        } else if (ctype == 0x004E4942u && !has_bin) {
+            bin.assign(file.begin() + off + 8, file.begin() + off + 8 + clen);
+            has_bin = true;
+        }
+        off += 8 + (size_t)clen;
+    }
+    if (!has_json)
+        throw std::runtime_error(".glb without a JSON chunk");
+    return true;
+}
+
 // glTF 2.0 import with the Assimp behaviour the reference relies on
 // (scene.cpp:537-550 import flags, :74-296 material extraction):
 //  - every mesh primitive becomes one mesh with one material (variant);
@@ -335,16 +392,31 @@ struct Accessor {
 //    sheen to 0, clearcoat 0 with roughness 0.5, anisotropy 0 (:263-295);
 //  - KHR_materials_emissive_strength gives the emission strength (:140-143);
 //  - KHR_materials_transmission gives opacity = 1 - transmission (:96-108).
-// Textures: PNG images (files, data URIs or buffer views); JPEG is rejected.
-// Cameras and lights inside glTF files are not imported.
+// Textures: PNG and baseline JPEG images (files, data URIs or buffer views).
+// Cameras inside glTF files are not imported: the reference hands the model
+// import a dummy camera and keeps the .scn one (scenebuild.cpp:306-317).
+// KHR_lights_punctual point and directional lights are (see below).
 Model load_gltf(const std::string& path)
 {
     std::string text = read_file(path);
+    std::string glb_json;
+    std::vector<uint8_t> glb_bin;
+    bool has_glb_bin = false;
+    if (split_glb(text, glb_json, glb_bin, has_glb_bin))
+        text.swap(glb_json);
     Json doc = pth::JsonParser(text).parse();
     std::string dir = directory_of(path);
     std::vector<std::vector<uint8_t>> buffers;
     for (size_t b = 0; b < doc["buffers"].size(); b++) {
         const Json& jb = doc["buffers"][b];
+        if (!jb.has("uri")) {
+            if (b != 0 || !has_glb_bin)
+                throw std::runtime_error("buffer " + std::to_string(b) + " has no uri and no .glb BIN chunk");
+            buffers.push_back(glb_bin);
+            if ((int64_t)buffers.back().size() < jb["byteLength"].integer(0))
+                throw std::runtime_error("buffer 0 shorter than its byteLength");
+            continue;
+        }
         std::string uri = jb["uri"].str;
         if (uri.rfind("data:", 0) == 0) {
             size_t comma = uri.find(',');
@@ -645,6 +717,26 @@ Model load_gltf(const std::string& path)
         Mat4 S = scaling((float)s[0].number(1), (float)s[1].number(1), (float)s[2].number(1));
         return mul(mul(T, R), S);
     };
+    // KHR_lights_punctual: Assimp's glTF importer turns every light of the
+    // extension's list, in list order, into an aiLight in the light's own node
+    // space (position (0, 0, 0), direction (0, 0, -1)) with colour * intensity;
+    // the reference keeps point and directional lights and skips spot lights
+    // (process_lights, scene.cpp:440-466).  The node transform is not applied.
+    const Json& lights = doc["extensions"]["KHR_lights_punctual"]["lights"];
+    for (size_t li = 0; li < lights.size(); li++) {
+        const Json& L = lights[li];
+        const std::string& type = L["type"].str;
+        const float intensity = (float)L["intensity"].number(1.0);
+        float c[3];
+        for (int k = 0; k < 3; k++)
+            c[k] = (float)L["color"][(size_t)k].number(1.0) * intensity;
+        if (type == "point")
+            md.point_lights.insert(md.point_lights.end(), {0.0f, 0.0f, 0.0f, c[0], c[1], c[2]});
+        else if (type == "directional")
+            md.dir_lights.insert(md.dir_lights.end(), {0.0f, 0.0f, -1.0f, c[0], c[1], c[2]});
+        else if (type != "spot")
+            throw std::runtime_error("unknown KHR_lights_punctual light type " + type);
+    }
     std::vector<std::pair<int64_t, Mat4>> stack;
     int64_t scene_idx = doc["scene"].integer(0);
     const Json& roots = doc["scenes"][(size_t)scene_idx]["nodes"];
@@ -1310,6 +1402,22 @@ pt_host_scene* load_scn(const std::string& path)
         if (s.instances.empty())
             continue;
         Model md = load_model(dir + s.path);
+        // the model's own lights, once per scene instance, moved by the
+        // instance transform (scenebuild.cpp:321-335)
+        for (const Mat4& si : s.instances) {
+            for (size_t k = 0; k + 6 <= md.point_lights.size(); k += 6) {
+                float p[3];
+                transform_point(si, &md.point_lights[k], 1.0f, p);
+                host->point_lights.insert(host->point_lights.end(), {p[0], p[1], p[2], md.point_lights[k + 3],
+                                                                     md.point_lights[k + 4], md.point_lights[k + 5]});
+            }
+            for (size_t k = 0; k + 6 <= md.dir_lights.size(); k += 6) {
+                float d[3];
+                transform_point(si, &md.dir_lights[k], 0.0f, d);
+                host->dir_lights.insert(host->dir_lights.end(), {d[0], d[1], d[2], md.dir_lights[k + 3],
+                                                                 md.dir_lights[k + 4], md.dir_lights[k + 5]});
+            }
+        }
         host->append_model(md, s.instances);
     }
     return host.release();

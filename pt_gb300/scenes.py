@@ -243,6 +243,56 @@ def write_gltf(path: Path, mesh, material: dict) -> None:
     path.write_text(json.dumps(doc))
 
 
+def write_glb(path: Path, mesh, material: dict, base_colour_image: bytes | None = None,
+              image_mime: str = "image/jpeg", lights: list | None = None) -> None:
+    """One mesh as a binary glTF (.glb): the JSON chunk and one BIN chunk
+    holding the vertex data and, optionally, an embedded base-colour image
+    (PNG or JPEG bytes, referenced through a buffer view).  `lights`: a list
+    of KHR_lights_punctual light dicts (type, color, intensity), each attached
+    to a node of its own."""
+    p, n, uv, idx = mesh
+    blobs = [np.ascontiguousarray(p, np.float32).tobytes(), np.ascontiguousarray(n, np.float32).tobytes(),
+             np.ascontiguousarray(uv, np.float32).tobytes(), np.ascontiguousarray(idx, np.uint32).reshape(-1).tobytes()]
+    if base_colour_image is not None:
+        blobs.append(bytes(base_colour_image))
+    bin_chunk, offsets = bytearray(), []
+    for b in blobs:
+        offsets.append(len(bin_chunk))
+        bin_chunk += b
+        bin_chunk += b"\0" * ((4 - len(b) % 4) % 4)
+    views = [{"buffer": 0, "byteOffset": o, "byteLength": len(b)} for o, b in zip(offsets, blobs)]
+    acc = [
+        {"bufferView": 0, "componentType": 5126, "count": len(p), "type": "VEC3",
+         "min": np.asarray(p).min(0).tolist(), "max": np.asarray(p).max(0).tolist()},
+        {"bufferView": 1, "componentType": 5126, "count": len(n), "type": "VEC3"},
+        {"bufferView": 2, "componentType": 5126, "count": len(uv), "type": "VEC2"},
+        {"bufferView": 3, "componentType": 5125, "count": int(np.asarray(idx).size), "type": "SCALAR"},
+    ]
+    pbr = {"metallicFactor": float(material.get("metallic", 0.0)), "roughnessFactor": float(material.get("roughness", 1.0))}
+    doc = {"asset": {"version": "2.0", "generator": "pt_gb300.scenes"}, "scene": 0,
+           "scenes": [{"nodes": [0]}], "nodes": [{"mesh": 0}],
+           "meshes": [{"name": path.stem, "primitives": [{"attributes": {"POSITION": 0, "NORMAL": 1, "TEXCOORD_0": 2},
+                                                          "indices": 3, "material": 0}]}],
+           "materials": [{"pbrMetallicRoughness": pbr}], "accessors": acc, "bufferViews": views,
+           "buffers": [{"byteLength": len(bin_chunk)}]}
+    if base_colour_image is not None:
+        doc["images"] = [{"bufferView": 4, "mimeType": image_mime}]
+        doc["textures"] = [{"source": 0}]
+        pbr["baseColorTexture"] = {"index": 0}
+    else:
+        pbr["baseColorFactor"] = [float(to_srgb(c)) for c in material.get("base", (0.8, 0.8, 0.8))] + [1.0]
+    if lights:
+        doc["extensionsUsed"] = ["KHR_lights_punctual"]
+        doc["extensions"] = {"KHR_lights_punctual": {"lights": lights}}
+        for i in range(len(lights)):
+            doc["nodes"].append({"extensions": {"KHR_lights_punctual": {"light": i}}, "translation": [0.0, 3.0, 0.0]})
+            doc["scenes"][0]["nodes"].append(len(doc["nodes"]) - 1)
+    js = json.dumps(doc).encode()
+    js += b" " * ((4 - len(js) % 4) % 4)
+    body = struct.pack("<II", len(js), 0x4E4F534A) + js + struct.pack("<II", len(bin_chunk), 0x004E4942) + bytes(bin_chunk)
+    path.write_bytes(struct.pack("<III", 0x46546C67, 2, 12 + len(body)) + body)
+
+
 def fmt(x: float) -> str:
     return repr(float(np.float32(x)))
 

@@ -24,6 +24,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(HERE))
 
 import oracle  # noqa: E402
 from pt_gb300 import abi, core, scenes  # noqa: E402
@@ -200,7 +201,49 @@ def meansq_cases():
     return out
 
 
+def _test_image(w, h, seed):
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w]
+    a = np.stack([128 + 100 * np.sin(x / 7.0), 128 + 100 * np.cos(y / 5.0 + x / 11.0), x * 255 // max(1, w - 1)], -1)
+    a[h // 3:h // 2, w // 4:w // 2] = [250, 10, 30]
+    return np.clip(a + rng.normal(0, 12, a.shape), 0, 255).astype(np.uint8)
+
+
+def jpeg_cases(R):
+    """JPEG files and their texels as the reference's stb_image decodes them
+    (TextureData, texturedata.cpp:64-76): files written by the reference's
+    own stb_image_write (4:2:0 at quality 75, 4:4:4 at 95) and by
+    jpeg_writer.py (greyscale, 4:2:2, 4:4:0, 4:2:0 with restart intervals,
+    RGB component ids)."""
+    import jpeg_writer
+    out = []
+    for w, h in [(24, 16), (37, 23)]:
+        src = _test_image(w, h, w * 7 + h)
+        files = []
+        for q in (75, 95):
+            buf = (C.c_uint8 * (1 << 20))()
+            n = R.ref_jpeg_encode(src.ctypes.data_as(C.POINTER(C.c_uint8)), w, h, 3, q, buf, len(buf))
+            assert n > 0
+            files.append((f"stb_q{q}", bytes(buf[:n])))
+        files += [("grey", jpeg_writer.encode(src[..., 0])),
+                  ("grey_restart3", jpeg_writer.encode(src[..., 1], restart=3)),
+                  ("h2v1", jpeg_writer.encode(src, sampling=(2, 1))),
+                  ("h1v2", jpeg_writer.encode(src, sampling=(1, 2))),
+                  ("h2v2_restart2", jpeg_writer.encode(src, sampling=(2, 2), restart=2)),
+                  ("rgb_ids", jpeg_writer.encode(src, rgb_ids=True))]
+        for name, data in files:
+            texels = (C.c_uint8 * (w * h * 4))()
+            ww, hh, ch = C.c_int(), C.c_int(), C.c_int()
+            n = R.ref_image_decode(data, len(data), texels, len(texels), C.byref(ww), C.byref(hh), C.byref(ch))
+            assert n == ww.value * hh.value * ch.value
+            out.append({"name": f"{name}_{w}x{h}", "jpeg": base64.b64encode(data).decode(), "width": ww.value,
+                        "height": hh.value, "channels": ch.value,
+                        "stb_texels": base64.b64encode(bytes(texels[:n])).decode()})
+    return out
+
+
 def main():
+    only = set(sys.argv[1:])  # fixture file names to write (default: all)
     oracle.build(reference=True)
     R = oracle.ref()
     assert R is not None, "oracle/_ref was not built"
@@ -213,9 +256,14 @@ def main():
         "instance_matrices.json": instance_matrices(R),
         "parse_transform.json": transforms(R),
         "light_stream.json": light_streams(R),
-        "meansq.json": meansq_cases(),
+        "meansq.json": meansq_cases,
+        "jpeg.json": lambda: jpeg_cases(R),
     }
     for name, data in fixtures.items():
+        if only and name not in only:
+            continue
+        if callable(data):
+            data = data()
         (HERE / name).write_text(json.dumps(data))
         print("wrote", name)
 
