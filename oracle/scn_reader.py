@@ -10,8 +10,11 @@ tests/test_oracle_scn_reader.py.  It covers what the benchmark scenes use:
 camera keys, envcol, objects, instances with s/r/t transforms, glTF meshes
 (POSITION, NORMAL, TEXCOORD_0, indices, node TRS/matrix hierarchy) and
 factor materials (base colour, metallic/roughness, emission with
-KHR_materials_emissive_strength, KHR_materials_transmission).  Textures,
-point/directional lights and OBJ files are refused.
+KHR_materials_emissive_strength, KHR_materials_transmission), one mesh,
+node and material per model file, and the reference's Assimp
+post-processing where it acts on such a file (FindDegenerates,
+JoinIdenticalVertices).  Textures, point/directional lights, OBJ files and
+multi-mesh files are refused.
 
 Reference semantics followed (file:line in anveba/pt):
   .scn camera section            src/scene/scenebuild.cpp:132-197 (defaults :138-144)
@@ -239,6 +242,47 @@ def read_gltf(path: Path):
             np.array(materials, np.float32).reshape(-1, 24))
 
 
+def assimp_single_mesh(v: np.ndarray, idx: np.ndarray):
+    """The reference's Assimp post-processing (scene.cpp:537-550) where it
+    acts on a file of one mesh, one node and one material: FindDegenerates
+    with Assimp's defaults (a triangle with two equal vertex positions keeps
+    fewer indices; the reference stores it as (0, 0, 0)), then
+    JoinIdenticalVertices (vertices no face uses dropped, vertices equal in
+    every attribute to an earlier one replaced by it, first occurrence in
+    vertex order kept).  Returns (vertices, indices)."""
+    f = idx.reshape(-1, 3).astype(np.int64)
+    p = v[:, :3]
+    faces = []  # the indices each face keeps
+    for a, b, c in f:
+        keep = [a, b, c]
+        i = 0
+        while i < len(keep):
+            k = i + 1
+            while k < len(keep):
+                if np.array_equal(p[keep[i]], p[keep[k]]):
+                    del keep[k]
+                else:
+                    k += 1
+            i += 1
+        faces.append(keep)
+    used = np.zeros(len(v), bool)
+    for keep in faces:
+        used[keep] = True
+    key = v.copy()
+    key[key == 0] = 0  # +0 and -0 compare equal
+    rows = key.view(np.uint32)
+    ids = np.nonzero(used)[0]
+    _, first, inverse = np.unique(rows[ids], axis=0, return_index=True, return_inverse=True)
+    rank = np.empty(len(first), np.int64)
+    rank[np.argsort(first)] = np.arange(len(first))
+    new_index = np.zeros(len(v), np.int64)
+    new_index[ids] = rank[inverse.reshape(-1)]
+    out_v = v[ids[np.sort(first)]]
+    out_i = np.array([[new_index[k] for k in keep] if len(keep) == 3 else [0, 0, 0] for keep in faces],
+                     np.uint32).reshape(-1)
+    return out_v.astype(np.float32), out_i
+
+
 def read_scn(path) -> tuple[dict, dict]:
     """A .scn file -> (raw scene dict, camera dict) (scenebuild.cpp:279-365)."""
     path = Path(path)
@@ -317,6 +361,10 @@ def read_scn(path) -> tuple[dict, dict]:
         if not scene_instances:
             continue
         v, ix, ms, mm, mi, mt = read_gltf(path.parent / rel)
+        if len(ms) != 1 or len(mt) != 1 or sum(len(x) for x in mi) != 1:
+            raise NotImplementedError("the oracle's scene reader takes model files of one mesh, node and material")
+        v, ix = assimp_single_mesh(v, ix)
+        ms = [(0, 0, len(ix) // 3, len(v))]
         verts.append(v)
         idxs.append(ix)
         for m, (vo, io, tris, vc) in enumerate(ms):

@@ -31,7 +31,7 @@ CU_SOURCES = ["api.cu", "batch.cu", "render_mega.cu", "render_wave.cu", "bvh_bui
               "nn/conv.cu", "nn/conv_rows.cu", "nn/ops.cu", "nn/unet.cu", "nn/api_nn.cu"]
 # The denoiser is not on the bit-exact path: let it contract multiply-adds.
 NN_FLAGS = [f for f in NVCC_FLAGS if f != "-fmad=false"]
-CPP_SOURCES = ["host/scene.cpp", "host/imageio.cpp", "host/png.cpp", "host/jpeg.cpp"]
+CPP_SOURCES = ["host/scene.cpp", "host/imageio.cpp", "host/png.cpp", "host/jpeg.cpp", "host/assimp_post.cpp"]
 HEADERS = list(CSRC.rglob("*.cuh")) + list(CSRC.rglob("*.h")) + list((HERE.parent / "include").glob("*.h"))
 
 

@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <limits>
 #include <numeric>
 #include <optional>
@@ -31,42 +32,21 @@
 
 #include "../../../include/pt_scene.h"
 #include "jpeg.h"
+#include "model.h"
 #include "json.h"
 #include "png.h"
 
 using pth::Json;
+using pt::host::HostTexture;
+using pt::host::Mat4;
+using pt::host::Model;
+using pt::host::ModelNode;
+using pt::host::mul;
+using pt::host::transform_point;
 
 namespace {
 
 thread_local std::string g_error;
-
-struct Mat4 {
-    float m[4][4]; // column-major, m[col][row] (the reference's glm::mat4)
-    static Mat4 identity()
-    {
-        Mat4 r{};
-        for (int i = 0; i < 4; i++)
-            r.m[i][i] = 1.0f;
-        return r;
-    }
-};
-
-// glm-style column-major product, each entry summed left to right.
-Mat4 mul(const Mat4& a, const Mat4& b)
-{
-    Mat4 r;
-    for (int j = 0; j < 4; j++)
-        for (int i = 0; i < 4; i++)
-            r.m[j][i] = ((a.m[0][i] * b.m[j][0] + a.m[1][i] * b.m[j][1]) + a.m[2][i] * b.m[j][2]) + a.m[3][i] * b.m[j][3];
-    return r;
-}
-
-// glm's mat4 * vec4 (type_mat4x4.inl): (m0*x + m1*y) + (m2*z + m3*w) per row.
-void transform_point(const Mat4& m, const float v[3], float w, float out[3])
-{
-    for (int i = 0; i < 3; i++)
-        out[i] = (m.m[0][i] * v[0] + m.m[1][i] * v[1]) + (m.m[2][i] * v[2] + m.m[3][i] * w);
-}
 
 // lalgebra.cpp:5-14
 Mat4 translation(float x, float y, float z)
@@ -198,24 +178,6 @@ std::string directory_of(const std::string& file)
 }
 
 // ---------------------------------------------------------------- loaded model
-// One texture as the reference's TextureData holds it: 8-bit texels with 1, 2
-// or 4 channels (3-channel images widened to 4), srgb only meaningful for 4.
-struct HostTexture {
-    uint32_t width = 0, height = 0, channels = 0, srgb = 0;
-    std::vector<uint8_t> texels;
-};
-
-struct Model {
-    std::vector<float> vertices; // PT_VERTEX_FLOATS each
-    std::vector<uint32_t> indices;
-    std::vector<pt_mesh_range> meshes;
-    std::vector<uint32_t> mesh_material;
-    std::vector<std::vector<Mat4>> mesh_instances;
-    std::vector<pt_material> materials;
-    std::vector<float> point_lights, dir_lights;
-    std::vector<HostTexture> textures;
-};
-
 // TextureData::has_alpha_less_than_one (texturedata.cpp:150-164).
 bool has_alpha_below_one(const HostTexture& t)
 {
@@ -688,7 +650,6 @@ Model load_gltf(const std::string& path)
             if ((size_t)mat >= md.materials.size())
                 throw std::runtime_error("primitive names a missing material");
             md.mesh_material.push_back((uint32_t)mat);
-            md.mesh_instances.emplace_back();
         }
     }
     // nodes
@@ -737,32 +698,40 @@ Model load_gltf(const std::string& path)
         else if (type != "spot")
             throw std::runtime_error("unknown KHR_lights_punctual light type " + type);
     }
-    std::vector<std::pair<int64_t, Mat4>> stack;
-    int64_t scene_idx = doc["scene"].integer(0);
-    const Json& roots = doc["scenes"][(size_t)scene_idx]["nodes"];
-    for (size_t k = 0; k < roots.size(); k++)
-        stack.push_back({roots[k].integer(-1), Mat4::identity()});
-    size_t visited = 0;
-    while (!stack.empty()) {
-        auto [ni, parent] = stack.back();
-        stack.pop_back();
-        if (++visited > 1000000)
-            throw std::runtime_error("node graph has a cycle");
+    // The node graph reachable from the scene's roots (a forest: a node with
+    // two parents or a cycle is refused).  Nodes that carry a light or a
+    // camera are locked for the graph optimisation (Assimp locks the nodes
+    // lights and cameras are named after).
+    std::vector<int64_t> node_slot(doc["nodes"].size(), -1);
+    std::function<int(int64_t)> add_node = [&](int64_t ni) -> int {
         const Json& n = doc["nodes"][(size_t)ni];
-        if (n.kind != Json::OBJ)
+        if (ni < 0 || n.kind != Json::OBJ)
             throw std::runtime_error("missing node");
-        Mat4 M = mul(parent, node_matrix(n));
+        if (node_slot[(size_t)ni] >= 0)
+            throw std::runtime_error("node graph is not a tree (node " + std::to_string(ni) + " has two parents or a cycle)");
+        const int slot = (int)md.nodes.size();
+        node_slot[(size_t)ni] = slot;
+        ModelNode mn;
+        mn.local = node_matrix(n);
         if (n.has("mesh")) {
             size_t mi = (size_t)n["mesh"].integer(0);
             if (mi >= gltf_mesh_prims.size())
                 throw std::runtime_error("node names a missing mesh");
-            for (uint32_t m : gltf_mesh_prims[mi])
-                md.mesh_instances[m].push_back(M);
+            mn.meshes = gltf_mesh_prims[mi];
         }
+        mn.locked = n.has("camera") || n["extensions"].has("KHR_lights_punctual");
+        md.nodes.push_back(mn);
+        std::vector<int> children;
         const Json& ch = n["children"];
-        for (size_t k = ch.size(); k-- > 0;)
-            stack.push_back({ch[k].integer(-1), M});
-    }
+        for (size_t k = 0; k < ch.size(); k++)
+            children.push_back(add_node(ch[k].integer(-1)));
+        md.nodes[(size_t)slot].children = children;
+        return slot;
+    };
+    int64_t scene_idx = doc["scene"].integer(0);
+    const Json& roots = doc["scenes"][(size_t)scene_idx]["nodes"];
+    for (size_t k = 0; k < roots.size(); k++)
+        md.roots.push_back(add_node(roots[k].integer(-1)));
     return md;
 }
 
@@ -1054,7 +1023,13 @@ Model load_obj(const std::string& path)
         }
         md.meshes.push_back(range);
         md.mesh_material.push_back(mi);
-        md.mesh_instances.push_back({Mat4::identity()});
+    }
+    // Assimp's OBJ importer: a root node with one child per object/group run
+    md.nodes.resize(1 + md.meshes.size());
+    md.roots = {0};
+    for (size_t m = 0; m < md.meshes.size(); m++) {
+        md.nodes[0].children.push_back((int)m + 1);
+        md.nodes[m + 1].meshes = {(uint32_t)m};
     }
     for (const auto& tf : tex_files) {
         std::string f = read_file(dir + tf.first);
@@ -1064,7 +1039,8 @@ Model load_obj(const std::string& path)
     return md;
 }
 
-// Model import by file extension: .obj (Wavefront + MTL), otherwise glTF 2.0.
+// Model import by file extension: .obj (Wavefront + MTL), otherwise glTF 2.0
+// (.gltf or .glb), followed by the reference's Assimp post-processing.
 Model load_model(const std::string& path)
 {
     std::string ext;
@@ -1072,7 +1048,10 @@ Model load_model(const std::string& path)
     if (dot != std::string::npos)
         for (char c : path.substr(dot + 1))
             ext += (char)std::tolower((unsigned char)c);
-    return ext == "obj" ? load_obj(path) : load_gltf(path);
+    Model md = ext == "obj" ? load_obj(path) : load_gltf(path);
+    // the reference's import flags (scene.cpp:537-550), see assimp_post.cpp
+    pt::host::assimp_postprocess(md);
+    return md;
 }
 
 // ---------------------------------------------------------------- 4x4 inverse (FP64 cofactors)

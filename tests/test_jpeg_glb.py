@@ -149,3 +149,21 @@ def test_glb_rejects_broken_containers(tmp_path):
         (tmp_path / "a.glb").write_bytes(bad)
         with pytest.raises(P.PtError):
             P.HostScene.load(tmp_path / "a.scn")
+
+
+@pytest.mark.gpu
+def test_glb_jpeg_scene_bitexact_on_gpu(tmp_path):
+    """The .glb scene (JPEG base-colour map, point and directional lights)
+    rendered by the CUDA path equals the oracle bit for bit."""
+    hs = P.HostScene.load(glb_scene(tmp_path))
+    view = hs.pack()
+    params = hs.render_params(96, 64, 4, 5)
+    with P.Context(0) as ctx:
+        ctx.upload(view)
+        ctx.build_accel()
+        st = ctx.render(params)
+        assert st.error_word == 0
+        gpu = ctx.read_image()
+    ref, ost = oracle.OracleScene(view).render(params)
+    assert np.array_equal(gpu.view(np.uint32), ref.view(np.uint32))
+    assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays

@@ -50,27 +50,3 @@ def test_reader_equals_product_loader(tmp_path, make):
     oracle.lib().or_camera_params(scn_reader.camera_desc(cam), 64, 48, p_or)
     p_pt = hs.render_params(64, 48, 1, 1)
     assert bytes(p_or.inv_view) == bytes(p_pt.inv_view) and bytes(p_or.inv_proj) == bytes(p_pt.inv_proj)
-
-
-def test_reader_node_transforms(tmp_path):
-    """A glTF node hierarchy with TRS and a matrix, instanced twice by the .scn."""
-    import json
-    mesh = scenes.icosphere(1)
-    scenes.write_gltf(tmp_path / "obj.gltf", mesh, {"base": (0.5, 0.4, 0.3), "roughness": 0.3, "metallic": 1.0})
-    doc = json.loads((tmp_path / "obj.gltf").read_text())
-    doc["nodes"] = [{"children": [1, 2], "translation": [1.0, 2.0, 3.0], "rotation": [0.0, 0.38268343, 0.0, 0.9238795],
-                     "scale": [2.0, 2.0, 2.0]},
-                    {"mesh": 0, "matrix": [1, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1, 0, 0.25, 0, -1, 1]},
-                    {"mesh": 0, "translation": [-3.0, 0.0, 0.5]}]
-    doc["materials"][0]["extensions"] = {"KHR_materials_transmission": {"transmissionFactor": 0.25}}
-    (tmp_path / "obj.gltf").write_text(json.dumps(doc))
-    scn = scenes.ScnWriter({"eye": (0.0, 1.0, -5.0), "target": (0.0, 0.0, 0.0), "fov": 50.0}, (0.1, 0.2, 0.3))
-    scn.add_object("obj", "obj.gltf")
-    scn.add_instance("obj", scale=(1.5, 1.5, 1.5), rotate=(0.3, 1.0, -0.2, 0.7), translate=(1.0, 0.0, 2.0))
-    scn.add_instance("obj", rotate=(0.0, 0.0, 1.0, 1e-6))
-    scn.write(tmp_path / "t.scn")
-    raw, _ = scn_reader.read_scn(tmp_path / "t.scn")
-    want = P.HostScene.load(tmp_path / "t.scn").raw()
-    assert raw["instance_matrices"].shape == (4, 16)
-    for k in KEYS:
-        assert _same(raw[k], want[k]), k

@@ -175,13 +175,17 @@ def test_cli_help():
 
 
 def _textured_gltf(d: Path, name: str, images, textures, materials, prim_material=0):
-    """A quad glTF whose document carries the given images / textures / materials."""
+    """A quad glTF whose document carries the given images / textures /
+    materials; prim_material is the primitive's material, or a list: one
+    primitive (the same quad) per material listed."""
     scenes.write_gltf(d / f"{name}.gltf", scenes.quad(2.0, 0.0, False), {"base": (1, 1, 1)})
     doc = json.loads((d / f"{name}.gltf").read_text())
     doc["images"] = images
     doc["textures"] = textures
     doc["materials"] = materials
-    doc["meshes"][0]["primitives"][0]["material"] = prim_material
+    prim = doc["meshes"][0]["primitives"][0]
+    mats = prim_material if isinstance(prim_material, list) else [prim_material]
+    doc["meshes"][0]["primitives"] = [dict(prim, material=m) for m in mats]
     (d / f"{name}.gltf").write_text(json.dumps(doc))
 
 
@@ -212,7 +216,7 @@ def test_gltf_texture_order_srgb_channels_and_transparency(tmp_path):
         {"pbrMetallicRoughness": {"baseColorTexture": {"index": 3}}, "emissiveTexture": {"index": 0}},
         {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}}},
     ]
-    _textured_gltf(tmp_path, "tq", images, textures, materials)
+    _textured_gltf(tmp_path, "tq", images, textures, materials, prim_material=[0, 1, 2])
     hs = P.HostScene.load(scn(tmp_path, "camera:\n\nobjects:\ntq tq.gltf\ntq\n"))
     raw = hs.raw()
     tex = raw["textures"]
@@ -309,7 +313,10 @@ def test_obj_import(tmp_path):
     meshes = raw["meshes"]
     assert meshes.shape[0] == 4 and meshes[:, 2].tolist() == [2, 1, 1, 1]
     v = raw["vertices"]
-    first = v[meshes[0, 0]:meshes[0, 0] + 6]
+    # per-corner vertices joined by JoinIdenticalVertices: the quad keeps 4
+    assert meshes[0, 3] == 4
+    tri = raw["indices"][meshes[0, 1]:meshes[0, 1] + 6].reshape(2, 3) + meshes[0, 0]
+    first = v[tri.reshape(-1)]
     assert np.allclose(first[:, 3:6], [0, -1, 0]) or np.allclose(first[:, 3:6], [0, 1, 0])
     assert np.allclose(first[:3, 7], [1, 1, 0.75])  # 1 - v
     assert np.array_equal(first[3:, 0:3], np.array([[0, 0, 0], [1, 0, 1], [0, 0, 1]], np.float32))  # fan (0, 2, 3)
