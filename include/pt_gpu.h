@@ -342,7 +342,8 @@ int pt_mse_noalloc(const float* image_rgba, const float* reference_rgba, uint32_
  * one wavefront launch sequence (a wave holds consecutive samples of several
  * jobs, so small jobs fill the GPU together), the sequence is captured into a
  * CUDA graph and launched as one unit, and small jobs may instead run as
- * megakernel launches on a parallel branch of the same graph.  An autotuner
+ * megakernel launches on a parallel branch of the same graph.  Jobs with less
+ * work go into the first waves, so small jobs finish early.  An autotuner
  * times short trial batches (every job at 1/32 of its samples, at least one)
  * and picks the wave capacity (2^21, 2^23 or 2^25 paths in flight, within a
  * quarter of the free device memory), the megakernel tile and the
@@ -385,6 +386,12 @@ int pt_render_batch(pt_ctx* ctx, const pt_batch_job* jobs, uint32_t count, uint3
 /* Copy job `job`'s image of the last pt_render_batch to host memory, as
  * pt_read_image does (fp64 = 1 needs PT_ACCUM_FP32_FP64 for that job). */
 int pt_read_batch_image(pt_ctx* ctx, uint32_t job, void* rgba, size_t pitch_bytes, int fp64);
+/* Per-job latency of the last pt_render_batch: ms[j] = device time from the
+ * batch's start until job j's image was final (the wave holding its last
+ * samples, or its last megakernel launch, completed).  Waves take the jobs
+ * with the least work (pixels x samples) first.  `count` must be the last
+ * batch's job count. */
+int pt_batch_job_times(pt_ctx* ctx, float* ms, uint32_t count);
 
 #ifdef __cplusplus
 }

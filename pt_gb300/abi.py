@@ -166,6 +166,7 @@ SIGNATURES = [
     ("pt_mse_host", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     ("pt_mse_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("pt_render_batch", C.c_int, [C.c_void_p, C.POINTER(BatchJob), C.c_uint32, C.c_uint32, C.POINTER(BatchStats)]),
+    ("pt_batch_job_times", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32]),
     ("pt_read_batch_image", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t, C.c_int]),
     ("pt_scene_last_error", C.c_char_p, []),
     ("pt_scene_load", C.c_void_p, [C.c_char_p]),

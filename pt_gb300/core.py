@@ -235,6 +235,13 @@ class Context:
         self._batch_sizes = [(p.height, p.width) for _, p in jobs]
         return st
 
+    def batch_job_times(self) -> np.ndarray:
+        """Per-job completion times (ms from the start) of the last render_batch."""
+        n = len(self._batch_sizes)
+        out = np.zeros(n, np.float32)
+        _check(lib().pt_batch_job_times(self._h, _ptr(out, C.c_float), n), self._h)
+        return out
+
     def read_batch_image(self, job: int, fp64: bool = False) -> np.ndarray:
         h, w = self._batch_sizes[job]
         out = np.empty((h, w, 4), dtype=np.float64 if fp64 else np.float32)

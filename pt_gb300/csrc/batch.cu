@@ -60,6 +60,10 @@ struct BatchState {
     DevBuf<uint32_t> error_word;
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, ev0 = nullptr, ev1 = nullptr;
+    // completion events: one per wave, then one per megakernel job; job_done[j]
+    // indexes the event after which job j's image is final
+    std::vector<cudaEvent_t> done_ev;
+    std::vector<uint32_t> job_done;
     // the captured graph and what it was captured for
     cudaGraphExec_t exec = nullptr;
     std::string graph_key;
@@ -90,6 +94,8 @@ void batch_free(BatchState* b)
     for (cudaEvent_t e : {b->fork, b->join, b->ev0, b->ev1, b->wfork, b->wjoin, b->wacc[0], b->wacc[1]})
         if (e)
             cudaEventDestroy(e);
+    for (cudaEvent_t e : b->done_ev)
+        cudaEventDestroy(e);
     delete b;
 }
 
@@ -122,8 +128,9 @@ struct Plan {
 };
 
 // Packs the wavefront jobs' samples into waves of at most `capacity` paths.
-// Jobs with more pixels go first; a job joins a wave with as many whole
-// samples as the remaining capacity holds.
+// Jobs with less work (pixels x samples) go first, so small jobs finish in
+// the first waves; a job joins a wave with as many whole samples as the
+// remaining capacity holds.
 bool plan_batch(const std::vector<pt_render_params>& p, const BatchChoice& ch, Plan& plan, std::string& err)
 {
     plan = Plan{};
@@ -135,7 +142,7 @@ bool plan_batch(const std::vector<pt_render_params>& p, const BatchChoice& ch, P
             order.push_back(j);
     }
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
-        return (uint64_t)p[a].width * p[a].height > (uint64_t)p[b].width * p[b].height;
+        return (uint64_t)p[a].width * p[a].height * p[a].samples < (uint64_t)p[b].width * p[b].height * p[b].samples;
     });
     std::vector<uint32_t> done(p.size(), 0);
     size_t remaining = order.size();
@@ -266,6 +273,20 @@ int prepare(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vecto
     }
     if (e != cudaSuccess)
         return c->cuda_fail(e, "batch allocation");
+    // completion events (created before any capture), and each job's last one
+    const size_t need = plan.waves.size() + plan.mega.size();
+    while (b->done_ev.size() < need) {
+        cudaEvent_t ev;
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess)
+            return c->cuda_fail(e, "batch events");
+        b->done_ev.push_back(ev);
+    }
+    b->job_done.assign(p.size(), 0);
+    for (size_t w = 0; w < plan.waves.size(); w++)
+        for (uint32_t s = 0; s < plan.waves[w].share_count; s++)
+            b->job_done[plan.shares[plan.waves[w].share_offset + s].job] = (uint32_t)w;
+    for (size_t k = 0; k < plan.mega.size(); k++)
+        b->job_done[plan.mega[k]] = (uint32_t)(plan.waves.size() + k);
     e = cudaMemcpyAsync(b->jobs.p, args.data(), args.size() * sizeof(RenderArgs), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && !plan.shares.empty())
         e = cudaMemcpyAsync(b->shares.p, plan.shares.data(), plan.shares.size() * sizeof(WaveShare), cudaMemcpyHostToDevice,
@@ -313,6 +334,7 @@ cudaError_t issue(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std:
                     return e;
                 nl++;
             }
+            cudaEventRecord(b->done_ev[b->job_done[j]], b->side);
         }
     }
     if (!plan.waves.empty()) {
@@ -331,7 +353,7 @@ cudaError_t issue(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std:
         }
         e = launch_wavefront_batch(b->jobs.p, b->shares.p, plan.waves.data(), (uint32_t)plan.waves.size(), b->path_share.p,
                                    b->counters.p, b->state.p, b->state.n, b->state_paths, b->w4, c->sm_count, &wl, st,
-                                   two ? &wm : nullptr, two ? b->path_share2.p : nullptr);
+                                   two ? &wm : nullptr, two ? b->path_share2.p : nullptr, b->done_ev.data());
         if (e != cudaSuccess)
             return e;
         nl += wl;
@@ -613,6 +635,24 @@ int pt_render_batch(pt_ctx* c, const pt_batch_job* jobs, uint32_t count, uint32_
         return c->fail((ew & ERR_WATCHDOG) ? PT_ERR_TIMEOUT : PT_ERR_DEVICE,
                       std::string((ew & ERR_WATCHDOG) ? "traversal iteration cap hit" : "device error") + " (error word " +
                           std::to_string(ew) + ")");
+    return PT_OK;
+}
+
+int pt_batch_job_times(pt_ctx* c, float* ms, uint32_t count)
+{
+    if (!c || !ms)
+        return PT_ERR_INVALID;
+    BatchState* b = c->batch;
+    if (!b || b->job_done.empty())
+        return c->fail(PT_ERR_STATE, "no batch rendered");
+    if (count != b->job_done.size())
+        return c->fail(PT_ERR_INVALID, "count differs from the last batch's job count");
+    cudaSetDevice(c->device);
+    for (uint32_t j = 0; j < count; j++) {
+        cudaError_t e = cudaEventElapsedTime(&ms[j], b->ev0, b->done_ev[b->job_done[j]]);
+        if (e != cudaSuccess)
+            return c->cuda_fail(e, "batch job times");
+    }
     return PT_OK;
 }
 

@@ -87,7 +87,8 @@ cudaError_t wave_batch_prepare();
 cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shares, const BatchWave* waves, uint32_t wave_count,
                                    uint32_t* path_share, unsigned long long* counters, void* state, size_t state_bytes,
                                    uint32_t n_paths_max, bool w4, int sm_count, uint32_t* launches, cudaStream_t stream,
-                                   const WaveMulti* multi = nullptr, uint32_t* path_share2 = nullptr);
+                                   const WaveMulti* multi = nullptr, uint32_t* path_share2 = nullptr,
+                                   cudaEvent_t* wave_done = nullptr);
 cudaError_t features_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
 
 // Denoiser features and packing (features.cu).

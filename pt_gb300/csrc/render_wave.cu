@@ -927,7 +927,7 @@ cudaError_t launch_wavefront(const RenderArgs& r, void* state, size_t state_byte
 cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shares, const BatchWave* waves, uint32_t wave_count,
                                    uint32_t* path_share, unsigned long long* counters, void* state, size_t state_bytes,
                                    uint32_t n_paths_max, bool w4, int sm_count, uint32_t* launches, cudaStream_t st,
-                                   const WaveMulti* multi, uint32_t* path_share2)
+                                   const WaveMulti* multi, uint32_t* path_share2, cudaEvent_t* wave_done)
 {
     WaveArgs<ManyJobs> a[2];
     if (!carve_state(a[0].w, state, state_bytes, n_paths_max))
@@ -954,11 +954,14 @@ cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shar
         x.src.share_count = bw.share_count;
         x.src.n_paths = bw.n_paths;
         x.src.n_pixels = bw.n_pixels;
+        const cudaStream_t ws = (ways == 2 && (i & 1)) ? multi->stream[1] : st;
         if (ways == 2)
-            nl += launch_wave(x, w4, bw.max_bounces, bw.n_pixels, sm_count, (i & 1) ? multi->stream[1] : st, nullptr,
+            nl += launch_wave(x, w4, bw.max_bounces, bw.n_pixels, sm_count, ws, nullptr,
                               i ? multi->acc[(i - 1) & 1] : nullptr, multi->acc[i & 1]);
         else
-            nl += launch_wave(x, w4, bw.max_bounces, bw.n_pixels, sm_count, st);
+            nl += launch_wave(x, w4, bw.max_bounces, bw.n_pixels, sm_count, ws);
+        if (wave_done)
+            cudaEventRecord(wave_done[i], ws); // after the wave's accumulation, the last of its launches
     }
     if (ways == 2) {
         cudaEventRecord(multi->join[1], multi->stream[1]);
