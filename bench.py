@@ -63,7 +63,8 @@ REF_SPP = 4096
 DENOISE_SPP = (1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64)
 
 BSEG = {"mid": {"n_node": 27.2106, "n_tri": 9.0453, "p_nee": 0.2336},
-        "small": {"n_node": 13.7945, "n_tri": 6.0748, "p_nee": 0.5218}}
+        "small": {"n_node": 13.7945, "n_tri": 6.0748, "p_nee": 0.5218},
+        "heavy": {"n_node": 70.6501, "n_tri": 24.7050, "p_nee": 0.3352}}
 
 
 def bseg_bytes(m: dict) -> float | None:
@@ -491,6 +492,103 @@ def time_to_mse_heavy(device_index: int, ref_spp: int = HEAVY["ref_spp"]) -> dic
     return out
 
 
+CONFIG_WORKLOADS = {
+    "small": "small scene: 256x256, 16 spp, max 8 bounces, 8 icospheres + ground + lamp (~10k instanced tris), pinhole",
+    "heavy": "heavy scene: 1920x1080, 256 spp, max 12 bounces, Russian roulette from segment 4, ~2M unique tris in "
+             "64 BLASes, 10,000 instances, 256 emitters"}
+
+
+def config_leg(device_index: int, name: str, steps: int, cpu_seconds: float, no_cpu: bool) -> dict:
+    """Throughput of one more benchmark configuration, measured like the main
+    line: device time of `steps` renders (L2 flushed between them, stage
+    events for the dominant kernel's roofline), and the oracle on the host
+    cores over a bounded sample of the same render.
+
+      small  256x256, 16 spp, 8 bounces: 8 icospheres + ground + lamp (~10k tris)
+      heavy  1920x1080, 256 spp, 12 bounces, Russian roulette from segment 4:
+             ~2M unique tris in 64 BLASes, 10,000 instances, 256 emitters"""
+    import numpy as np
+    import torch
+    import oracle
+    import pt_gb300 as P
+    from oracle import scn_reader
+    from pt_gb300 import abi, scenes
+
+    if name == "small":
+        td = tempfile.TemporaryDirectory()
+        path = scenes.small_scene(Path(td.name) / "small", seed=0)
+        hs = P.HostScene.load(path)
+        raw_o, cam_o = scn_reader.read_scn(path)
+        W, H, S, B, RR = 256, 256, 16, 8, 1
+    else:
+        td = None
+        raw_o, cam_o = scenes.heavy_scene()
+        hs = P.HostScene.from_raw(raw_o, cam_o)
+        cam_o = {"position": cam_o["position"], "lookdir": cam_o["lookdir"], "up": (0.0, 1.0, 0.0),
+                 "fov_degrees": cam_o["fov_degrees"], "near_plane": 0.1, "far_plane": 1000.0, "focus_dist": 0.0,
+                 "lens_radius": 0.0, "exposure": 1.0}
+        W, H, S, B, RR = 1920, 1080, 256, 12, 4
+    ctx = P.Context(device_index)
+    ctx.upload(hs.pack())
+    info = ctx.build_accel()
+    p = hs.render_params(W, H, S, B, rr_start=RR)
+    st = ctx.render(p)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device_index}")
+    ms, stage, launches = [], [0.0] * 6, 0
+    p.flags = abi.PT_RENDER_TIME_STAGES
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s = ctx.render(p)
+        ms.append(s.milliseconds)
+        stage = [a + b for a, b in zip(stage, s.stage_ms)]
+        launches += s.stage_launches
+    t = sum(ms) / 1000.0
+    value = st.segments * steps / t / 1e6
+    peaks = measured_peaks()
+    ext_b = extend_bytes(BSEG[name])
+    ext_s = stage[1] / 1000.0
+    out = {"workload": CONFIG_WORKLOADS[name], "image": f"{W}x{H}", "spp": S, "max_bounces": B, "rr_start": RR, "value": value, "unit": "Mpath-segs/s",
+           "ms_per_step": 1000.0 * t / steps, "steps": steps, "segments_per_step": int(st.segments),
+           "accel_build_ms": info.build_ms,
+           "roofline": {"bound": "hbm", "kernel": "k_wf_extend", "bytes_per_ray": ext_b,
+                        "achieved": ext_b * st.segments * steps / ext_s / 1e9 if ext_s > 0 else None,
+                        "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                        "frac": ext_b * st.segments * steps / ext_s / 1e9 / peaks["hbm_gbs"] if ext_s > 0 else None,
+                        "avg_launch_ms": stage[1] / max(1, launches),
+                        "stage_ms_per_step": {k: v / steps for k, v in zip(abi.STAGES, stage)},
+                        "step": {"bytes_per_segment": bseg_bytes(BSEG[name]),
+                                 "frac": bseg_bytes(BSEG[name]) * st.segments / (t / steps) / 1e9 / peaks["hbm_gbs"]}}}
+    if not no_cpu:
+        rs, keep = scn_reader.raw_struct(raw_o)
+        packed = oracle.OraclePacked(rs)
+        osc = oracle.OracleScene(packed.view)
+        cd = scn_reader.camera_desc(cam_o)
+
+        def params(samples, first):
+            q = abi.RenderParams()
+            oracle.lib().or_camera_params(cd, W, H, q)
+            q.sample_index, q.samples, q.max_bounces, q.rr_start = first, samples, B, RR
+            return q
+
+        threads = os.cpu_count() or 1
+        segs, dt, n = 0, 0.0, 0
+        while n < S and (dt < cpu_seconds or n == 0):
+            t0 = time.perf_counter()
+            _, ost = osc.render(params(1, n), threads=threads)
+            dt += time.perf_counter() - t0
+            segs += ost.segments
+            n += 1
+        out["cpu_baseline"] = {"value": segs / dt / 1e6, "unit": "Mpath-segs/s", "cores": threads, "kind": "port",
+                               "sample": f"{name} {W}x{H}, samples 0-{n - 1} of {S} ({segs} segments, {dt:.1f} s)"
+                                         + (" = the whole render" if n == S else "")}
+        del osc, packed, keep
+    ctx.close()
+    if td is not None:
+        td.cleanup()
+    return out
+
+
 def batch_bench(device_index: int, jobs: int = 64, side=(128, 1024), spp=(4, 256), tris=(1000, 500000)) -> dict:
     """The batch workload (scenes.batch_workload: `jobs` jobs, own scene each,
     square side, samples and unique triangles log-uniform in the given
@@ -498,6 +596,7 @@ def batch_bench(device_index: int, jobs: int = 64, side=(128, 1024), spp=(4, 256
     for comparison, job after job with pt_render (wavefront).  The tuner's
     trials and the graph capture run in a first, untimed call; the timed
     batch is the graph launch of a second call (device time)."""
+    import numpy as np
     import pt_gb300 as P
     from pt_gb300 import scenes
 
@@ -515,11 +614,13 @@ def batch_bench(device_index: int, jobs: int = 64, side=(128, 1024), spp=(4, 256
         js.append((c, hs.render_params(j["side"], j["side"], j["spp"], j["max_bounces"])))
     first = ctx.render_batch(js)
     st = ctx.render_batch(js)
-    seq_ms, seq_segs = 0.0, 0
+    done = ctx.batch_job_times()
+    seq_ms, seq_segs, seq_done = 0.0, 0, []
     for c, p in js:
         s1 = c.render(p)
         seq_ms += s1.milliseconds
         seq_segs += s1.segments
+        seq_done.append(seq_ms)  # job after job in submission order: each job's latency
     out = {"jobs": jobs, "side": list(side), "spp": list(spp), "tris": list(tris),
            "paths": int(st.paths), "segments": int(st.segments),
            "batch_ms": st.milliseconds, "batch_mseg_s": st.segments / st.milliseconds / 1e3,
@@ -527,7 +628,12 @@ def batch_bench(device_index: int, jobs: int = 64, side=(128, 1024), spp=(4, 256
            "speedup_vs_sequential": seq_ms / st.milliseconds,
            "tune_ms": first.tune_milliseconds, "capture_ms": first.build_milliseconds, "graph_reused": int(st.graph_reused),
            "waves": st.waves, "graph_launches": st.kernel_launches, "wave_capacity": st.wave_capacity,
-           "mega_jobs": st.mega_jobs, "mega_threshold": int(st.mega_threshold), "tile_w": st.tile_w}
+           "mega_jobs": st.mega_jobs, "mega_threshold": int(st.mega_threshold), "tile_w": st.tile_w,
+           "job_latency_ms": {"batch_p50": float(np.percentile(done, 50)), "batch_p99": float(np.percentile(done, 99)),
+                              "sequential_p50": float(np.percentile(seq_done, 50)),
+                              "sequential_p99": float(np.percentile(seq_done, 99)),
+                              "note": "time from the start until each job's image is final; sequential = one pt_render "
+                                      "after another in submission order"}}
     for c, _ in js:
         c.close()
     ctx.close()
@@ -721,6 +827,10 @@ def run_ours(args) -> None:
                 ttm["held_out_seeds"] = time_to_mse_seeds(device_index, args.kernel, args.ref_spp)
             if not args.no_heavy:
                 ttm["heavy"] = time_to_mse_heavy(device_index, args.heavy_ref_spp)
+        configs = None
+        if not args.no_configs:
+            configs = {"small": config_leg(device_index, "small", 5, 5.0, args.no_cpu),
+                       "heavy": config_leg(device_index, "heavy", 2, 5.0, args.no_cpu)}
         batches = None
         if not args.no_batch:
             batches = {"uneven_64": batch_bench(device_index),
@@ -742,6 +852,7 @@ def run_ours(args) -> None:
                         "includes": "scene upload + BVH build + render + image read-back"},
                 "gpu_launches": int(launches_per_step * args.steps),
                 "roofline": roof, "cpu_baseline": base, "clocks": clocks.summary(), "time_to_mse": ttm, "batch": batches,
+                "configs": configs,
                 "wall_s_timed_region": wall}
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -763,6 +874,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mse", action="store_true", help="skip the time-to-MSE measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering measurement")
+    ap.add_argument("--no-configs", action="store_true", help="skip the small and heavy configuration lines")
     ap.add_argument("--ref-spp", type=int, default=REF_SPP)
     ap.add_argument("--no-seeds", action="store_true", help="skip time to MSE on held-out mid-scene seeds")
     ap.add_argument("--no-heavy", action="store_true", help="skip time to MSE on the heavy configuration")

@@ -22,3 +22,14 @@ def test_bseg_constants(tmp_path, name, fn, w, h):
     for k, v in got.items():
         assert abs(v - bench.BSEG[name][k]) < 1e-3, (k, v)
     assert 1500 < bench.bseg_bytes(bench.BSEG[name]) < 5000
+
+
+def test_bseg_constants_heavy():
+    """The heavy configuration: 1920x1080, first sample, 12 bounces, Russian
+    roulette from segment 4."""
+    raw, cam = scenes.heavy_scene()
+    hs = P.HostScene.from_raw(raw, cam)
+    _, st = oracle.OracleScene(hs.pack()).render(hs.render_params(1920, 1080, 1, 12, rr_start=4))
+    got = {"n_node": st.node_visits / st.ray_count, "n_tri": st.tri_tests / st.ray_count, "p_nee": st.shadow_rays / st.segments}
+    for k, v in got.items():
+        assert abs(v - bench.BSEG["heavy"][k]) < 1e-3, (k, v)
