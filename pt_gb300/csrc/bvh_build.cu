@@ -104,7 +104,8 @@ struct Scratch {
     uint32_t* a_flag;
     uint32_t* m_scan;
     uint32_t* a_scan;
-    uint32_t* counters; // [0] nodes emitted, [1] clusters after the round, [2] merges in the round
+    uint32_t* counters; // [0] nodes emitted, [1] live clusters, [2] merges in the last round,
+                        // [3] 1 once a round merged nothing, [4] buffer holding the clusters
     void* scan_temp;
     size_t scan_bytes;
     // leaf collapse of the BLAS trees
@@ -175,7 +176,7 @@ Scratch carve_scratch(void* base, uint32_t n, uint32_t nseg)
     s.a_flag = carve<uint32_t>(p, nn);
     s.m_scan = carve<uint32_t>(p, nn);
     s.a_scan = carve<uint32_t>(p, nn);
-    s.counters = carve<uint32_t>(p, 4);
+    s.counters = carve<uint32_t>(p, 8);
     s.cnt = carve<uint32_t>(p, nn);
     s.sah = carve<float>(p, nn);
     s.collapse = carve<uint32_t>(p, nn);
@@ -502,10 +503,14 @@ __device__ __forceinline__ bool pair_before(int i, int j, int k)
     return a0 < b0 || (a0 == b0 && a1 < b1);
 }
 
-__global__ void k_ploc_nn(const float4* lo, const float4* hi, const uint32_t* seg, int n, int radius, int* nn)
+// The round kernels read the live cluster count (counters[1]) and whether
+// the rounds are over (counters[3]) from device memory, so rounds run back to
+// back without the host; grids and scans cover `cap` >= live positions.
+__global__ void k_ploc_nn(const float4* lo, const float4* hi, const uint32_t* seg, const uint32_t* counters, int radius, int* nn)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n)
+    const int n = (int)counters[1];
+    if (counters[3] || i >= n)
         return;
     const float4 li = lo[i], hi_i = hi[i];
     const uint32_t si = seg[i];
@@ -524,22 +529,28 @@ __global__ void k_ploc_nn(const float4* lo, const float4* hi, const uint32_t* se
     nn[i] = bj;
 }
 
-// Mutual nearest neighbours merge; the lower index of a pair keeps the merged cluster.
-__global__ void k_ploc_flags(const int* nn, int n, uint32_t* m_flag, uint32_t* a_flag)
+// Mutual nearest neighbours merge; the lower index of a pair keeps the merged
+// cluster.  Positions past the live count get zero flags (the scans cover cap).
+__global__ void k_ploc_flags(const int* nn, const uint32_t* counters, int cap, uint32_t* m_flag, uint32_t* a_flag)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n)
+    if (i >= cap || counters[3])
         return;
+    if (i >= (int)counters[1]) {
+        m_flag[i] = 0u;
+        a_flag[i] = 0u;
+        return;
+    }
     const int j = nn[i];
     const bool mutual = j >= 0 && nn[j] == i;
     m_flag[i] = (mutual && i < j) ? 1u : 0u;
     a_flag[i] = (mutual && i > j) ? 0u : 1u;
 }
 
-__global__ void k_ploc_merge(Scratch s, int cur, int n, BvhNode* nodes, int node_base)
+__global__ void k_ploc_merge(Scratch s, int cur, BvhNode* nodes, int node_base)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !s.a_flag[i])
+    if (s.counters[3] || i >= (int)s.counters[1] || !s.a_flag[i])
         return;
     const int nxt = cur ^ 1;
     const uint32_t o = s.a_scan[i];
@@ -568,18 +579,27 @@ __global__ void k_ploc_merge(Scratch s, int cur, int n, BvhNode* nodes, int node
     s.c_seg[nxt][o] = s.c_seg[cur][i];
 }
 
-__global__ void k_ploc_count(Scratch s, int n)
+// End of a round: the clusters now sit in buffer `nxt`; a round without a
+// merge ends the rounds (every non-empty segment is one cluster).
+__global__ void k_ploc_count(Scratch s, int nxt)
 {
+    if (s.counters[3])
+        return;
+    const int n = (int)s.counters[1];
     const uint32_t merges = s.m_scan[n - 1] + s.m_flag[n - 1];
     s.counters[0] += merges;
     s.counters[1] = s.a_scan[n - 1] + s.a_flag[n - 1];
     s.counters[2] = merges;
+    s.counters[4] = (uint32_t)nxt;
+    if (merges == 0 || s.counters[1] <= 1)
+        s.counters[3] = 1u;
 }
 
-__global__ void k_ploc_roots(Scratch s, int cur, int n)
+__global__ void k_ploc_roots(Scratch s)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n)
+    const int cur = (int)s.counters[4];
+    if (i < (int)s.counters[1])
         s.seg_root[s.c_seg[cur][i]] = s.c_ref[cur][i];
 }
 
@@ -796,40 +816,49 @@ bool use_ploc_tlas()
     return v;
 }
 
-// PLOC rounds over the sorted primitives; ends when a round merges nothing
-// (then every non-empty segment is one cluster).
+// PLOC rounds over the sorted primitives; they end when a round merges
+// nothing (then every non-empty segment is one cluster).  The rounds run in
+// chunks of PLOC_CHUNK back to back on the device (a round after the end does
+// nothing); the host reads the counters once per chunk, not once per round.
+constexpr uint32_t PLOC_CHUNK = 8;
+
 cudaError_t build_ploc(Scratch& s, uint32_t n, BvhNode* nodes, int node_base, int mode_tlas, cudaStream_t st)
 {
     k_ploc_init<<<blocks(n, 256), 256, 0, st>>>(s, n, mode_tlas);
-    cudaMemsetAsync(s.counters, 0, 4 * sizeof(uint32_t), st);
+    cudaMemsetAsync(s.counters, 0, 8 * sizeof(uint32_t), st);
+    const uint32_t init[4] = {0u, n, 0u, n <= 1 ? 1u : 0u};
+    cudaError_t e = cudaMemcpyAsync(s.counters, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess)
+        return e;
     int cur = 0;
-    uint32_t live = n;
-    for (uint32_t round = 0; live > 1; round++) {
-        if (round > n)
+    uint32_t cap = n, rounds = 0;
+    uint32_t c[5] = {0u, n, 0u, n <= 1 ? 1u : 0u, 0u};
+    while (!c[3]) {
+        if (rounds > n + PLOC_CHUNK)
             return cudaErrorUnknown; // every round merges at least one pair while a segment has two clusters
-        k_ploc_nn<<<blocks(live, 128), 128, 0, st>>>(s.c_lo[cur], s.c_hi[cur], s.c_seg[cur], (int)live, ploc_radius(mode_tlas), s.nn);
-        k_ploc_flags<<<blocks(live, 256), 256, 0, st>>>(s.nn, (int)live, s.m_flag, s.a_flag);
-        size_t bytes = s.scan_bytes;
-        cudaError_t e = cub::DeviceScan::ExclusiveSum(s.scan_temp, bytes, s.m_flag, s.m_scan, (int)live, st);
-        if (e == cudaSuccess)
-            e = cub::DeviceScan::ExclusiveSum(s.scan_temp, bytes, s.a_flag, s.a_scan, (int)live, st);
-        if (e != cudaSuccess)
-            return e;
-        k_ploc_merge<<<blocks(live, 128), 128, 0, st>>>(s, cur, (int)live, nodes, node_base);
-        k_ploc_count<<<1, 1, 0, st>>>(s, (int)live);
-        uint32_t c[3];
-        e = cudaMemcpyAsync(c, s.counters, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        for (uint32_t k = 0; k < PLOC_CHUNK; k++, rounds++) {
+            k_ploc_nn<<<blocks(cap, 128), 128, 0, st>>>(s.c_lo[cur], s.c_hi[cur], s.c_seg[cur], s.counters,
+                                                          ploc_radius(mode_tlas), s.nn);
+            k_ploc_flags<<<blocks(cap, 256), 256, 0, st>>>(s.nn, s.counters, (int)cap, s.m_flag, s.a_flag);
+            size_t bytes = s.scan_bytes;
+            e = cub::DeviceScan::ExclusiveSum(s.scan_temp, bytes, s.m_flag, s.m_scan, (int)cap, st);
+            if (e == cudaSuccess)
+                e = cub::DeviceScan::ExclusiveSum(s.scan_temp, bytes, s.a_flag, s.a_scan, (int)cap, st);
+            if (e != cudaSuccess)
+                return e;
+            k_ploc_merge<<<blocks(cap, 128), 128, 0, st>>>(s, cur, nodes, node_base);
+            k_ploc_count<<<1, 1, 0, st>>>(s, cur ^ 1);
+            cur ^= 1;
+        }
+        e = cudaMemcpyAsync(c, s.counters, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(st);
         if (e != cudaSuccess)
             return e;
-        cur ^= 1;
-        live = c[1];
-        s.blas_nodes = c[0];
-        if (c[2] == 0)
-            break;
+        cap = c[1];
     }
-    k_ploc_roots<<<blocks(live, 128), 128, 0, st>>>(s, cur, (int)live);
+    s.blas_nodes = c[0];
+    k_ploc_roots<<<blocks(c[1], 128), 128, 0, st>>>(s);
     return cudaGetLastError();
 }
 

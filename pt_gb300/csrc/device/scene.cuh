@@ -298,8 +298,27 @@ __device__ __forceinline__ int node_children(const BvhNode* node, const ObjRay& 
     return (e0 <= x0 ? 1 : 0) | (e1 <= x1 ? 2 : 0);
 }
 
+// Three-input minimum / maximum (PTX min/max.f32 with three operands on
+// sm_100 and later): the same value as two nested fminf / fmaxf, NaN operands
+// ignored likewise.
+__device__ __forceinline__ float fmin3f(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmax3f(float a, float b, float c)
+{
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // Intersect the four child boxes of a 4-wide node; bit k of the result is
-// set when child k is hit, e[k] its entry distance.
+// set when child k is hit, e[k] its entry distance.  The far distance is
+// scaled once after the minimum over the axes instead of once per axis:
+// rounding is monotonic, so min(a s, b s, c s) = min(a, b, c) s for s > 0 and
+// the value equals the per-axis form of slab_enter bit for bit.
 __device__ __forceinline__ int node4_children(const Bvh4Node* node, const ObjRay& r, float tmin, float tmax, float (&e)[4], int (&c)[4])
 {
     const float4 lx = ldg4(&node->lox), hx = ldg4(&node->hix), ly = ldg4(&node->loy), hy = ldg4(&node->hiy);
@@ -312,12 +331,12 @@ __device__ __forceinline__ int node4_children(const Bvh4Node* node, const ObjRay
     int m = 0;
 #define PT_NODE4_CHILD(k, q)                                                                     \
     {                                                                                            \
-        float fx, fy, fz;                                                                        \
-        const float nx = slab_enter(lx.q, hx.q, r.inv_d.x, r.o_inv.x, fx);                       \
-        const float ny = slab_enter(ly.q, hy.q, r.inv_d.y, r.o_inv.y, fy);                       \
-        const float nz = slab_enter(lz.q, hz.q, r.inv_d.z, r.o_inv.z, fz);                       \
-        e[k] = fmaxf(fmaxf(fmaxf(nx, ny), nz), tmin);                                            \
-        const float x = fminf(fminf(fminf(fx, fy), fz), tmax);                                   \
+        const float x0 = fmaf(lx.q, r.inv_d.x, -r.o_inv.x), x1 = fmaf(hx.q, r.inv_d.x, -r.o_inv.x); \
+        const float y0 = fmaf(ly.q, r.inv_d.y, -r.o_inv.y), y1 = fmaf(hy.q, r.inv_d.y, -r.o_inv.y); \
+        const float z0 = fmaf(lz.q, r.inv_d.z, -r.o_inv.z), z1 = fmaf(hz.q, r.inv_d.z, -r.o_inv.z); \
+        e[k] = fmaxf(fmax3f(fminf(x0, x1), fminf(y0, y1), fminf(z0, z1)), tmin);                   \
+        const float far = fmin3f(fmaxf(x0, x1), fmaxf(y0, y1), fmaxf(z0, z1)) * SLAB_SCALE;      \
+        const float x = fminf(far, tmax);                                                        \
         m |= (e[k] <= x && l.q != REF_EMPTY) ? (1 << k) : 0;                                     \
     }
     PT_NODE4_CHILD(0, x)
@@ -594,6 +613,64 @@ __device__ __forceinline__ bool closest_step(const DevScene& s, ClosestTrace& t,
     return false;
 }
 
+// A closest-hit traversal paused after a step budget (its "parking"): what a
+// later pass needs to continue it exactly where it stopped.  The world ray is
+// rebuilt from the path state and the object-space ray from the instance, so
+// a slot holds the node reference, the stack, the instance, the step count and
+// the best hit so far; slots are SoA arrays of `cap` entries, the stack
+// word-major (stack[k * cap + slot]) so a warp's loads and stores coalesce.
+constexpr int PARK_STACK = 32; // deeper stacks finish in the first pass
+
+struct TraceParking {
+    uint32_t* path;  // the path of each slot
+    int4* state;     // ref, sp | in_blas << 16 | found << 17, cur_inst, iter
+    float4* hit;     // t, b1, b2, bits(inst)
+    uint32_t* prim;  // primitive of the best hit
+    int* stack;      // PARK_STACK words per slot, word-major
+    uint32_t cap;    // slots
+};
+
+__device__ __forceinline__ void park_closest(const TraceParking& pk, uint32_t slot, uint32_t path, const ClosestTrace& t,
+                                             const TraceStack& stack)
+{
+    pk.path[slot] = path;
+    pk.state[slot] = make_int4(t.ref, t.sp | (t.in_blas ? 1 << 16 : 0) | (t.found ? 1 << 17 : 0), (int)t.cur_inst, (int)t.iter);
+    pk.hit[slot] = make_float4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.inst));
+    pk.prim[slot] = t.h.prim;
+    for (int k = 0; k < t.sp; k++)
+        pk.stack[(size_t)k * pk.cap + slot] = stack[k];
+}
+
+// Restores a parked traversal of the ray (o, d, tmin): the same state the
+// first pass left, so closest_step continues the same sequence of steps.
+__device__ __forceinline__ void resume_closest(const DevScene& s, const TraceParking& pk, uint32_t slot, f3 o, f3 d, float tmin,
+                                               ClosestTrace& t, TraceStack& stack)
+{
+    const int4 st = pk.state[slot];
+    const float4 h = pk.hit[slot];
+    t.world.o = o;
+    t.world.d = d;
+    setup_slab(t.world);
+    t.tmin = tmin;
+    t.ref = st.x;
+    t.sp = st.y & 0xFFFF;
+    t.in_blas = (st.y >> 16) & 1;
+    t.found = (st.y >> 17) & 1;
+    t.cur_inst = (uint32_t)st.z;
+    t.iter = (uint32_t)st.w;
+    t.h.t = h.x;
+    t.h.b1 = h.y;
+    t.h.b2 = h.z;
+    t.h.inst = __float_as_uint(h.w);
+    t.h.prim = pk.prim[slot];
+    if (t.in_blas)
+        to_object(s.dinst + t.cur_inst, t.world.o, t.world.d, t.r);
+    else
+        t.r = t.world;
+    for (int k = 0; k < t.sp; k++)
+        stack[k] = pk.stack[(size_t)k * pk.cap + slot];
+}
+
 // Closest hit of one ray, traversed to the end.  Returns true on a hit.
 template <bool W4>
 static __device__ __forceinline__ bool trace_closest_inl(const DevScene& s, f3 o, f3 d, float tmin, float tmax, Hit& h, TraceCounters& tc)
@@ -742,7 +819,7 @@ struct ShadowTrace {
     ObjRay world, r;
     float tmin, tmax, throughput, alpha_pass;
     int ref, sp;
-    uint32_t iter, alpha_tex, alpha_inst;
+    uint32_t iter, alpha_tex, alpha_inst, inst;
     bool in_blas, opaque, alpha_map; // alpha_map: the transparent instance's alpha comes from a base colour map
 };
 
@@ -760,7 +837,7 @@ __device__ __forceinline__ void shadow_begin(const DevScene& s, f3 o, f3 d, floa
     t.in_blas = false;
     t.opaque = true;
     t.alpha_map = false;
-    t.alpha_tex = t.alpha_inst = 0;
+    t.alpha_tex = t.alpha_inst = t.inst = 0;
     t.alpha_pass = 1.0f;
     t.throughput = 1.0f;
     t.iter = 0;
@@ -806,6 +883,7 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
             return false;
         }
         const uint32_t flags = __ldg(&di->flags);
+        t.inst = first;
         t.opaque = (flags & 1u) != 0;
         if (!t.opaque) {
             const uint32_t mi = __ldg(&s.inst_data[first].material_index);
@@ -849,6 +927,52 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
         return true;
     t.ref = stack[--t.sp];
     return false;
+}
+
+// Parking of an any-hit (shadow) traversal in the slots of TraceParking:
+// state = ref, sp | in_blas << 16 | opaque << 17 | alpha_map << 18, the
+// instance being traversed, iter; hit = throughput, alpha_pass,
+// bits(alpha_tex), unused.  The instance's object-space ray is rebuilt on
+// resume from the world ray, as on entry.
+__device__ __forceinline__ void park_shadow(const TraceParking& pk, uint32_t slot, uint32_t path, const ShadowTrace& t,
+                                            const TraceStack& stack)
+{
+    pk.path[slot] = path;
+    pk.state[slot] = make_int4(t.ref,
+                               t.sp | (t.in_blas ? 1 << 16 : 0) | (t.opaque ? 1 << 17 : 0) | (t.alpha_map ? 1 << 18 : 0),
+                               (int)t.inst, (int)t.iter);
+    pk.hit[slot] = make_float4(t.throughput, t.alpha_pass, __uint_as_float(t.alpha_tex), 0.0f);
+    for (int k = 0; k < t.sp; k++)
+        pk.stack[(size_t)k * pk.cap + slot] = stack[k];
+}
+
+__device__ __forceinline__ void resume_shadow(const DevScene& s, const TraceParking& pk, uint32_t slot, f3 o, f3 d, float tmin,
+                                              float tmax, ShadowTrace& t, TraceStack& stack)
+{
+    const int4 st = pk.state[slot];
+    const float4 h = pk.hit[slot];
+    t.world.o = o;
+    t.world.d = d;
+    setup_slab(t.world);
+    t.tmin = tmin;
+    t.tmax = tmax;
+    t.ref = st.x;
+    t.sp = st.y & 0xFFFF;
+    t.in_blas = (st.y >> 16) & 1;
+    t.opaque = (st.y >> 17) & 1;
+    t.alpha_map = (st.y >> 18) & 1;
+    t.inst = (uint32_t)st.z;
+    t.alpha_inst = t.inst;
+    t.iter = (uint32_t)st.w;
+    t.throughput = h.x;
+    t.alpha_pass = h.y;
+    t.alpha_tex = __float_as_uint(h.z);
+    if (t.in_blas)
+        to_object(s.dinst + t.inst, t.world.o, t.world.d, t.r);
+    else
+        t.r = t.world;
+    for (int k = 0; k < t.sp; k++)
+        stack[k] = pk.stack[(size_t)k * pk.cap + slot];
 }
 
 template <bool W4>

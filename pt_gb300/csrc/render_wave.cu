@@ -135,7 +135,10 @@ struct WaveState {
     uint32_t* queue[2];
     uint32_t* shadow_queue;
     uint32_t* hit_queue; // paths whose ray hit something this segment (shade's input)
-    uint32_t* counts;   // [0],[1] path queues, [2] shadow queue, [3] work fetch, [4] shadow fetch, [5] hit queue
+    uint32_t* counts;   // [0],[1] path queues, [2] shadow queue, [3] work fetch, [4] shadow fetch, [5] hit queue,
+                        // [6] parked closest-hit traversals, [7] their fetch, [8] parked shadow
+                        // traversals, [9] their fetch
+    TraceParking park;  // closest-hit traversals paused by the first extend pass
 };
 
 template <class Src>
@@ -205,6 +208,10 @@ __global__ void __launch_bounds__(256) k_wf_raygen(WaveArgs<Src> a)
         a.w.counts[3] = 0;
         a.w.counts[4] = 0;
         a.w.counts[5] = 0;
+        a.w.counts[6] = 0;
+        a.w.counts[7] = 0;
+        a.w.counts[8] = 0;
+        a.w.counts[9] = 0;
     }
 }
 
@@ -228,8 +235,17 @@ enum Traversal : int { TRAV_BVH4 = 0, TRAV_BVH2 = 1, TRAV_BVH2_WW = 2 };
 
 // Persistent traversal: warps fetch 32 queue entries at a time.
 // Only traces: k_wf_split then separates hits from misses.
-template <class Src, int TRAV>
-__global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 7 : 1) k_wf_extend(WaveArgs<Src> a, uint32_t qi)
+//
+// With a step budget (4-wide nodes, budget > 0) this is the first of two
+// passes: a ray still traversing after `budget` steps is parked (its state
+// saved to a slot of a.w.park, slots taken by one atomic per warp) and the
+// lane moves on, so a warp's rays no longer wait for its slowest one;
+// k_wf_extend_resume finishes the parked rays 32 to a warp.  A ray whose stack
+// is deeper than PARK_STACK, or that finds no free slot, finishes here.  The
+// hit is the same either way: the resumed traversal continues the same
+// sequence of steps.
+template <class Src, int TRAV, bool BUDGET = false>
+__global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 7 : 1) k_wf_extend(WaveArgs<Src> a, uint32_t qi, uint32_t budget)
 {
     const uint32_t* queue = a.w.queue[qi];
     const uint32_t count = *(volatile uint32_t*)&a.w.counts[qi];
@@ -251,7 +267,45 @@ __global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 7 : 1) k_wf_extend(Wa
             p = queue[i];
             PT_CHECK_ENTRY(ok, p, a)
         }
-        if (ok) {
+        if (TRAV == TRAV_BVH4 && BUDGET) {
+            // one warp-uniform loop (a single copy of the step code): at
+            // iteration `budget` the lanes still traversing park together
+            ClosestTrace t;
+            TraceStack stack;
+            const uint32_t job = ok ? a.src.job_of(p) : 0u;
+            bool live = ok;
+            if (ok) {
+                const float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
+                closest_begin(a.src.args(job).s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, d.w, t, stack);
+            }
+            for (uint32_t k = 0;; k++) {
+                if (k == budget) {
+                    const bool park = live && t.sp <= PARK_STACK;
+                    const unsigned want = __ballot_sync(0xffffffffu, park);
+                    if (want) {
+                        uint32_t slot0 = 0;
+                        const int leader = __ffs(want) - 1;
+                        if ((int)lane == leader)
+                            slot0 = atomicAdd(&a.w.counts[6], (uint32_t)__popc(want));
+                        slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+                        const uint32_t slot = slot0 + __popc(want & ((1u << lane) - 1u));
+                        if (park && slot < a.w.park.cap) {
+                            park_closest(a.w.park, slot, p, t, stack);
+                            live = false;
+                        }
+                    }
+                }
+                if (!__any_sync(0xffffffffu, live))
+                    break;
+                if (live && closest_step<true>(a.src.args(job).s, t, stack, tc)) {
+                    a.w.hit[p] = make_float4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.inst));
+                    a.w.hit_prim[p] = t.found ? t.h.prim : 0xFFFFFFFFu;
+                    live = false;
+                }
+            }
+            continue;
+        }
+        if (!BUDGET && ok) {
             const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
             Hit h;
@@ -265,6 +319,46 @@ __global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 7 : 1) k_wf_extend(Wa
     }
     uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
     uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
+    if (lane == 0) {
+        atomicAdd(a.src.counters() + 3, (unsigned long long)nodes);
+        atomicAdd(a.src.counters() + 4, (unsigned long long)tris);
+    }
+}
+
+// Second extend pass: finishes the traversals the first pass parked, 32 to a
+// warp (persistent warps over the parked slots).
+template <class Src>
+__global__ void __launch_bounds__(128, 7) k_wf_extend_resume(WaveArgs<Src> a)
+{
+    const uint32_t parked = *(volatile uint32_t*)&a.w.counts[6];
+    const uint32_t count = parked < a.w.park.cap ? parked : a.w.park.cap;
+    const unsigned lane = threadIdx.x & 31;
+    TraceCounters tc{0u, 0u};
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0)
+            base = atomicAdd(&a.w.counts[7], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count)
+            break;
+        const uint32_t slot = base + lane;
+        bool ok = slot < count;
+        uint32_t p = ok ? a.w.park.path[slot] : 0u;
+        PT_CHECK_ENTRY(ok, p, a)
+        if (ok) {
+            const DevScene& s = a.src.args(a.src.job_of(p)).s;
+            const float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
+            ClosestTrace t;
+            TraceStack stack;
+            resume_closest(s, a.w.park, slot, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), o.w, t, stack);
+            while (!closest_step<true>(s, t, stack, tc)) {
+            }
+            a.w.hit[p] = make_float4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.inst));
+            a.w.hit_prim[p] = t.found ? t.h.prim : 0xFFFFFFFFu;
+        }
+    }
+    const uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
+    const uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
     if (lane == 0) {
         atomicAdd(a.src.counters() + 3, (unsigned long long)nodes);
         atomicAdd(a.src.counters() + 4, (unsigned long long)tris);
@@ -548,8 +642,31 @@ __global__ void __launch_bounds__(128) k_wf_shadow_refill(WaveArgs<Src> a, uint3
     }
 }
 
-template <class Src, bool W4>
-__global__ void __launch_bounds__(128, W4 ? 7 : 1) k_wf_shadow(WaveArgs<Src> a)
+// Completes the NEE term of path p with the shadow ray's visibility.
+template <class Src>
+__device__ __forceinline__ void shadow_finish(const WaveArgs<Src>& a, uint32_t p, float vis)
+{
+    NeeRequest nee;
+    nee.add = true;
+    nee.trace = true;
+    const float4 e = a.w.nee_e[p], b = a.w.nee_b[p], t = a.w.nee_tp[p];
+    nee.emission = mk3(e.x, e.y, e.z);
+    nee.cos_i = e.w;
+    nee.brdf = mk3(b.x, b.y, b.z);
+    nee.pdf = b.w;
+    nee.w = a.w.nee_d[p].w;
+    nee.tp_before = mk3(t.x, t.y, t.z);
+    const float4 r4 = a.w.rad[p];
+    f3 rad = mk3(r4.x, r4.y, r4.z);
+    finish_nee(rad, nee, vis);
+    a.w.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+}
+
+// Persistent shadow (any-hit) traversal.  With BUDGET (4-wide nodes) the
+// first of two passes, as k_wf_extend: rays still traversing after `budget`
+// steps park (counters [8]/[9]) and k_wf_shadow_resume finishes them.
+template <class Src, bool W4, bool BUDGET = false>
+__global__ void __launch_bounds__(128, W4 ? 7 : 1) k_wf_shadow(WaveArgs<Src> a, uint32_t budget)
 {
     const uint32_t count = a.w.counts[2];
     unsigned lane = threadIdx.x & 31;
@@ -565,28 +682,88 @@ __global__ void __launch_bounds__(128, W4 ? 7 : 1) k_wf_shadow(WaveArgs<Src> a)
         bool ok = i < count;
         uint32_t p = ok ? a.w.shadow_queue[i] : 0u;
         PT_CHECK_ENTRY(ok, p, a)
+        if (W4 && BUDGET) {
+            ShadowTrace t;
+            TraceStack stack;
+            const uint32_t job = ok ? a.src.job_of(p) : 0u;
+            bool live = ok;
+            if (ok) {
+                const float4 o = a.w.nee_o[p], d = a.w.nee_d[p];
+                shadow_begin(a.src.args(job).s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, o.w, t, stack);
+            }
+            for (uint32_t k = 0;; k++) {
+                if (k == budget) {
+                    const bool park = live && t.sp <= PARK_STACK;
+                    const unsigned want = __ballot_sync(0xffffffffu, park);
+                    if (want) {
+                        uint32_t slot0 = 0;
+                        const int leader = __ffs(want) - 1;
+                        if ((int)lane == leader)
+                            slot0 = atomicAdd(&a.w.counts[8], (uint32_t)__popc(want));
+                        slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+                        const uint32_t slot = slot0 + __popc(want & ((1u << lane) - 1u));
+                        if (park && slot < a.w.park.cap) {
+                            park_shadow(a.w.park, slot, p, t, stack);
+                            live = false;
+                        }
+                    }
+                }
+                if (!__any_sync(0xffffffffu, live))
+                    break;
+                if (live && shadow_step<true>(a.src.args(job).s, t, stack, tc)) {
+                    shadow_finish(a, p, shadow_result(t));
+                    live = false;
+                }
+            }
+            continue;
+        }
         if (ok) {
             const DevScene& s = a.src.args(a.src.job_of(p)).s;
             float4 o = a.w.nee_o[p], d = a.w.nee_d[p];
             float vis = trace_shadow_inl<W4>(s, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, o.w, tc);
-            NeeRequest nee;
-            nee.add = true;
-            nee.trace = true;
-            float4 e = a.w.nee_e[p], b = a.w.nee_b[p], t = a.w.nee_tp[p];
-            nee.emission = mk3(e.x, e.y, e.z);
-            nee.cos_i = e.w;
-            nee.brdf = mk3(b.x, b.y, b.z);
-            nee.pdf = b.w;
-            nee.w = d.w;
-            nee.tp_before = mk3(t.x, t.y, t.z);
-            float4 r4 = a.w.rad[p];
-            f3 rad = mk3(r4.x, r4.y, r4.z);
-            finish_nee(rad, nee, vis);
-            a.w.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+            shadow_finish(a, p, vis);
         }
     }
     uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
     uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
+    if (lane == 0) {
+        atomicAdd(a.src.counters() + 3, (unsigned long long)nodes);
+        atomicAdd(a.src.counters() + 4, (unsigned long long)tris);
+    }
+}
+
+// Second shadow pass: finishes the shadow traversals the first pass parked.
+template <class Src>
+__global__ void __launch_bounds__(128, 7) k_wf_shadow_resume(WaveArgs<Src> a)
+{
+    const uint32_t parked = *(volatile uint32_t*)&a.w.counts[8];
+    const uint32_t count = parked < a.w.park.cap ? parked : a.w.park.cap;
+    const unsigned lane = threadIdx.x & 31;
+    TraceCounters tc{0u, 0u};
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0)
+            base = atomicAdd(&a.w.counts[9], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count)
+            break;
+        const uint32_t slot = base + lane;
+        bool ok = slot < count;
+        uint32_t p = ok ? a.w.park.path[slot] : 0u;
+        PT_CHECK_ENTRY(ok, p, a)
+        if (ok) {
+            const DevScene& s = a.src.args(a.src.job_of(p)).s;
+            const float4 o = a.w.nee_o[p], d = a.w.nee_d[p];
+            ShadowTrace t;
+            TraceStack stack;
+            resume_shadow(s, a.w.park, slot, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), 0.0f, o.w, t, stack);
+            while (!shadow_step<true>(s, t, stack, tc)) {
+            }
+            shadow_finish(a, p, shadow_result(t));
+        }
+    }
+    const uint32_t nodes = __reduce_add_sync(0xffffffffu, tc.nodes);
+    const uint32_t tris = __reduce_add_sync(0xffffffffu, tc.tris);
     if (lane == 0) {
         atomicAdd(a.src.counters() + 3, (unsigned long long)nodes);
         atomicAdd(a.src.counters() + 4, (unsigned long long)tris);
@@ -601,6 +778,10 @@ __global__ void k_wf_reset(uint32_t* counts, uint32_t qi)
     counts[3] = 0;
     counts[4] = 0;
     counts[5] = 0;  // hit queue consumed by shade
+    counts[6] = 0;  // parked traversals finished
+    counts[7] = 0;
+    counts[8] = 0;
+    counts[9] = 0;
 }
 
 template <class Src>
@@ -656,9 +837,13 @@ __global__ void __launch_bounds__(256) k_wf_accumulate(WaveArgs<Src> a)
         atomicAdd(a.src.counters() + 2, (unsigned long long)a.src.n_paths);
 }
 
+// Parking slots for a quarter of a wave's paths (a multiple of 32).
+static inline size_t park_slots(size_t n_paths) { return ((n_paths / 4) + 31) / 32 * 32; }
+
 size_t wave_state_bytes(uint32_t n_paths)
 {
-    return (size_t)n_paths * (16 * 13 + 4 * 6) + 4096;
+    const size_t park = park_slots(n_paths) * (4 + 16 + 16 + 4 + 4 * (size_t)PARK_STACK);
+    return (size_t)n_paths * (16 * 13 + 4 * 6) + park + 8192;
 }
 
 static inline char* bump(char*& p, size_t bytes)
@@ -693,6 +878,13 @@ static bool carve_state(WaveState& w, void* state, size_t state_bytes, size_t n)
     w.shadow_queue = (uint32_t*)bump(p, 4 * n);
     w.hit_queue = (uint32_t*)bump(p, 4 * n);
     w.counts = (uint32_t*)bump(p, 64);
+    const size_t slots = park_slots(n);
+    w.park.cap = (uint32_t)slots;
+    w.park.path = (uint32_t*)bump(p, 4 * slots);
+    w.park.state = (int4*)bump(p, 16 * slots);
+    w.park.hit = (float4*)bump(p, 16 * slots);
+    w.park.prim = (uint32_t*)bump(p, 4 * slots);
+    w.park.stack = (int*)bump(p, 4 * (size_t)PARK_STACK * slots);
     return (size_t)(p - (char*)state) <= state_bytes;
 }
 
@@ -717,6 +909,8 @@ struct StageVariant {
     bool ww = false;
     int shade = 6;       // resident-block target of shade (0: none)
     uint32_t refill = 0; // 0: no refill; else 1..32
+    uint32_t budget = 48; // extend's first-pass step budget over 4-wide nodes (PT_EXTEND_BUDGET; 0: one pass)
+    uint32_t shadow_budget = 48; // the same for shadow rays (PT_SHADOW_BUDGET)
 };
 
 static StageVariant stage_variant()
@@ -732,6 +926,14 @@ static StageVariant stage_variant()
         if (const char* f = std::getenv("PT_REFILL")) {
             const int k = std::atoi(f);
             r.refill = k <= 0 ? 0u : (uint32_t)std::min(k, 32);
+        }
+        if (const char* b = std::getenv("PT_EXTEND_BUDGET")) {
+            const int k = std::atoi(b);
+            r.budget = k <= 0 ? 0u : (uint32_t)std::min(k, 1 << 20);
+        }
+        if (const char* b = std::getenv("PT_SHADOW_BUDGET")) {
+            const int k = std::atoi(b);
+            r.shadow_budget = k <= 0 ? 0u : (uint32_t)std::min(k, 1 << 20);
         }
         return r;
     }();
@@ -833,12 +1035,18 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, bool w4, uint32_t max_bounce
             k_wf_extend_refill<Src, true><<<trace_blocks, 128, 0, st>>>(a, qi, sv.refill);
         else if (refill)
             k_wf_extend_refill<Src, false><<<trace_blocks, 128, 0, st>>>(a, qi, sv.refill);
-        else if (trav == TRAV_BVH4)
-            k_wf_extend<Src, TRAV_BVH4><<<trace_blocks, 128, 0, st>>>(a, qi);
-        else if (trav == TRAV_BVH2_WW)
-            k_wf_extend<Src, TRAV_BVH2_WW><<<trace_blocks, 128, 0, st>>>(a, qi);
+        else if (trav == TRAV_BVH4) {
+            if (sv.budget) {
+                k_wf_extend<Src, TRAV_BVH4, true><<<trace_blocks, 128, 0, st>>>(a, qi, sv.budget);
+                k_wf_extend_resume<Src><<<trace_blocks, 128, 0, st>>>(a);
+                nl++;
+            } else {
+                k_wf_extend<Src, TRAV_BVH4><<<trace_blocks, 128, 0, st>>>(a, qi, 0u);
+            }
+        } else if (trav == TRAV_BVH2_WW)
+            k_wf_extend<Src, TRAV_BVH2_WW><<<trace_blocks, 128, 0, st>>>(a, qi, 0u);
         else
-            k_wf_extend<Src, TRAV_BVH2><<<trace_blocks, 128, 0, st>>>(a, qi);
+            k_wf_extend<Src, TRAV_BVH2><<<trace_blocks, 128, 0, st>>>(a, qi, 0u);
         mark(2);
         k_wf_split<Src><<<capped_grid(a.src.n_paths, 256, sm_count), 256, 0, st>>>(a, qi);
         if (sv.shade == 5)
@@ -852,10 +1060,14 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, bool w4, uint32_t max_bounce
             k_wf_shadow_refill<Src, true><<<shadow_blocks, 128, 0, st>>>(a, sv.refill);
         else if (refill)
             k_wf_shadow_refill<Src, false><<<shadow_blocks, 128, 0, st>>>(a, sv.refill);
-        else if (w4)
-            k_wf_shadow<Src, true><<<shadow_blocks, 128, 0, st>>>(a);
+        else if (w4 && sv.shadow_budget) {
+            k_wf_shadow<Src, true, true><<<shadow_blocks, 128, 0, st>>>(a, sv.shadow_budget);
+            k_wf_shadow_resume<Src><<<shadow_blocks, 128, 0, st>>>(a);
+            nl++;
+        } else if (w4)
+            k_wf_shadow<Src, true><<<shadow_blocks, 128, 0, st>>>(a, 0u);
         else
-            k_wf_shadow<Src, false><<<shadow_blocks, 128, 0, st>>>(a);
+            k_wf_shadow<Src, false><<<shadow_blocks, 128, 0, st>>>(a, 0u);
         mark(4);
         k_wf_reset<<<1, 1, 0, st>>>(a.w.counts, qi);
         nl += 5;
