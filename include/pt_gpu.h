@@ -345,7 +345,7 @@ int pt_mse_noalloc(const float* image_rgba, const float* reference_rgba, uint32_
  * megakernel launches on a parallel branch of the same graph.  Jobs with less
  * work go into the first waves, so small jobs finish early.  An autotuner
  * times short trial batches (every job at 1/32 of its samples, at least one)
- * and picks the wave capacity (2^21, 2^23 or 2^25 paths in flight, within a
+ * and picks the wave capacity (2^21, 2^23, 2^25 or 2^26 paths in flight, within a
  * quarter of the free device memory), the megakernel tile and the
  * work size below which a job runs on the megakernel; its choice is cached
  * per batch.  Every job's image equals, bit for bit, rendering that job alone

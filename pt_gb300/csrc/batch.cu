@@ -12,7 +12,7 @@
 //
 // The autotuner times trial batches (each job at 1/32 of its samples, at
 // least 1) for a few candidate settings and keeps the fastest, per batch:
-//   1. wave capacity 2^21, 2^23, 2^25 paths (all jobs on the wavefront);
+//   1. wave capacity 2^21, 2^23, 2^25, 2^26 paths (all jobs on the wavefront);
 //   2. megakernel threshold 0, 2^18, 2^21 on a job's trial work, pixels x
 //      trial samples x (bounces + 1) (tile 16x8);
 //   3. if a threshold won: megakernel tile 8x16 or 32x4 against 16x8.
@@ -423,7 +423,7 @@ int tune(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vector<p
         return PT_OK;
     };
     int rc;
-    for (uint32_t lg : {21u, 23u, 25u}) {
+    for (uint32_t lg : {21u, 23u, 25u, 26u}) {
         BatchChoice ch;
         ch.capacity = fixed_capacity ? fixed_capacity : 1u << lg;
         if ((rc = consider(ch)) != PT_OK)

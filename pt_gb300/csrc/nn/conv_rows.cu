@@ -12,8 +12,9 @@
 //
 // Warp roles: warp 0 produces (TMA), warp 1 allocates TMEM and issues the
 // MMAs, warps 2-5 drain the accumulators (bias, ReLU, gradient mask, store).
-// CTAs are persistent over tiles; two CTAs share an SM, so one CTA's epilogue
-// overlaps the other's loads and MMAs.
+// One persistent CTA per SM with as many pipeline stages as shared memory
+// holds; the accumulators are double-buffered in TMEM (2 x MT x N columns),
+// so the MMAs of the next tile run while the epilogue drains this one.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -43,7 +44,7 @@ struct RowsParams {
     int mask_pitch, mask_c0;
     int n, h, w, tiles_x, tiles_y, tiles;
     int stages;
-    uint32_t tmem_cols;
+    uint32_t tmem_cols; // one accumulator buffer; the CTA allocates two
     uint32_t* error;
 };
 
@@ -77,9 +78,9 @@ __global__ void __launch_bounds__(192) k_conv3x3_rows(const __grid_constant__ CU
     const int S = p.stages;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)S * stage_bytes);
     uint64_t* empty = full + S;
-    uint64_t* acc_full = empty + S;
-    uint64_t* acc_empty = acc_full + 1;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(acc_empty + 1);
+    uint64_t* acc_full = empty + S;     // [2]: buffer b holds a finished tile
+    uint64_t* acc_empty = acc_full + 2; // [2]: buffer b was drained
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(acc_empty + 2);
     volatile uint32_t* fail = tslot + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int chunks = p.cin / KC;
@@ -89,13 +90,15 @@ __global__ void __launch_bounds__(192) k_conv3x3_rows(const __grid_constant__ CU
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(acc_full, 1);
-        mbar_init(acc_empty, 4);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);
+        }
         *fail = 0;
         mbar_init_fence();
     }
     if (warp == 1) {
-        tmem_alloc(tslot, p.tmem_cols);
+        tmem_alloc(tslot, 2 * p.tmem_cols);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -133,12 +136,14 @@ __global__ void __launch_bounds__(192) k_conv3x3_rows(const __grid_constant__ CU
             const uint32_t b_lbo = (uint32_t)p.nout * 16;
             uint32_t it = 0, tc = 0;
             for (int t = blockIdx.x; t < p.tiles && !failed(fail); t += gridDim.x, tc++) {
-                // the epilogue of the previous tile must have drained TMEM
-                if (tc > 0 && !mbar_wait(acc_empty, (tc - 1) & 1u)) {
+                // buffer b's previous tile (two tiles back) must have been drained
+                const uint32_t b = tc & 1u, use = tc >> 1;
+                if (use > 0 && !mbar_wait(&acc_empty[b], (use - 1) & 1u)) {
                     atomicOr((uint32_t*)fail, 1u);
                     break;
                 }
                 tc_fence_after();
+                const uint32_t acc = tmem + b * p.tmem_cols;
                 for (int c = 0; c < chunks; c++, it++) {
                     const uint32_t s = it % S;
                     if (!mbar_wait(&full[s], (it / S) & 1u)) {
@@ -154,12 +159,12 @@ __global__ void __launch_bounds__(192) k_conv3x3_rows(const __grid_constant__ CU
                             const uint32_t a_off = (uint32_t)((r + ky) * HALO_W + kx) * 16u;
                             const uint64_t ad = smem_desc(sa + a_off, a_box, 128u);
                             const uint64_t bd = smem_desc(sb + (uint32_t)tap * b_tap, b_lbo, 128u);
-                            mma_bf16(tmem + (uint32_t)(r * p.nout), ad, bd, idesc, (c | tap) != 0);
+                            mma_bf16(acc + (uint32_t)(r * p.nout), ad, bd, idesc, (c | tap) != 0);
                         }
                     }
                     mma_commit(&empty[s]);
                 }
-                mma_commit(acc_full);
+                mma_commit(&acc_full[b]);
             }
         }
     } else {
@@ -168,7 +173,8 @@ __global__ void __launch_bounds__(192) k_conv3x3_rows(const __grid_constant__ CU
         const int m = quarter * 32 + lane;
         uint32_t tc = 0;
         for (int t = blockIdx.x; t < p.tiles; t += gridDim.x, tc++) {
-            const bool ok = !failed(fail) && mbar_wait(acc_full, tc & 1u);
+            const uint32_t b = tc & 1u, use = tc >> 1;
+            const bool ok = !failed(fail) && mbar_wait(&acc_full[b], use & 1u);
             // warp-uniform decision before the warp-collective TMEM loads
             if (__any_sync(0xffffffffu, !ok)) {
                 if (lane == 0)
@@ -188,7 +194,7 @@ __global__ void __launch_bounds__(192) k_conv3x3_rows(const __grid_constant__ CU
                 const size_t pix = ((size_t)img * p.h + py) * p.w + px;
                 for (int j = 0; j < p.nout / 16; j++) {
                     uint32_t v32[16];
-                    tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(r * p.nout + j * 16), v32);
+                    tmem_ld16(tmem + b * p.tmem_cols + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(r * p.nout + j * 16), v32);
                     if (!valid)
                         continue;
                     float v[16];
@@ -234,14 +240,14 @@ __global__ void __launch_bounds__(192) k_conv3x3_rows(const __grid_constant__ CU
             tc_fence_before();
             __syncwarp();
             if (lane == 0)
-                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(acc_empty)) : "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&acc_empty[b])) : "memory");
         }
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, p.tmem_cols);
+        tmem_dealloc(tmem, 2 * p.tmem_cols);
     }
     if (threadIdx.x == 0 && *fail)
         atomicOr(p.error, 1u);
@@ -333,33 +339,26 @@ cudaError_t conv3x3_rows(const ConvCall& c, const CUtensorMap* halo_map, int sm_
         return cudaSuccess;
     const size_t a_box = ((size_t)(p.mt + 2) * HALO_W * 16 + 127) & ~(size_t)127;
     const size_t stage = 2 * a_box + (size_t)9 * p.nout * 32;
-    const size_t extra = 8 * (2 * 4 + 2) + 64;
-    const size_t two_per_sm = 113 * 1024; // leaves room for a second CTA on the SM
-    int S = 4;
-    while (S > 2 && S * stage + extra > two_per_sm)
+    const size_t extra = 8 * (2 * 8 + 4) + 64;
+    const size_t smem_max = 232448; // one CTA per SM: all of its shared memory
+    int S = 8;
+    while (S > 2 && S * stage + extra > smem_max)
         S--;
-    if (S * stage + extra > 232448)
+    if (S * stage + extra > smem_max || 2 * p.tmem_cols > 512)
         return cudaErrorInvalidValue;
     p.stages = S;
-    size_t smem = S * stage + extra;
-    // at most 512 / tmem_cols CTAs per SM so every TMEM allocation fits
-    const size_t per_sm = 233472;
-    const size_t max_ctas = 512 / p.tmem_cols;
-    smem = std::max(smem, per_sm / (max_ctas + 1) + 1 - 1024);
-    smem = std::min<size_t>(smem, 232448);
+    const size_t smem = S * stage + extra;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(k_conv3x3_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
-        if (e == cudaSuccess) // all of L1 as shared memory, so two CTAs fit on an SM
+        if (e == cudaSuccess) // all of L1 as shared memory
             e = cudaFuncSetAttribute(k_conv3x3_rows, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if (e != cudaSuccess)
             return e;
         attr = true;
     }
-    int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv3x3_rows, 192, smem);
-    per = std::max(1, std::min<int>(per, (int)max_ctas));
-    const int grid = std::min(p.tiles, sm_count * per);
+    // one CTA per SM (its two accumulator buffers may take all 512 TMEM columns)
+    const int grid = std::min(p.tiles, sm_count);
     k_conv3x3_rows<<<grid, 192, smem, st>>>(*halo_map, p);
     return cudaGetLastError();
 }

@@ -1,6 +1,8 @@
 """pt_render_batch: many jobs (own scene, camera, size, samples, bounces) in
 one launch sequence.  Every job's image must equal rendering that job alone,
 bit for bit, whatever the wave packing, the tuner's choice or the graph."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -176,3 +178,18 @@ def test_invalid_batches(batch):
         ctx.render_batch([(fresh, p)])
     assert e.value.status == abi.PT_ERR_STATE
     fresh.close()
+
+
+def test_batch_job_times(batch):
+    """pt_batch_job_times: each job's completion time of the last batch, within
+    the batch's device time; waves take the least work first, so the smallest
+    job is final no later than the largest."""
+    ctx, jobs, _ = batch
+    st = ctx.render_batch(jobs, abi.PT_BATCH_NO_TUNE | abi.PT_BATCH_CAPACITY_LOG2(11))
+    t = ctx.batch_job_times()
+    assert t.shape == (len(jobs),) and (t > 0).all() and (t <= st.milliseconds * 1.01 + 0.05).all()
+    work = [w * h * s for _, _, w, h, s, _ in SPECS]
+    assert t[int(np.argmin(work))] <= t[int(np.argmax(work))]
+    out = np.zeros(len(jobs) - 1, np.float32)
+    rc = abi.lib().pt_batch_job_times(ctx._h, out.ctypes.data_as(C.POINTER(C.c_float)), len(jobs) - 1)
+    assert rc == abi.PT_ERR_INVALID  # the count must be the last batch's

@@ -366,12 +366,18 @@ np.save(sys.argv[3], ctx.read_image(fp64=True))
 
 @pytest.mark.parametrize("env", [{"PT_WAVE_STREAMS": "1"}, {"PT_WAVE_STREAMS": "3"}, {"PT_BVH_WIDTH": "2"},
                                  {"PT_REFILL": "16"}, {"PT_BVH_WIDTH": "2", "PT_TRAVERSAL": "ww"},
-                                 {"PT_WAVE_PATHS_LOG2": "20"}],
-                         ids=["one_stream", "three_streams", "bvh2", "refill", "bvh2_while_while", "small_waves"])
+                                 {"PT_WAVE_PATHS_LOG2": "20"},
+                                 {"PT_EXTEND_BUDGET": "0", "PT_SHADOW_BUDGET": "0"},
+                                 {"PT_EXTEND_BUDGET": "2", "PT_SHADOW_BUDGET": "2"}],
+                         ids=["one_stream", "three_streams", "bvh2", "refill", "bvh2_while_while", "small_waves",
+                              "one_pass_traversal", "budget_2_slots_overflow"])
 def test_execution_variants_agree(ctx, mid, tmp_path, env):
     """Every execution variant (sub-wave streams, node width, traversal
-    order, lane refill, wave size; each read once per process, so set in a
-    child) renders the same image and FP64 sums bit for bit as the default."""
+    order, lane refill, wave size, the traversal step budget: one pass, or a
+    budget of 2 steps that parks nearly every ray and overflows the parking
+    slots, a quarter of a wave, so the rest finish in the first pass; each
+    read once per process, so set in a child) renders the same image and FP64
+    sums bit for bit as the default."""
     import os
     import subprocess
     import sys
