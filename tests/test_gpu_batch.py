@@ -185,7 +185,8 @@ def test_batch_job_times(batch):
     the batch's device time; waves take the least work first, so the smallest
     job is final no later than the largest."""
     ctx, jobs, _ = batch
-    st = ctx.render_batch(jobs, abi.PT_BATCH_NO_TUNE | abi.PT_BATCH_CAPACITY_LOG2(11))
+    st = ctx.render_batch(jobs, abi.PT_BATCH_NO_TUNE | abi.PT_BATCH_CAPACITY_LOG2(13))
+    assert st.waves > 1
     t = ctx.batch_job_times()
     assert t.shape == (len(jobs),) and (t > 0).all() and (t <= st.milliseconds * 1.01 + 0.05).all()
     work = [w * h * s for _, _, w, h, s, _ in SPECS]
