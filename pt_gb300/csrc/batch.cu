@@ -334,7 +334,7 @@ cudaError_t issue(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std:
                     return e;
                 nl++;
             }
-            cudaEventRecordWithFlags(b->done_ev[b->job_done[j]], b->side, cudaEventRecordExternal);
+            record_timed(b->done_ev[b->job_done[j]], b->side);
         }
     }
     if (!plan.waves.empty()) {

@@ -89,6 +89,20 @@ cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shar
                                    uint32_t n_paths_max, bool w4, int sm_count, uint32_t* launches, cudaStream_t stream,
                                    const WaveMulti* multi = nullptr, uint32_t* path_share2 = nullptr,
                                    cudaEvent_t* wave_done = nullptr);
+// Records `ev` on `st` so that its time can be read later: inside a stream
+// capture as an external event (an event-record node of the graph; a plain
+// record there only orders streams), otherwise as a plain record (the
+// external flag is refused outside a capture).
+inline cudaError_t record_timed(cudaEvent_t ev, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess)
+        return e;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                                               : cudaEventRecord(ev, st);
+}
+
 cudaError_t features_init_tables(const uint32_t* table128, const float* srgb256, cudaStream_t stream);
 
 // Denoiser features and packing (features.cu).

@@ -1172,11 +1172,8 @@ cudaError_t launch_wavefront_batch(const RenderArgs* jobs, const WaveShare* shar
                               i ? multi->acc[(i - 1) & 1] : nullptr, multi->acc[i & 1]);
         else
             nl += launch_wave(x, w4, bw.max_bounces, bw.n_pixels, sm_count, ws);
-        // after the wave's accumulation, the last of its launches; an external
-        // record so that, inside a stream capture, it becomes an event-record
-        // node of the graph (a plain record there only orders streams)
-        if (wave_done)
-            cudaEventRecordWithFlags(wave_done[i], ws, cudaEventRecordExternal);
+        if (wave_done) // after the wave's accumulation, the last of its launches
+            record_timed(wave_done[i], ws);
     }
     if (ways == 2) {
         cudaEventRecord(multi->join[1], multi->stream[1]);
