@@ -339,7 +339,9 @@ def test_wavefront_many_waves(ctx, small, tmp_path):
     r = subprocess.run([sys.executable, "-c", _MANY_WAVES, str(tmp_path / "scene"), str(out)], env=env, cwd=root,
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
-    assert "launches" in r.stdout and int(r.stdout.split()[-1]) == 3 * (2 + 5 * 4)  # 3 waves of 4 segments
+    # 3 waves of raygen + accumulate and 4 segments of extend, extend resume, split,
+    # shade, shadow, shadow resume, reset
+    assert "launches" in r.stdout and int(r.stdout.split()[-1]) == 3 * (2 + 7 * 4)
     gpu = np.load(out)
     hs, view = small
     ctx.upload(view)
