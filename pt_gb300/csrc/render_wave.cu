@@ -910,7 +910,7 @@ struct StageVariant {
     int shade = 6;       // resident-block target of shade (0: none)
     uint32_t refill = 0; // 0: no refill; else 1..32
     uint32_t budget = 48; // extend's first-pass step budget over 4-wide nodes (PT_EXTEND_BUDGET; 0: one pass)
-    uint32_t shadow_budget = 48; // the same for shadow rays (PT_SHADOW_BUDGET)
+    uint32_t shadow_budget = 0; // the same for shadow rays (PT_SHADOW_BUDGET; measured slower, off)
 };
 
 static StageVariant stage_variant()
