@@ -340,8 +340,8 @@ def test_wavefront_many_waves(ctx, small, tmp_path):
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     # 3 waves of raygen + accumulate and 4 segments of extend, extend resume, split,
-    # shade, shadow, shadow resume, reset
-    assert "launches" in r.stdout and int(r.stdout.split()[-1]) == 3 * (2 + 7 * 4)
+    # shade, shadow, reset
+    assert "launches" in r.stdout and int(r.stdout.split()[-1]) == 3 * (2 + 6 * 4)
     gpu = np.load(out)
     hs, view = small
     ctx.upload(view)
