@@ -394,6 +394,9 @@ def raw_struct(raw: dict):
     """raw dict -> pt_raw_scene (ctypes) + the arrays that must stay alive."""
     from pt_gb300 import abi  # struct layouts of include/pt_scene.h only
     keep = {k: np.ascontiguousarray(v) for k, v in raw.items() if isinstance(v, np.ndarray)}
+    for k in ("point_lights", "directional_lights"):  # raw scenes of the generators may have none
+        keep.setdefault(k, np.zeros((0, 6), np.float32))
+    keep["environment_colour"] = np.asarray(raw.get("environment_colour", (0.0, 0.0, 0.0)), np.float32)
 
     def p(name, ct):
         return keep[name].ctypes.data_as(C.POINTER(ct))

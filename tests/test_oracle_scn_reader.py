@@ -50,3 +50,20 @@ def test_reader_equals_product_loader(tmp_path, make):
     oracle.lib().or_camera_params(scn_reader.camera_desc(cam), 64, 48, p_or)
     p_pt = hs.render_params(64, 48, 1, 1)
     assert bytes(p_or.inv_view) == bytes(p_pt.inv_view) and bytes(p_or.inv_proj) == bytes(p_pt.inv_proj)
+
+
+def test_raw_struct_of_generated_raw_scenes():
+    """The oracle's marshalling of the generators' raw scenes (which carry no
+    light arrays): the oracle's packing equals the product's, on the heavy
+    configuration's scene."""
+    raw, cam = scenes.heavy_scene()
+    rs, keep = scn_reader.raw_struct(raw)
+    packed = oracle.OraclePacked(rs)
+    hs = P.HostScene.from_raw(raw, cam)  # the packed view borrows its memory
+    a = P.view_arrays(hs.pack())
+    b = P.view_arrays(packed.view)
+    for k in a:
+        if isinstance(a[k], np.ndarray):
+            assert np.array_equal(a[k], b[k]), k
+        else:
+            assert a[k] == b[k], k
