@@ -240,8 +240,7 @@ enum Traversal : int { TRAV_BVH4 = 0, TRAV_BVH2 = 1, TRAV_BVH2_WW = 2 };
 // passes: a ray still traversing after `budget` steps is parked (its state
 // saved to a slot of a.w.park, slots taken by one atomic per warp) and the
 // lane moves on, so a warp's rays no longer wait for its slowest one;
-// k_wf_extend_resume finishes the parked rays 32 to a warp.  Rays park only
-// while the queue holds fresh rays for the warp to take next.  A ray whose stack
+// k_wf_extend_resume finishes the parked rays 32 to a warp.  A ray whose stack
 // is deeper than PARK_STACK, or that finds no free slot, finishes here.  The
 // hit is the same either way: the resumed traversal continues the same
 // sequence of steps.
@@ -281,14 +280,7 @@ __global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 7 : 1) k_wf_extend(Wa
             }
             for (uint32_t k = 0;; k++) {
                 if (k == budget) {
-                    // park only while the queue still holds fresh rays for the
-                    // warp to take; after that a parked ray would only wait for
-                    // the resume launch, so it continues here
-                    uint32_t fetched = 0;
-                    if (lane == 0)
-                        fetched = *(volatile uint32_t*)&a.w.counts[3];
-                    const bool more = __shfl_sync(0xffffffffu, fetched, 0) < count;
-                    const bool park = more && live && t.sp <= PARK_STACK;
+                    const bool park = live && t.sp <= PARK_STACK;
                     const unsigned want = __ballot_sync(0xffffffffu, park);
                     if (want) {
                         uint32_t slot0 = 0;
