@@ -8,8 +8,11 @@ accumulation.  Synthetic, seeded scene data (pt_gb300.scenes.mid_scene).
   value   Mpath-segs/s of the device render with the scene and image resident
           in HBM: path segments (primary + extension rays, each with its
           shading and NEE shadow ray) / device time (CUDA events on the render
-          stream), summed over the timed steps.  L2 is flushed (512 MiB write)
-          between steps, outside the event pairs.
+          stream, which joins the sub-wave streams), summed over the timed
+          steps.  L2 is flushed (512 MiB write) between steps, outside the
+          event pairs.  The renders run as the library runs them by default
+          (two sub-waves in flight); the per-stage times of the roofline come
+          from a second pass of the same steps on one stream.
   e2e     the same metric through the C ABI with host buffers: each step
           uploads the packed scene from pinned host memory, builds the BVH,
           renders and reads the image back to host memory.
@@ -535,12 +538,15 @@ def config_leg(device_index: int, name: str, steps: int, cpu_seconds: float, no_
     st = ctx.render(p)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device_index}")
     ms, stage, launches = [], [0.0] * 6, 0
+    for _ in range(steps):  # the library's default streams
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms.append(ctx.render(p).milliseconds)
     p.flags = abi.PT_RENDER_TIME_STAGES
-    for _ in range(steps):
+    for _ in range(steps):  # the same renders on one stream, stage by stage
         flush.zero_()
         torch.cuda.synchronize()
         s = ctx.render(p)
-        ms.append(s.milliseconds)
         stage = [a + b for a, b in zip(stage, s.stage_ms)]
         launches += s.stage_launches
     t = sum(ms) / 1000.0
@@ -729,9 +735,13 @@ def run_ours(args) -> None:
     segs_per_step = st.segments
     launches_per_step = st.kernel_launches
 
-    # ---- device-resident timing
+    # ---- device-resident timing: K renders as the library runs them (its
+    # default sub-wave streams), then the same K renders on one stream with
+    # events between the stages (per-stage times for the roofline; stage
+    # events need a single stream)
     dev_ms = []
     stage_ms = [0.0] * 6
+    stage_step_ms = []
     stage_launches = 0
     if dist:
         tdist.barrier()
@@ -740,14 +750,21 @@ def run_ours(args) -> None:
     with ClockSampler(device_index) as clocks:
         for _ in range(args.steps):
             l2_flush()
-            s = ctx.render(params(flags=abi.PT_RENDER_TIME_STAGES))
+            s = ctx.render(params())
             if s.segments != segs_per_step:
                 raise RuntimeError("segment count changed between identical renders")
             dev_ms.append(s.milliseconds)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        for _ in range(args.steps):
+            l2_flush()
+            s = ctx.render(params(flags=abi.PT_RENDER_TIME_STAGES))
+            if s.segments != segs_per_step:
+                raise RuntimeError("segment count changed between identical renders")
+            stage_step_ms.append(s.milliseconds)
             stage_ms = [a + b for a, b in zip(stage_ms, s.stage_ms)]
             stage_launches += s.stage_launches
     torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
     t_dev = sum(dev_ms) / 1000.0
     if dist:
         t = torch.tensor([t_dev], device=f"cuda:{device_index}")
@@ -813,6 +830,7 @@ def run_ours(args) -> None:
                 "launches": stage_launches, "avg_launch_ms": stage_ms[1] / ext_launches, "rays_per_launch": rays_per_launch,
                 "peak_source": peak_src,
                 "stage_ms_per_step": {k: v / args.steps for k, v in zip(abi.STAGES, stage_ms)},
+                "stage_timed_ms_per_step": sum(stage_step_ms) / args.steps,
                 "step": {"achieved": step_achieved, "frac": step_achieved / peaks["hbm_gbs"], "bytes_per_segment": b,
                          "note": "whole render step: B_seg x segments / step time"}}
         base = None
@@ -840,8 +858,9 @@ def run_ours(args) -> None:
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": shared_config(world),
                 "details": {"kernel": {1: "megakernel", 2: "wavefront"}.get(st.kernel_used, str(st.kernel_used)),
-                           "wave_streams": "timed steps: 1 (per-launch stage events need one stream); e2e and "
-                                           "time_to_mse: the library default (PT_WAVE_STREAMS, 2)",
+                           "wave_streams": "value, e2e and time_to_mse: the library default (PT_WAVE_STREAMS, 2 sub-waves in "
+                                           "flight); roofline stage times: a second pass of the same steps on one stream "
+                                           "(per-launch stage events need one stream)",
                            "segments_per_step": int(segs_per_step), "accel_build_ms": info.build_ms,
                            "image": f"{WIDTH}x{HEIGHT}", "spp": SPP,
                            "node_visits_per_ray": st.node_visits / max(1, st.segments + st.shadow_rays),

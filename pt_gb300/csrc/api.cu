@@ -90,7 +90,8 @@ void inverse4(const double m[16], double out[16])
 
 static thread_local std::string g_create_error;
 
-// The 4-wide node a reachable BVH2 node must have (k_make_bvh4 restated).
+// The 4-wide node a reachable BVH2 node must have (k_make_bvh4 restated):
+// its grandchildren's links, and their boxes rounded outwards to half precision.
 // The node's children are in range (checked by the caller); its
 // grandchildren are read only when in range.
 static bool bvh4_matches(const std::vector<BvhNode>& nodes, size_t i, const Bvh4Node& got)
@@ -115,10 +116,21 @@ static bool bvh4_matches(const std::vector<BvhNode>& nodes, size_t i, const Bvh4
             put(nd.c1xy, nd.c01z.z, nd.c01z.w, cr);
         }
     }
-    const float4* planes[6] = {&got.lox, &got.hix, &got.loy, &got.hiy, &got.loz, &got.hiz};
-    for (int a = 0; a < 6; a++)
-        if (std::memcmp(planes[a], b[a], sizeof(float) * k) != 0)
-            return false;
+    // each half-precision plane is the BVH2's plane rounded outwards
+    const uint4* axes[3] = {&got.x, &got.y, &got.z};
+    for (int a = 0; a < 3; a++) {
+        const uint32_t w[4] = {axes[a]->x, axes[a]->y, axes[a]->z, axes[a]->w};
+        for (int j = 0; j < k; j++) {
+            const uint32_t lo_w = w[j / 2], hi_w = w[2 + j / 2];
+            const unsigned short lo_bits = (unsigned short)(j & 1 ? lo_w >> 16 : lo_w & 0xFFFFu);
+            const unsigned short hi_bits = (unsigned short)(j & 1 ? hi_w >> 16 : hi_w & 0xFFFFu);
+            const __half lo = __ushort_as_half(lo_bits), hi = __ushort_as_half(hi_bits);
+            if (!(lo_bits == __half_as_ushort(__float2half_rd(b[2 * a][j])) && __half2float(lo) <= b[2 * a][j]))
+                return false;
+            if (!(hi_bits == __half_as_ushort(__float2half_ru(b[2 * a + 1][j])) && __half2float(hi) >= b[2 * a + 1][j]))
+                return false;
+        }
+    }
     const int gl[4] = {got.link.x, got.link.y, got.link.z, got.link.w};
     return std::memcmp(gl, ref, sizeof(gl)) == 0;
 }

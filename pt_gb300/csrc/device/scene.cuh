@@ -8,9 +8,10 @@
 //   light      u32 light-sampler stream (lightsample.cpp:89-221)
 //   nodes      BvhNode, 64 B: both child boxes of a BVH2 node (one array for
 //              every BLAS and the TLAS)
-//   nodes4     Bvh4Node, 128 B (one cache line), same indices as `nodes`: node
-//              i's grandchildren (a child that is a leaf stands for itself),
-//              so the traversal descends two BVH2 levels per dependent fetch
+//   nodes4     Bvh4Node, 64 B (half-precision planes rounded outwards; two
+//              nodes per cache line), same indices as `nodes`: node i's
+//              grandchildren (a child that is a leaf stands for itself), so
+//              the traversal descends two BVH2 levels per dependent fetch
 //   tris       TriRec, 48 B: the three object-space vertices of a triangle in
 //              BVH leaf order plus its mesh-local primitive index
 //   dinst      DevInstance, 64 B: world-to-object rows + BLAS root reference
@@ -18,6 +19,7 @@
 // read-only path.
 #pragma once
 #include <cstdint>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "ptmath.cuh"
@@ -44,10 +46,13 @@ struct __align__(16) BvhNode {
 
 // Four child boxes as x/y/z planes across the children (lane k = child k)
 // and their references; REF_EMPTY marks an unused slot.
-struct __align__(128) Bvh4Node {
-    float4 lox, hix, loy, hiy, loz, hiz;
+// Half-precision planes, rounded outwards from the BVH2's boxes (lower planes
+// toward -inf, upper planes toward +inf), so each box contains the box it
+// stands for; two nodes share a 128-byte line.  Per axis a uint4 holds
+// (lo0, lo1), (lo2, lo3), (hi0, hi1), (hi2, hi3) as half2 pairs.
+struct __align__(64) Bvh4Node {
+    uint4 x, y, z;
     int4 link;
-    int4 pad;
 };
 
 struct __align__(16) TriRec {
@@ -314,15 +319,32 @@ __device__ __forceinline__ float fmax3f(float a, float b, float c)
     return d;
 }
 
+// One axis of a half-precision 4-wide node: the lower and upper planes of the
+// four children as floats (exact: every half is a float).
+__device__ __forceinline__ void unpack_planes(const uint4& q, float4& lo, float4& hi)
+{
+    const float2 l01 = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
+    const float2 l23 = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
+    const float2 h01 = __half22float2(*reinterpret_cast<const __half2*>(&q.z));
+    const float2 h23 = __half22float2(*reinterpret_cast<const __half2*>(&q.w));
+    lo = make_float4(l01.x, l01.y, l23.x, l23.y);
+    hi = make_float4(h01.x, h01.y, h23.x, h23.y);
+}
+
 // Intersect the four child boxes of a 4-wide node; bit k of the result is
-// set when child k is hit, e[k] its entry distance.  The far distance is
+// set when child k is hit, e[k] its entry distance.  The boxes contain the
+// BVH2's (outward rounding), so a child the BVH2 would enter is entered here
+// too and the closest hit is the same.  The far distance is
 // scaled once after the minimum over the axes instead of once per axis:
 // rounding is monotonic, so min(a s, b s, c s) = min(a, b, c) s for s > 0 and
 // the value equals the per-axis form of slab_enter bit for bit.
 __device__ __forceinline__ int node4_children(const Bvh4Node* node, const ObjRay& r, float tmin, float tmax, float (&e)[4], int (&c)[4])
 {
-    const float4 lx = ldg4(&node->lox), hx = ldg4(&node->hix), ly = ldg4(&node->loy), hy = ldg4(&node->hiy);
-    const float4 lz = ldg4(&node->loz), hz = ldg4(&node->hiz);
+    const uint4 qx = __ldg(&node->x), qy = __ldg(&node->y), qz = __ldg(&node->z);
+    float4 lx, hx, ly, hy, lz, hz;
+    unpack_planes(qx, lx, hx);
+    unpack_planes(qy, ly, hy);
+    unpack_planes(qz, lz, hz);
     const int4 l = ldg4i(&node->link);
     c[0] = l.x;
     c[1] = l.y;
