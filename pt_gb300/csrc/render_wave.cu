@@ -244,8 +244,11 @@ enum Traversal : int { TRAV_BVH4 = 0, TRAV_BVH2 = 1, TRAV_BVH2_WW = 2 };
 // is deeper than PARK_STACK, or that finds no free slot, finishes here.  The
 // hit is the same either way: the resumed traversal continues the same
 // sequence of steps.
+// Residency: 8 blocks of 128 per SM (64 registers, 40-52 B of spills) over
+// the half-precision 4-wide nodes; 7 blocks measured 74.2 against 71.9 ms of
+// extend per step on the mid scene (the shadow kernel is faster at 7).
 template <class Src, int TRAV, bool BUDGET = false>
-__global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 7 : 1) k_wf_extend(WaveArgs<Src> a, uint32_t qi, uint32_t budget)
+__global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 8 : 1) k_wf_extend(WaveArgs<Src> a, uint32_t qi, uint32_t budget)
 {
     const uint32_t* queue = a.w.queue[qi];
     const uint32_t count = *(volatile uint32_t*)&a.w.counts[qi];
@@ -328,7 +331,7 @@ __global__ void __launch_bounds__(128, TRAV == TRAV_BVH4 ? 7 : 1) k_wf_extend(Wa
 // Second extend pass: finishes the traversals the first pass parked, 32 to a
 // warp (persistent warps over the parked slots).
 template <class Src>
-__global__ void __launch_bounds__(128, 7) k_wf_extend_resume(WaveArgs<Src> a)
+__global__ void __launch_bounds__(128, 8) k_wf_extend_resume(WaveArgs<Src> a)
 {
     const uint32_t parked = *(volatile uint32_t*)&a.w.counts[6];
     const uint32_t count = parked < a.w.park.cap ? parked : a.w.park.cap;
