@@ -913,6 +913,11 @@ struct StageVariant {
     int shade = 6;       // resident-block target of shade (0: none)
     uint32_t refill = 0; // 0: no refill; else 1..32
     uint32_t budget = 48; // extend's first-pass step budget over 4-wide nodes (PT_EXTEND_BUDGET; 0: one pass)
+    // two passes only for waves of at least 2^budget_min_log2 paths
+    // (PT_EXTEND_BUDGET_MIN_LOG2): smaller waves ran 2-11 % faster in one
+    // pass (the resume launch's latency tail), waves of 2^25 paths and more
+    // 0.3-0.5 % slower
+    uint32_t budget_min_log2 = 25;
     uint32_t shadow_budget = 0; // the same for shadow rays (PT_SHADOW_BUDGET; measured slower, off)
 };
 
@@ -933,6 +938,10 @@ static StageVariant stage_variant()
         if (const char* b = std::getenv("PT_EXTEND_BUDGET")) {
             const int k = std::atoi(b);
             r.budget = k <= 0 ? 0u : (uint32_t)std::min(k, 1 << 20);
+        }
+        if (const char* b = std::getenv("PT_EXTEND_BUDGET_MIN_LOG2")) {
+            const int k = std::atoi(b);
+            r.budget_min_log2 = (uint32_t)std::max(0, std::min(k, 32));
         }
         if (const char* b = std::getenv("PT_SHADOW_BUDGET")) {
             const int k = std::atoi(b);
@@ -1039,7 +1048,7 @@ static uint32_t launch_wave(const WaveArgs<Src>& a, bool w4, uint32_t max_bounce
         else if (refill)
             k_wf_extend_refill<Src, false><<<trace_blocks, 128, 0, st>>>(a, qi, sv.refill);
         else if (trav == TRAV_BVH4) {
-            if (sv.budget) {
+            if (sv.budget && (uint64_t)a.src.n_paths >= (1ull << sv.budget_min_log2)) {
                 k_wf_extend<Src, TRAV_BVH4, true><<<trace_blocks, 128, 0, st>>>(a, qi, sv.budget);
                 k_wf_extend_resume<Src><<<trace_blocks, 128, 0, st>>>(a);
                 nl++;

@@ -6,6 +6,11 @@ import pytest
 
 # every BVH built during the tests is checked on the host for structure
 os.environ.setdefault("PT_VALIDATE_BVH", "1")
+# the two-pass extend (step budget, parked rays resumed) runs on waves of
+# every size here, not only on the large waves it is used for by default, so
+# the parity tests cover it; the one-pass form is covered by the
+# execution-variant tests (which set their own environment)
+os.environ.setdefault("PT_EXTEND_BUDGET_MIN_LOG2", "0")
 
 ROOT = Path(__file__).resolve().parent.parent
 if str(ROOT) not in sys.path:

@@ -370,16 +370,19 @@ np.save(sys.argv[3], ctx.read_image(fp64=True))
                                  {"PT_REFILL": "16"}, {"PT_BVH_WIDTH": "2", "PT_TRAVERSAL": "ww"},
                                  {"PT_WAVE_PATHS_LOG2": "20"},
                                  {"PT_EXTEND_BUDGET": "0", "PT_SHADOW_BUDGET": "0"},
+                                 {"PT_EXTEND_BUDGET_MIN_LOG2": "25"},
                                  {"PT_EXTEND_BUDGET": "2", "PT_SHADOW_BUDGET": "2"}],
                          ids=["one_stream", "three_streams", "bvh2", "refill", "bvh2_while_while", "small_waves",
-                              "one_pass_traversal", "budget_2_slots_overflow"])
+                              "one_pass_traversal", "default_pass_threshold", "budget_2_slots_overflow"])
 def test_execution_variants_agree(ctx, mid, tmp_path, env):
     """Every execution variant (sub-wave streams, node width, traversal
-    order, lane refill, wave size, the traversal step budget: one pass, or a
-    budget of 2 steps that parks nearly every ray and overflows the parking
-    slots, a quarter of a wave, so the rest finish in the first pass; each
-    read once per process, so set in a child) renders the same image and FP64
-    sums bit for bit as the default."""
+    order, lane refill, wave size, the traversal step budget: one pass, the
+    library's default of two passes only for waves of 2^25 paths or more
+    (one pass here), or a budget of 2 steps that parks nearly every ray and
+    overflows the parking slots, a quarter of a wave, so the rest finish in
+    the first pass; each read once per process, so set in a child) renders
+    the same image and FP64 sums bit for bit as the two-pass extend the tests
+    run by default."""
     import os
     import subprocess
     import sys
