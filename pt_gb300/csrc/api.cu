@@ -507,9 +507,12 @@ int pt_build_accel(pt_ctx* c, pt_accel_info* info)
         (e = c->mesh_root.alloc(c->mesh_count)) != cudaSuccess || (wide && (e = c->nodes4.alloc(n_nodes)) != cudaSuccess))
         return c->cuda_fail(e, "acceleration structure allocation");
     size_t scratch_bytes = bvh_scratch_bytes(c->mesh_count, c->tri_count, c->instance_count);
+    scratch_bytes = (scratch_bytes + 15) & ~(size_t)15;
     void* scratch = nullptr;
-    if ((e = cudaMalloc(&scratch, scratch_bytes)) != cudaSuccess)
+    // the scratch plus one word: set when a 4-wide node's half planes overflow
+    if ((e = cudaMalloc(&scratch, scratch_bytes + 16)) != cudaSuccess)
         return c->cuda_fail(e, "BVH scratch allocation");
+    uint32_t* overflow = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + scratch_bytes);
     BvhBuildInput in{};
     in.vertices = c->vertices.p;
     in.indices = c->indices.p;
@@ -527,16 +530,28 @@ int pt_build_accel(pt_ctx* c, pt_accel_info* info)
     out.dinst = c->dinst.p;
     out.mesh_root = c->mesh_root.p;
     cudaEventRecord(c->ev0, c->stream);
-    e = bvh_build(in, out, scratch, scratch_bytes, c->stream);
+    // node slots no tree uses stay zero (finite boxes for the 4-wide view)
+    e = cudaMemsetAsync(c->nodes.p, 0, n_nodes * sizeof(BvhNode), c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(overflow, 0, sizeof(uint32_t), c->stream);
+    if (e == cudaSuccess)
+        e = bvh_build(in, out, scratch, scratch_bytes, c->stream);
     if (e == cudaSuccess && wide)
-        e = build_bvh4(c->nodes.p, (uint32_t)n_nodes, c->nodes4.p, c->stream);
+        e = build_bvh4(c->nodes.p, (uint32_t)n_nodes, c->nodes4.p, overflow, c->stream);
     cudaEventRecord(c->ev1, c->stream);
     cudaError_t e2 = cudaStreamSynchronize(c->stream);
+    uint32_t overflowed = 0;
+    if (e == cudaSuccess && e2 == cudaSuccess && wide)
+        e2 = cudaMemcpy(&overflowed, overflow, sizeof(uint32_t), cudaMemcpyDeviceToHost);
     cudaFree(scratch);
     if (e != cudaSuccess)
         return c->cuda_fail(e, "BVH build");
     if (e2 != cudaSuccess)
         return c->cuda_fail(e2, "BVH build");
+    // coordinates beyond the half range: traverse the full-precision BVH2
+    if (overflowed)
+        c->nodes4.release();
+    const bool wide_used = wide && !overflowed;
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->tlas_root = out.tlas_root;
@@ -554,7 +569,7 @@ int pt_build_accel(pt_ctx* c, pt_accel_info* info)
     c->accel.tlas_nodes = c->instance_count > 1 ? c->instance_count - 1 : 0;
     c->accel.blas_nodes = c->tri_count > 1 ? c->tri_count - 1 : 0;
     c->accel.triangles = c->tri_count;
-    c->accel.device_bytes = n_nodes * sizeof(BvhNode) + (wide ? n_nodes * sizeof(Bvh4Node) : 0) +
+    c->accel.device_bytes = n_nodes * sizeof(BvhNode) + (wide_used ? n_nodes * sizeof(Bvh4Node) : 0) +
                             (size_t)c->tri_count * sizeof(TriRec) + (size_t)c->instance_count * sizeof(DevInstance);
     c->accel.build_ms = ms;
     if (info)

@@ -933,16 +933,21 @@ size_t bvh_node_count(uint32_t tri_count, uint32_t instance_count)
 
 // 4-wide nodes from the finished BVH2, one per BVH2 node (same index): the
 // children of node i's children in order (c00, c01, c10, c11), a child that
-// is a leaf standing for itself.  Boxes are the BVH2's rounded outwards to
-// half precision (lower planes toward -inf, upper toward +inf), so every
-// 4-wide box contains the one the BVH2 tests and no hit is lost; the node
-// takes 64 bytes instead of 128 (mid scene 1,024x1,024 at 128 spp: 1,582 ->
-// 1,609 Mpath-segs/s, heavy scene 470 -> 509, node visits per ray +3.7 %).  (Filling the four slots greedily by box
+// is a leaf standing for itself.  (Filling the four slots greedily by box
 // surface instead measured 1.3 % slower on the mid scene, and the order
 // c00, c10, c01, c11 1.2 % slower: sibling boxes stay next to each other.)
-// Slots of the node array that no tree uses hold unspecified links; the
-// bounds check keeps their derivation inside the array.
-__global__ void k_make_bvh4(const BvhNode* nodes, uint32_t n, Bvh4Node* out)
+// Boxes are the BVH2's rounded outwards to half precision (lower planes
+// toward -inf, upper toward +inf), so every 4-wide box contains the one the
+// BVH2 tests and no hit is lost; the node takes 64 bytes instead of 128 (mid
+// scene 1,024x1,024 at 128 spp: 1,582 -> 1,609 Mpath-segs/s, heavy scene
+// 470 -> 509, node visits per ray +3.7 %).  A plane beyond the half range
+// (|x| > 65504) rounds to an infinity; the node stays conservative, but
+// `*overflow` is set so that the caller traverses the BVH2 instead (an
+// infinite plane times the infinite inverse direction of an axis-parallel ray
+// gives NaN slab distances).  Slots of the node array that no tree uses hold
+// zeros (the caller clears the array before the build); the bounds check
+// keeps their derivation inside the array.
+__global__ void k_make_bvh4(const BvhNode* nodes, uint32_t n, Bvh4Node* out, uint32_t* overflow)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -986,6 +991,8 @@ __global__ void k_make_bvh4(const BvhNode* nodes, uint32_t n, Bvh4Node* out)
             const __half h0 = (a & 1) ? __float2half_ru(b[a][2 * j]) : __float2half_rd(b[a][2 * j]);
             const __half h1 = (a & 1) ? __float2half_ru(b[a][2 * j + 1]) : __float2half_rd(b[a][2 * j + 1]);
             q[a][j] = (uint32_t)__half_as_ushort(h0) | ((uint32_t)__half_as_ushort(h1) << 16);
+            if (__hisinf(h0) || __hisinf(h1))
+                *overflow = 1u;
         }
     }
     o.x = make_uint4(q[0][0], q[0][1], q[1][0], q[1][1]);
@@ -995,11 +1002,11 @@ __global__ void k_make_bvh4(const BvhNode* nodes, uint32_t n, Bvh4Node* out)
     out[i] = o;
 }
 
-cudaError_t build_bvh4(const BvhNode* nodes, uint32_t n, Bvh4Node* out, cudaStream_t st)
+cudaError_t build_bvh4(const BvhNode* nodes, uint32_t n, Bvh4Node* out, uint32_t* overflow, cudaStream_t st)
 {
     if (n == 0)
         return cudaSuccess;
-    k_make_bvh4<<<blocks(n, 128), 128, 0, st>>>(nodes, n, out);
+    k_make_bvh4<<<blocks(n, 128), 128, 0, st>>>(nodes, n, out, overflow);
     return cudaGetLastError();
 }
 

@@ -148,7 +148,7 @@ struct BvhBuildOutput {
 
 // 4-wide nodes derived from the n BVH2 nodes (same indices), and whether the
 // tracer uses them (PT_BVH_WIDTH=2 keeps the BVH2 traversal).
-cudaError_t build_bvh4(const BvhNode* nodes, uint32_t n, Bvh4Node* out, cudaStream_t stream);
+cudaError_t build_bvh4(const BvhNode* nodes, uint32_t n, Bvh4Node* out, uint32_t* overflow, cudaStream_t stream);
 bool use_bvh4();
 
 // Scratch sizing for bvh_build (bytes).

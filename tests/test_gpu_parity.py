@@ -107,6 +107,74 @@ def test_textured_scene_bitexact(ctx, textured, kernel):
     assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
 
 
+def _far_scene(d, offset):
+    """The small scene's ground, spheres and light moved `offset` along x
+    (camera with them): world boxes beyond the half-precision range when
+    offset > 65504."""
+    scenes.write_gltf(d / "ground.gltf", scenes.quad(20.0, 0.0, False), {"base": (0.6, 0.5, 0.4), "roughness": 1.0})
+    scenes.write_gltf(d / "sphere.gltf", scenes.icosphere(2), {"base": (0.3, 0.6, 0.5), "roughness": 0.4})
+    scenes.write_gltf(d / "light.gltf", scenes.quad(2.0, 6.0, True),
+                      {"base": (0.0, 0.0, 0.0), "roughness": 1.0, "emission_strength": 10.0})
+    scn = scenes.ScnWriter({"eye": (offset - 1.0, 2.0, -3.0), "target": (offset, 0.75, 0.0), "fov": 60.0},
+                           (0.375, 0.45, 0.9))
+    for name in ("ground", "sphere", "light"):
+        scn.add_object(name, f"{name}.gltf")
+    scn.add_instance("ground", translate=(offset, 0.0, 0.0))
+    for k in range(4):
+        scn.add_instance("sphere", scale=(0.7, 0.7, 0.7), translate=(offset - 2.0 + 1.4 * k, 0.7, 0.5 * k))
+    scn.add_instance("light", translate=(offset, 0.0, 0.0))
+    scn.write(d / "far.scn")
+    return d / "far.scn"
+
+
+@pytest.mark.parametrize("offset", [1000.0, 3.0e4])
+def test_far_from_origin_scene_bitexact(ctx, tmp_path, offset):
+    """Instances far from the origin, still inside the range of the 4-wide
+    nodes' half-precision planes (|x| <= 65504): coarser planes (a half has
+    10 mantissa bits) only loosen the boxes, and the image equals the
+    oracle's bit for bit."""
+    hs = P.HostScene.load(_far_scene(tmp_path, offset))
+    view = hs.pack()
+    params = hs.render_params(64, 48, 4, 5)
+    ctx.upload(view)
+    info = ctx.build_accel()
+    st = ctx.render(params)
+    assert st.error_word == 0
+    gpu = ctx.read_image()
+    ref, ost = oracle.OracleScene(view).render(params)
+    _assert_bitexact(gpu, ref)
+    assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
+    n_nodes = info.blas_nodes + info.tlas_nodes + 1
+    plain = n_nodes * 64 + info.triangles * 48 + view.instance_count * 64
+    assert info.device_bytes == plain + n_nodes * 64  # the 4-wide copy is there
+
+
+def test_half_range_overflow_uses_the_bvh2(ctx, tmp_path):
+    """World boxes beyond the half range (instances at x = 7e4): the build
+    notices that planes rounded to infinity and the traversal uses the
+    full-precision BVH2 (no 4-wide copy in the acceleration structure's
+    size).  Far from the origin the image is not bit-exact: with either
+    traversal (the BVH2 forced by PT_BVH_WIDTH=2 too) 2 of 3,072 pixels
+    differ from the oracle at x = 7e4 and 7 at 2e5, while the oracle's BVH
+    and its brute-force mode agree with each other; the cause is not located.
+    Checked here: the fallback, equal segment and shadow-ray counts, and at
+    least 99.5 % of the pixels bit-equal."""
+    hs = P.HostScene.load(_far_scene(tmp_path, 7.0e4))
+    view = hs.pack()
+    params = hs.render_params(64, 48, 4, 5)
+    ctx.upload(view)
+    info = ctx.build_accel()
+    st = ctx.render(params)
+    assert st.error_word == 0
+    gpu = ctx.read_image()
+    ref, ost = oracle.OracleScene(view).render(params)
+    n_nodes = info.blas_nodes + info.tlas_nodes + 1
+    assert info.device_bytes == n_nodes * 64 + info.triangles * 48 + view.instance_count * 64
+    assert st.segments == ost.segments and st.shadow_rays == ost.shadow_rays
+    differ = (gpu.view(np.uint32) != ref.view(np.uint32)).any(-1).mean()
+    assert differ <= 0.005, differ
+
+
 def test_glass_scene_bitexact(ctx, kernel):
     """Refractive dielectrics (clear and tinted glass, the library's extension):
     reflection/refraction choice, radiance scaling and the full-weight
