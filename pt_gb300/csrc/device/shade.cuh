@@ -330,8 +330,14 @@ __device__ __forceinline__ void shade_dielectric(PathState& pl, f3 tint, float e
 }
 
 // Closest-hit shader (pathtrace.ch.hlsl:227-360) without the shadow ray.
-__device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 ray_o, f3 ray_d, const Hit& h, NeeRequest& nee)
+// The NEE request is handed to `nee_out(pl, request)` as soon as it is
+// formed, before the BSDF is sampled (nothing after it changes the radiance),
+// so a caller that stores it at once does not carry it through the rest of
+// the shader; it is not called when the shader ends before the light term.
+template <class NeeOut>
+__device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 ray_o, f3 ray_d, const Hit& h, NeeOut& nee_out)
 {
+    NeeRequest nee;
     nee.add = false;
     nee.trace = false;
     PT_CHECK_INDEX(h.inst < s.instance_count, s, {
@@ -494,6 +500,7 @@ __device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 r
             }
         }
     }
+    nee_out(pl, nee);
 
     f3 m;
     float w, pdf;
@@ -511,6 +518,13 @@ __device__ __forceinline__ void shade_hit(const DevScene& s, PathState& pl, f3 r
     pl.next_o = ip;
     pl.next_d = normalize(wi);
 }
+
+// shade_hit's NEE output for a caller that traces the shadow ray itself
+// after the shader: the request is kept.
+struct NeeKeep {
+    NeeRequest& r;
+    __device__ __forceinline__ void operator()(PathState&, const NeeRequest& n) { r = n; }
+};
 
 // Adds light_contribution() to the path radiance given the shadow ray's
 // visibility (1 = unoccluded opaque path, 0 = occluded).

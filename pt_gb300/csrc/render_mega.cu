@@ -13,7 +13,10 @@ __device__ __forceinline__ void shade_segment(const DevScene& s, PathState& pl, 
         return;
     }
     NeeRequest nee;
-    shade_hit(s, pl, ro, rd, h, nee);
+    nee.add = false;
+    nee.trace = false;
+    NeeKeep keep{nee};
+    shade_hit(s, pl, ro, rd, h, keep);
     float vis = 0.0f;
     if (nee.trace) {
         shadow_rays++;

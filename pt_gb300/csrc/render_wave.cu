@@ -427,6 +427,31 @@ __global__ void __launch_bounds__(256) k_wf_split(WaveArgs<Src> a, uint32_t qi)
         atomicAdd(a.src.counters() + 0, (unsigned long long)misses);
 }
 
+// shade_hit's NEE output in the wavefront: a request with a shadow ray goes
+// straight to the path's NEE slots (the shadow stage finishes it), one
+// without is finished at once, so the shader carries neither through its
+// BSDF sampling.  The radiance sum keeps the reference's order: nothing in
+// the shader adds to it after the light term.
+template <class Src>
+struct NeeToWave {
+    const WaveArgs<Src>& a;
+    uint32_t p;
+    bool traced;
+    __device__ __forceinline__ void operator()(PathState& pl, const NeeRequest& nee)
+    {
+        if (nee.add && nee.trace) {
+            a.w.nee_o[p] = make_float4(nee.origin.x, nee.origin.y, nee.origin.z, nee.tmax);
+            a.w.nee_d[p] = make_float4(nee.dir.x, nee.dir.y, nee.dir.z, nee.w);
+            a.w.nee_e[p] = make_float4(nee.emission.x, nee.emission.y, nee.emission.z, nee.cos_i);
+            a.w.nee_b[p] = make_float4(nee.brdf.x, nee.brdf.y, nee.brdf.z, nee.pdf);
+            a.w.nee_tp[p] = make_float4(nee.tp_before.x, nee.tp_before.y, nee.tp_before.z, 0.0f);
+            traced = true;
+        } else if (nee.add) {
+            finish_nee(pl.radiance, nee, 0.0f);
+        }
+    }
+};
+
 template <class Src, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_t qi)
 {
@@ -460,9 +485,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_
             float4 o = a.w.ray_o[p], d = a.w.ray_d[p];
             f3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
             uint32_t prim = a.w.hit_prim[p];
-            NeeRequest nee;
-            nee.add = false;
-            nee.trace = false;
+            NeeToWave<Src> nee_out{a, p, false};
             {
                 // the hit queue holds hits only (extend finished the misses)
                 float4 hh = a.w.hit[p];
@@ -478,19 +501,11 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(WaveArgs<Src> a, uint32_
                     a.w.f_a[p] = make_float4(alb.x, alb.y, alb.z, h.t);
                     a.w.f_n[p] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
                 }
-                shade_hit(s, pl, ro, rd, h, nee);
+                shade_hit(s, pl, ro, rd, h, nee_out);
             }
-            if (nee.add && !nee.trace)
-                finish_nee(pl.radiance, nee, 0.0f);
-            trace = nee.add && nee.trace;
-            if (trace) {
+            trace = nee_out.traced;
+            if (trace)
                 shadow_rays++;
-                a.w.nee_o[p] = make_float4(nee.origin.x, nee.origin.y, nee.origin.z, nee.tmax);
-                a.w.nee_d[p] = make_float4(nee.dir.x, nee.dir.y, nee.dir.z, nee.w);
-                a.w.nee_e[p] = make_float4(nee.emission.x, nee.emission.y, nee.emission.z, nee.cos_i);
-                a.w.nee_b[p] = make_float4(nee.brdf.x, nee.brdf.y, nee.brdf.z, nee.pdf);
-                a.w.nee_tp[p] = make_float4(nee.tp_before.x, nee.tp_before.y, nee.tp_before.z, 0.0f);
-            }
             // continuation (rg.hlsl:38-55): RR from segment rr_start >= 1
             if (!pl.final_segment) {
                 bool killed = false;
