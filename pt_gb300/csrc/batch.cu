@@ -12,7 +12,8 @@
 //
 // The autotuner times trial batches (each job at 1/32 of its samples, at
 // least 1) for a few candidate settings and keeps the fastest, per batch:
-//   1. wave capacity 2^21, 2^23, 2^25, 2^26 paths (all jobs on the wavefront);
+//   1. wave capacity 2^26, 2^25, 2^23, 2^21 paths (all jobs on the wavefront;
+//      a smaller capacity must be more than 3 % faster to be kept);
 //   2. megakernel threshold 0, 2^18, 2^21 on a job's trial work, pixels x
 //      trial samples x (bounces + 1) (tile 16x8);
 //   3. if a threshold won: megakernel tile 8x16 or 32x4 against 16x8.
@@ -406,14 +407,22 @@ int tune(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vector<p
     uint64_t mem_paths = ~0ull;
     if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
         mem_paths = ((uint64_t)free_b + (uint64_t)b->state.n + (uint64_t)b->state2.n) / 8 / (wave_state_bytes(1u << 20) >> 20);
-    auto consider = [&](const BatchChoice& ch) -> int {
+    // times one setting; `ran` is false when the setting does not apply
+    auto measure = [&](const BatchChoice& ch, float& ms, bool& ran) -> int {
+        ran = false;
         if (max_px > ch.capacity)
             return PT_OK; // the largest job would not fit a wave
         if (ch.capacity > mem_paths && ch.capacity > (1u << 21))
             return PT_OK;
+        const int rc = trial(c, b, jobs, tp, ch, ms);
+        ran = rc == PT_OK;
+        return rc;
+    };
+    auto consider = [&](const BatchChoice& ch) -> int {
         float ms = 0.0f;
-        int rc = trial(c, b, jobs, tp, ch, ms);
-        if (rc != PT_OK)
+        bool ran = false;
+        const int rc = measure(ch, ms, ran);
+        if (rc != PT_OK || !ran)
             return rc;
         if (!have || ms < best_ms) {
             best_ms = ms;
@@ -423,11 +432,22 @@ int tune(pt_ctx* c, BatchState* b, const pt_batch_job* jobs, const std::vector<p
         return PT_OK;
     };
     int rc;
-    for (uint32_t lg : {21u, 23u, 25u, 26u}) {
+    // Capacity: the trial batch holds 1/32 of the samples, so its waves are
+    // emptier than the real batch's and it understates what larger waves gain
+    // (fuller late segments, fewer launches per sample); a larger capacity is
+    // kept unless a smaller one is more than 3 % faster in the trial.
+    for (uint32_t lg : {26u, 25u, 23u, 21u}) {
         BatchChoice ch;
         ch.capacity = fixed_capacity ? fixed_capacity : 1u << lg;
-        if ((rc = consider(ch)) != PT_OK)
+        float ms = 0.0f;
+        bool ran = false;
+        if ((rc = measure(ch, ms, ran)) != PT_OK)
             return rc;
+        if (ran && (!have || ms * 1.03f < best_ms)) {
+            best_ms = ms;
+            best = ch;
+            have = true;
+        }
         if (fixed_capacity)
             break;
     }
