@@ -369,20 +369,23 @@ __device__ __forceinline__ int node4_children(const Bvh4Node* node, const ObjRay
     return m;
 }
 
+constexpr int STACK_SIZE = 96;
+
 // One interior step of a 4-wide traversal: the nearest hit child becomes
 // `ref`, the others are pushed far to near (SORT; else in slot order, for
 // any-hit queries whose result does not depend on the order); nothing hit
 // pops the stack.  A push that would overflow sets ERR_STACK_OVERFLOW and
 // drops those children.
-template <int N, bool SORT = true>
-__device__ __forceinline__ void step4(const DevScene& s, const ObjRay& r, float tmin, float tmax, int& ref, int (&stack)[N], int& sp)
+template <bool SORT = true, class Stack>
+__device__ __forceinline__ void step4(const DevScene& s, const ObjRay& r, float tmin, float tmax, int& ref, Stack& stack, int& sp)
 {
+    constexpr int N = STACK_SIZE;
     float e[4];
     int c[4];
     const int m = node4_children(s.nodes4 + ref, r, tmin, tmax, e, c);
     const int cnt = __popc(m);
     if (cnt == 0) {
-        ref = stack[--sp];
+        ref = stack.get(--sp);
         return;
     }
     if (cnt == 1) {
@@ -399,7 +402,7 @@ __device__ __forceinline__ void step4(const DevScene& s, const ObjRay& r, float 
         ref = c[__ffs(rest) - 1];
         rest &= rest - 1;
         while (rest) {
-            stack[sp++] = c[__ffs(rest) - 1];
+            stack.set(sp++, c[__ffs(rest) - 1]);
             rest &= rest - 1;
         }
         return;
@@ -427,10 +430,10 @@ __device__ __forceinline__ void step4(const DevScene& s, const ObjRay& r, float 
         atomicOr(s.error_word, ERR_STACK_OVERFLOW);
     } else {
         if (cnt == 4)
-            stack[sp++] = r3;
+            stack.set(sp++, r3);
         if (cnt >= 3)
-            stack[sp++] = r2;
-        stack[sp++] = r1;
+            stack.set(sp++, r2);
+        stack.set(sp++, r1);
     }
     ref = r0;
 }
@@ -497,13 +500,13 @@ __device__ __forceinline__ bool better(float t, uint32_t inst, uint32_t prim, co
     return inst < h.inst || (inst == h.inst && prim < h.prim);
 }
 
-constexpr int STACK_SIZE = 96;
 
 // BVH2 interior step: the nearer hit child becomes `ref`, the farther is
 // pushed; nothing hit pops the stack.
-template <int N>
-__device__ __forceinline__ void step2(const DevScene& s, const ObjRay& r, float tmin, float tmax, int& ref, int (&stack)[N], int& sp)
+template <class Stack>
+__device__ __forceinline__ void step2(const DevScene& s, const ObjRay& r, float tmin, float tmax, int& ref, Stack& stack, int& sp)
 {
+    constexpr int N = STACK_SIZE;
     float e0, e1;
     int c0, c1;
     const int m = node_children(s.nodes + ref, r, tmin, tmax, e0, e1, c0, c1);
@@ -514,7 +517,7 @@ __device__ __forceinline__ void step2(const DevScene& s, const ObjRay& r, float 
             far = c0;
         }
         if (sp < N)
-            stack[sp++] = far;
+            stack.set(sp++, far);
         else
             atomicOr(s.error_word, ERR_STACK_OVERFLOW);
         ref = near;
@@ -523,7 +526,7 @@ __device__ __forceinline__ void step2(const DevScene& s, const ObjRay& r, float 
     } else if (m == 2) {
         ref = c1;
     } else {
-        ref = stack[--sp];
+        ref = stack.get(--sp);
     }
 }
 
@@ -541,9 +544,45 @@ struct ClosestTrace {
     uint32_t cur_inst, iter;
     bool in_blas, found;
 };
-// The traversal stack is a separate array: inside the state it would pull
-// every field of the state into local memory with it.
-typedef int TraceStack[STACK_SIZE];
+// The traversal stack is kept apart from the state: inside the state it
+// would pull every field of the state into local memory with it.  It lives in
+// local memory (L1).  Built with PT_SMEM_STACK = k > 0, its first k entries
+// live in shared memory instead, entry i of thread x at word i * 128 + x
+// (every lane in its own bank whatever its depth); that measured slower on
+// the mid scene (extend 72.0 ms per step in local memory, 77.9 with 8 entries
+// and 78.6 with 16 in shared memory: the per-access branch and the smaller
+// L1 cost more than the bank-parallel accesses save).  Every kernel that
+// traverses runs blocks of at most 128 threads; a stack is used by one
+// traversal at a time per thread.
+#ifndef PT_SMEM_STACK
+#define PT_SMEM_STACK 0
+#endif
+constexpr int STACK_SMEM = PT_SMEM_STACK;
+constexpr int STACK_BLOCK = 128;
+
+struct TraceStack {
+#if PT_SMEM_STACK
+    int* sm; // this thread's column of the block's shared array
+    int loc[STACK_SIZE - STACK_SMEM];
+    __device__ __forceinline__ TraceStack()
+    {
+        __shared__ int s_stack[STACK_SMEM * STACK_BLOCK];
+        sm = s_stack + threadIdx.x;
+    }
+    __device__ __forceinline__ int get(int i) const { return i < STACK_SMEM ? sm[i * STACK_BLOCK] : loc[i - STACK_SMEM]; }
+    __device__ __forceinline__ void set(int i, int v)
+    {
+        if (i < STACK_SMEM)
+            sm[i * STACK_BLOCK] = v;
+        else
+            loc[i - STACK_SMEM] = v;
+    }
+#else
+    int loc[STACK_SIZE];
+    __device__ __forceinline__ int get(int i) const { return loc[i]; }
+    __device__ __forceinline__ void set(int i, int v) { loc[i] = v; }
+#endif
+};
 
 __device__ __forceinline__ void closest_begin(const DevScene& s, f3 o, f3 d, float tmin, float tmax, ClosestTrace& t, TraceStack& stack)
 {
@@ -558,7 +597,7 @@ __device__ __forceinline__ void closest_begin(const DevScene& s, f3 o, f3 d, flo
     t.r = t.world;
     t.tmin = tmin;
     t.sp = 0;
-    stack[t.sp++] = REF_DONE;
+    stack.set(t.sp++, REF_DONE);
     t.ref = s.tlas_root == REF_EMPTY ? REF_DONE : s.tlas_root;
     t.in_blas = false;
     t.cur_inst = 0;
@@ -589,7 +628,7 @@ __device__ __forceinline__ bool closest_step(const DevScene& s, ClosestTrace& t,
     if (ref == REF_EXIT_BLAS) {
         t.r = t.world;
         t.in_blas = false;
-        t.ref = stack[--t.sp];
+        t.ref = stack.get(--t.sp);
         return false;
     }
     const uint32_t first = leaf_first(ref), count = leaf_count(ref);
@@ -600,16 +639,16 @@ __device__ __forceinline__ bool closest_step(const DevScene& s, ClosestTrace& t,
         const DevInstance* di = s.dinst + first;
         const int root = __ldg(&di->blas_root);
         if (root == REF_EMPTY || count != 1) {
-            t.ref = stack[--t.sp];
+            t.ref = stack.get(--t.sp);
             return false;
         }
         to_object(di, t.world.o, t.world.d, t.r);
         if (t.sp >= STACK_SIZE) {
             atomicOr(s.error_word, ERR_STACK_OVERFLOW);
-            t.ref = stack[--t.sp];
+            t.ref = stack.get(--t.sp);
             return false;
         }
-        stack[t.sp++] = REF_EXIT_BLAS;
+        stack.set(t.sp++, REF_EXIT_BLAS);
         t.in_blas = true;
         t.ref = root;
         return false;
@@ -631,7 +670,7 @@ __device__ __forceinline__ bool closest_step(const DevScene& s, ClosestTrace& t,
             t.found = true;
         }
     }
-    t.ref = stack[--t.sp];
+    t.ref = stack.get(--t.sp);
     return false;
 }
 
@@ -660,7 +699,7 @@ __device__ __forceinline__ void park_closest(const TraceParking& pk, uint32_t sl
     pk.hit[slot] = make_float4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.inst));
     pk.prim[slot] = t.h.prim;
     for (int k = 0; k < t.sp; k++)
-        pk.stack[(size_t)k * pk.cap + slot] = stack[k];
+        pk.stack[(size_t)k * pk.cap + slot] = stack.get(k);
 }
 
 // Restores a parked traversal of the ray (o, d, tmin): the same state the
@@ -690,7 +729,7 @@ __device__ __forceinline__ void resume_closest(const DevScene& s, const TracePar
     else
         t.r = t.world;
     for (int k = 0; k < t.sp; k++)
-        stack[k] = pk.stack[(size_t)k * pk.cap + slot];
+        stack.set(k, pk.stack[(size_t)k * pk.cap + slot]);
 }
 
 // Closest hit of one ray, traversed to the end.  Returns true on a hit.
@@ -854,7 +893,7 @@ __device__ __forceinline__ void shadow_begin(const DevScene& s, f3 o, f3 d, floa
     t.tmin = tmin;
     t.tmax = tmax;
     t.sp = 0;
-    stack[t.sp++] = REF_DONE;
+    stack.set(t.sp++, REF_DONE);
     t.ref = s.tlas_root == REF_EMPTY ? REF_DONE : s.tlas_root;
     t.in_blas = false;
     t.opaque = true;
@@ -882,7 +921,7 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
         PT_CHECK_INDEX((uint32_t)ref < s.node_count, s, return true)
         tc.nodes++;
         if (W4)
-            step4<STACK_SIZE, false>(s, t.r, t.tmin, t.tmax, t.ref, stack, t.sp);
+            step4<false>(s, t.r, t.tmin, t.tmax, t.ref, stack, t.sp);
         else
             step2(s, t.r, t.tmin, t.tmax, t.ref, stack, t.sp);
         return false;
@@ -892,7 +931,7 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
     if (ref == REF_EXIT_BLAS) {
         t.r = t.world;
         t.in_blas = false;
-        t.ref = stack[--t.sp];
+        t.ref = stack.get(--t.sp);
         return false;
     }
     const uint32_t first = leaf_first(ref), count = leaf_count(ref);
@@ -901,7 +940,7 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
         const DevInstance* di = s.dinst + first;
         const int root = __ldg(&di->blas_root);
         if (root == REF_EMPTY || count != 1) {
-            t.ref = stack[--t.sp];
+            t.ref = stack.get(--t.sp);
             return false;
         }
         const uint32_t flags = __ldg(&di->flags);
@@ -917,10 +956,10 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
         to_object(di, t.world.o, t.world.d, t.r);
         if (t.sp >= STACK_SIZE) {
             atomicOr(s.error_word, ERR_STACK_OVERFLOW);
-            t.ref = stack[--t.sp];
+            t.ref = stack.get(--t.sp);
             return false;
         }
-        stack[t.sp++] = REF_EXIT_BLAS;
+        stack.set(t.sp++, REF_EXIT_BLAS);
         t.in_blas = true;
         t.ref = root;
         return false;
@@ -947,7 +986,7 @@ __device__ __forceinline__ bool shadow_step(const DevScene& s, ShadowTrace& t, T
     }
     if (t.throughput == 0.0f || t.throughput < 1e-5f)
         return true;
-    t.ref = stack[--t.sp];
+    t.ref = stack.get(--t.sp);
     return false;
 }
 
@@ -965,7 +1004,7 @@ __device__ __forceinline__ void park_shadow(const TraceParking& pk, uint32_t slo
                                (int)t.inst, (int)t.iter);
     pk.hit[slot] = make_float4(t.throughput, t.alpha_pass, __uint_as_float(t.alpha_tex), 0.0f);
     for (int k = 0; k < t.sp; k++)
-        pk.stack[(size_t)k * pk.cap + slot] = stack[k];
+        pk.stack[(size_t)k * pk.cap + slot] = stack.get(k);
 }
 
 __device__ __forceinline__ void resume_shadow(const DevScene& s, const TraceParking& pk, uint32_t slot, f3 o, f3 d, float tmin,
@@ -994,7 +1033,7 @@ __device__ __forceinline__ void resume_shadow(const DevScene& s, const TracePark
     else
         t.r = t.world;
     for (int k = 0; k < t.sp; k++)
-        stack[k] = pk.stack[(size_t)k * pk.cap + slot];
+        stack.set(k, pk.stack[(size_t)k * pk.cap + slot]);
 }
 
 template <bool W4>
