@@ -230,11 +230,27 @@ def run_reference(args) -> None:
                                  "sample": runs[0]["sample"] + " per step; the reference's Vulkan tracer is unavailable "
                                                                "on this box (no graphics stack), so its CPU restatement "
                                                                "(the oracle) is timed"},
-                "e2e": {"value": v, "unit": "Mpath-segs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                "e2e": {"value": v, "unit": "Mpath-segs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "native_libraries": repo_libraries()}
         print(json.dumps(line), flush=True)
 
 
 METRIC = "time to MSE≤1e-3 vs FP64 ref: denoised vs plain (1 GB300); Mpath-segs/s"
+
+
+def repo_libraries() -> list:
+    """Shared objects of this repository mapped into this process (from
+    /proc/self/maps), relative to the repository root."""
+    found = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 6 and parts[-1].endswith(".so") and parts[-1].startswith(str(ROOT) + os.sep):
+                    found.add(os.path.relpath(parts[-1], ROOT))
+    except OSError:
+        pass
+    return sorted(found)
 
 
 def pinned_view(view):
@@ -872,6 +888,7 @@ def run_ours(args) -> None:
                 "gpu_launches": int(launches_per_step * args.steps),
                 "roofline": roof, "cpu_baseline": base, "clocks": clocks.summary(), "time_to_mse": ttm, "batch": batches,
                 "configs": configs,
+                "native_libraries": repo_libraries(),
                 "wall_s_timed_region": wall}
         print(json.dumps(line), flush=True)
     ctx.close()
