@@ -440,14 +440,18 @@ def time_to_mse_heavy(device_index: int, ref_spp: int = HEAVY["ref_spp"]) -> dic
            "reference": {"spp": ref_spp, "accumulation": "fp64 on the GPU", "seconds": round(ref_s, 3),
                          "mpath_segs_s": st.segments / st.milliseconds / 1e3}}
 
-    # plain: progressive search (untimed), then one timed render
+    # plain: progressive search (untimed), then one timed render.  The error
+    # times spp still falls between 32 and a few hundred spp here (early
+    # fireflies), so a 1/spp projection overshoots: each step covers half the
+    # projected distance (at least 8 spp), which ends within a few spp of the
+    # first sample count that reaches the threshold.
     n, m = 32, None
     ctx.render(params(32), stats=False)
     m = ctx.mse(ref32)
     trail = [(n, m)]
     while m > MSE_TARGET:
         proj = n * m / MSE_TARGET
-        step = int(min(512, max(8, round((proj - n) * 0.7))))
+        step = int(min(512, max(8, round((proj - n) * 0.5))))
         ctx.render(params(step, first=n), stats=False)
         n += step
         m = ctx.mse(ref32)
