@@ -410,6 +410,15 @@ def test_wavefront_many_waves(ctx, small, tmp_path):
     # 3 waves of raygen + accumulate and 4 segments of extend, extend resume, split,
     # shade, shadow, reset
     assert "launches" in r.stdout and int(r.stdout.split()[-1]) == 3 * (2 + 6 * 4)
+    # with the library's default threshold these 2^20-path waves run the
+    # extend in one pass: no resume launch, and the same image
+    out1 = tmp_path / "waves1.npy"
+    env1 = dict(env, PT_EXTEND_BUDGET_MIN_LOG2="25")
+    r1 = subprocess.run([sys.executable, "-c", _MANY_WAVES, str(tmp_path / "scene1"), str(out1)], env=env1, cwd=root,
+                        capture_output=True, text=True, timeout=600)
+    assert r1.returncode == 0, r1.stderr[-2000:]
+    assert int(r1.stdout.split()[-1]) == 3 * (2 + 5 * 4)
+    assert np.array_equal(np.load(out1).view(np.uint32), np.load(out).view(np.uint32))
     gpu = np.load(out)
     hs, view = small
     ctx.upload(view)
